@@ -1,0 +1,419 @@
+// ed_capi.cu — the extern "C" boundary (include/ed_hubbard.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/ed_hubbard.h"
+#include "ed_device.cuh"
+#include "ed_internal.hpp"
+
+namespace ed {
+ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, const double* start, int start_mem,
+                      double* evec, int evec_mem, double* alpha_h, double* beta_h, ed_lanczos_result* res,
+                      cudaStream_t s);
+void lanczos_free_ws(void* p);
+cudaError_t launch_random(double* f, int64_t n, uint64_t seed, cudaStream_t s);
+size_t tridiag_scratch_bytes(int n);
+cudaError_t launch_tridiag_lowest(int n, const double* alpha, const double* off, double* out, void* scratch,
+                                  cudaStream_t s);
+
+// ------------------------------------------------------- device rank/unrank --
+__global__ void k_unrank(const int64_t* __restrict__ ranks, int64_t count, uint64_t* __restrict__ words, int n_sites,
+                         int n_part, const int64_t* __restrict__ bt) {
+    const int kdim = n_part + 2;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t r = ranks[i];
+        uint64_t w = 0;
+        int p = n_sites - 1;
+        for (int k = n_part; k >= 1; --k) {
+            while (p >= 0 && bt[p * kdim + k] > r) --p;
+            if (p < 0) break;
+            w |= 1ULL << p;
+            r -= bt[p * kdim + k];
+            --p;
+        }
+        words[i] = w;
+    }
+}
+
+__global__ void k_rank(const uint64_t* __restrict__ words, int64_t count, int64_t* __restrict__ ranks, int n_sites,
+                       int n_part, const int64_t* __restrict__ bt) {
+    const int kdim = n_part + 2;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        uint64_t w = words[i];
+        if (__popcll(w) != n_part || (n_sites < 64 && (w >> n_sites))) {
+            ranks[i] = -1;
+            continue;
+        }
+        int64_t r = 0;
+        int k = 0;
+        while (w) {
+            const int p = __ffsll((long long)w) - 1;
+            r += bt[p * kdim + k + 1];
+            ++k;
+            w &= w - 1;
+        }
+        ranks[i] = r;
+    }
+}
+
+}  // namespace ed
+
+namespace {
+
+int ceil_log2(double x) {
+    if (!(x > 0.0)) return 0;
+    int k;
+    const double f = std::frexp(x, &k);  // x = f 2^k, f in [0.5, 1)
+    return f == 0.5 ? k - 1 : k;
+}
+
+int bitlen_u64h(uint64_t v) { return v ? 64 - __builtin_clzll(v) : 0; }
+
+struct OpExtra {
+    void* lz_ws = nullptr;
+};
+
+template <typename T>
+cudaError_t upload(T** dst, const T* src, size_t n) {
+    const size_t bytes = sizeof(T) * std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc(dst, bytes);
+    if (e != cudaSuccess) return e;
+    if (n) e = cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice);
+    return e;
+}
+
+}  // namespace
+
+// The Lanczos workspace pointer rides on the op (opaque to the header).
+struct ed_op_ext : ed_op {
+    OpExtra extra;
+};
+
+extern "C" {
+
+const char* ed_status_string(ed_status s) {
+    switch (s) {
+        case ED_OK: return "ok";
+        case ED_ERR_ARG: return "invalid argument";
+        case ED_ERR_CUDA: return "CUDA error";
+        case ED_ERR_ALLOC: return "allocation failed";
+        case ED_ERR_TABLE: return "table row overflows its slots";
+        case ED_ERR_RANGE: return "size beyond the supported range";
+        case ED_ERR_NONFINITE: return "non-finite value in an input vector";
+        case ED_ERR_BREAKDOWN: return "Lanczos breakdown (invariant subspace)";
+        case ED_ERR_NOT_CONVERGED: return "not converged";
+        case ED_ERR_TIMEOUT: return "bounded device wait gave up";
+        case ED_ERR_NOT_BUILT: return "feature not available";
+        default: return "unknown status";
+    }
+}
+
+int ed_version(void) { return 100; }
+
+int64_t ed_binom(int n, int k) { return ed::binom(n, k); }
+
+ed_status ed_basis_unrank(int n_sites, int n_part, const int64_t* ranks, int64_t count, uint64_t* words) {
+    if (n_sites < 1 || n_sites > 62 || n_part < 0 || n_part > n_sites || (count && (!ranks || !words)))
+        return ED_ERR_ARG;
+    ed::SpinBasis b;
+    b.n_sites = n_sites;
+    b.n_part = n_part;
+    b.count = ed::binom(n_sites, n_part);
+    const int kdim = n_part + 2;
+    b.binom_tab.assign((size_t)(n_sites + 1) * kdim, 0);
+    for (int p = 0; p <= n_sites; ++p)
+        for (int k = 0; k < kdim; ++k) b.binom_tab[(size_t)p * kdim + k] = ed::binom(p, k);
+    for (int64_t i = 0; i < count; ++i) {
+        if (ranks[i] < 0 || ranks[i] >= b.count) return ED_ERR_ARG;
+        words[i] = b.unrank(ranks[i]);
+    }
+    return ED_OK;
+}
+
+ed_status ed_basis_rank(int n_sites, int n_part, const uint64_t* words, int64_t count, int64_t* ranks) {
+    if (n_sites < 1 || n_sites > 62 || n_part < 0 || n_part > n_sites || (count && (!ranks || !words)))
+        return ED_ERR_ARG;
+    ed::SpinBasis b;
+    b.n_sites = n_sites;
+    b.n_part = n_part;
+    const int kdim = n_part + 2;
+    b.binom_tab.assign((size_t)(n_sites + 1) * kdim, 0);
+    for (int p = 0; p <= n_sites; ++p)
+        for (int k = 0; k < kdim; ++k) b.binom_tab[(size_t)p * kdim + k] = ed::binom(p, k);
+    ed_status st = ED_OK;
+    for (int64_t i = 0; i < count; ++i) {
+        ranks[i] = b.rank(words[i]);
+        if (ranks[i] < 0) st = ED_ERR_ARG;
+    }
+    return st;
+}
+
+static ed_status device_rank_common(int n_sites, int n_part, const void* in, int64_t count, void* out, void* stream,
+                                    bool rank) {
+    if (n_sites < 1 || n_sites > 62 || n_part < 0 || n_part > n_sites || (count && (!in || !out))) return ED_ERR_ARG;
+    if (count == 0) return ED_OK;
+    const int kdim = n_part + 2;
+    std::vector<int64_t> bt((size_t)(n_sites + 1) * kdim);
+    for (int p = 0; p <= n_sites; ++p)
+        for (int k = 0; k < kdim; ++k) bt[(size_t)p * kdim + k] = ed::binom(p, k);
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int64_t* d_bt = nullptr;
+    if (cudaMallocAsync(&d_bt, sizeof(int64_t) * bt.size(), s) != cudaSuccess) return ED_ERR_ALLOC;
+    cudaMemcpyAsync(d_bt, bt.data(), sizeof(int64_t) * bt.size(), cudaMemcpyHostToDevice, s);
+    int64_t blocks = (count + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (rank)
+        ed::k_rank<<<(int)blocks, 256, 0, s>>>(reinterpret_cast<const uint64_t*>(in), count,
+                                               reinterpret_cast<int64_t*>(out), n_sites, n_part, d_bt);
+    else
+        ed::k_unrank<<<(int)blocks, 256, 0, s>>>(reinterpret_cast<const int64_t*>(in), count,
+                                                 reinterpret_cast<uint64_t*>(out), n_sites, n_part, d_bt);
+    cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(d_bt, s);
+    return e == cudaSuccess ? ED_OK : ED_ERR_CUDA;
+}
+
+ed_status ed_basis_unrank_device(int n_sites, int n_part, const int64_t* ranks, int64_t count, uint64_t* words,
+                                 void* stream) {
+    return device_rank_common(n_sites, n_part, ranks, count, words, stream, false);
+}
+
+ed_status ed_basis_rank_device(int n_sites, int n_part, const uint64_t* words, int64_t count, int64_t* ranks,
+                               void* stream) {
+    return device_rank_common(n_sites, n_part, words, count, ranks, stream, true);
+}
+
+ed_status ed_tables_ell(int n_sites, int n_part, const ed_term* terms, int n_terms, double* ax, int64_t* aj,
+                        uint64_t* state) {
+    if (n_sites < 1 || n_sites > 62 || n_part < 0 || n_part > n_sites || (n_terms && !terms)) return ED_ERR_ARG;
+    for (int t = 0; t < n_terms; ++t)
+        if (terms[t].kind == ED_TERM_PEIERLS) return ED_ERR_ARG;
+    ed::SpinBasis b;
+    b.build(n_sites, n_part);
+    ed::SpinEll ell;
+    std::string err;
+    ed_status st = ed::build_spin(b, terms, n_terms, false, nullptr, &ell, &err);
+    if (st != ED_OK && st != ED_ERR_TABLE) return st;
+    if (ax) std::memcpy(ax, ell.ax.data(), sizeof(double) * ell.ax.size());
+    if (aj) std::memcpy(aj, ell.aj.data(), sizeof(int64_t) * ell.aj.size());
+    if (state) std::memcpy(state, b.state.data(), sizeof(uint64_t) * b.state.size());
+    return ell.overflow ? ED_ERR_TABLE : ED_OK;
+}
+
+ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
+    if (!out || !desc) return ED_ERR_ARG;
+    *out = nullptr;
+    const int N = desc->n_sites;
+    if (N < 1 || N > 62 || desc->n_up < 0 || desc->n_up > N || desc->n_dn < 0 || desc->n_dn > N) return ED_ERR_ARG;
+    if ((desc->n_up_terms && !desc->up_terms) || (desc->n_dn_terms && !desc->dn_terms)) return ED_ERR_ARG;
+    if (!std::isfinite(desc->U)) return ED_ERR_ARG;
+    const bool cplx = (desc->flags & ED_OP_COMPLEX) != 0;
+    ed_op_ext* op = new (std::nothrow) ed_op_ext();
+    if (!op) return ED_ERR_ALLOC;
+    op->device = device;
+    op->n_sites = N;
+    op->n_up = desc->n_up;
+    op->n_dn = desc->n_dn;
+    op->cplx = cplx;
+    op->U = desc->U;
+    const uint64_t all = (N >= 64) ? ~0ULL : ((1ULL << N) - 1ULL);
+    op->mask = desc->interaction_mask ? (desc->interaction_mask & all) : all;
+    op->bup.build(N, desc->n_up);
+    op->bdn.build(N, desc->n_dn);
+    op->dimUP = op->bup.count;
+    op->dimDN = op->bdn.count;
+    if (op->dimUP > (1LL << 24) || op->dimDN > (1LL << 24)) { delete op; return ED_ERR_RANGE; }
+    op->D = op->dimUP * op->dimDN;
+    std::string err;
+    ed_status st = ed::build_spin(op->bup, desc->up_terms, desc->n_up_terms, cplx, &op->tup, nullptr, &err);
+    if (st == ED_OK) st = ed::build_spin(op->bdn, desc->dn_terms, desc->n_dn_terms, cplx, &op->tdn, nullptr, &err);
+    if (st != ED_OK) { delete op; return st; }
+
+    // ---- fixed-point scale of the coefficients ----------------------------
+    const ed::SpinTable& tu = op->tup;
+    const ed::SpinTable& td = op->tdn;
+    double cmax = 0.0;
+    for (auto& c : tu.coef) cmax = std::max({cmax, std::fabs(c.real()), std::fabs(c.imag())});
+    for (auto& c : td.coef) cmax = std::max({cmax, std::fabs(c.real()), std::fabs(c.imag())});
+    double dmax_u = 0.0, dmax_d = 0.0;
+    for (double v : tu.diag_re) dmax_u = std::max(dmax_u, std::fabs(v));
+    for (double v : td.diag_re) dmax_d = std::max(dmax_d, std::fabs(v));
+    const int nU = std::min({desc->n_up, desc->n_dn, __builtin_popcountll(op->mask)});
+    const double diag_bound = dmax_u + dmax_d + std::fabs(desc->U) * nU;
+    const double Bc = std::max({cmax, diag_bound, 1e-300});
+    const int nterms = ((int)tu.coef.size() + (int)td.coef.size()) * (cplx ? 2 : 1) + 1;
+    const int extra = std::max(0, ceil_log2((double)nterms) - 4);
+    const int Fc = 61 - ceil_log2(Bc) - extra;
+    ed::MvArgs& a = op->mv;
+    std::memset(&a, 0, sizeof(a));
+    a.dimUP = op->dimUP;
+    a.dimDN = op->dimDN;
+    a.Fc = Fc;
+    a.mask = op->mask;
+    a.Uq = (int64_t)std::llrint(std::ldexp(desc->U, Fc));
+    a.nclsUP = (int)tu.coef.size();
+    a.nclsDN = (int)td.coef.size();
+    for (int c = 0; c < a.nclsUP; ++c) {
+        a.coefUP[2 * c] = (int64_t)std::llrint(std::ldexp(tu.coef[c].real(), Fc));
+        a.coefUP[2 * c + 1] = (int64_t)std::llrint(std::ldexp(tu.coef[c].imag(), Fc));
+    }
+    for (int c = 0; c < a.nclsDN; ++c) {
+        a.coefDN[2 * c] = (int64_t)std::llrint(std::ldexp(td.coef[c].real(), Fc));
+        a.coefDN[2 * c + 1] = (int64_t)std::llrint(std::ldexp(td.coef[c].imag(), Fc));
+    }
+    a.unitUP = (a.nclsUP == 1 && tu.coef[0] == std::complex<double>(1.0, 0.0)) ? 1 : 0;
+    a.unitDN = (a.nclsDN == 1 && td.coef[0] == std::complex<double>(1.0, 0.0)) ? 1 : 0;
+    a.mergeUD = (a.nclsUP == 1 && a.nclsDN == 1 && tu.coef[0] == td.coef[0]) ? 1 : 0;
+    if (a.nclsUP == 0 && a.nclsDN == 0) a.mergeUD = 0;
+    // |acc| <= (row sums + diagonal) * 2^Fc * max|x_q|
+    const double rowb = (tu.max_row_abs + td.max_row_abs) * (cplx ? 2.0 : 1.0) + diag_bound;
+    a.bq_bits = ceil_log2(std::ldexp(std::max(rowb, 1e-300), Fc) + 1.0) + 1;
+
+    // ---- device upload -------------------------------------------------------
+    if (cudaSetDevice(device) != cudaSuccess) { delete op; return ED_ERR_CUDA; }
+    std::vector<int64_t> dq_u(op->dimUP), dq_d(op->dimDN);
+    for (int64_t i = 0; i < op->dimUP; ++i) dq_u[i] = (int64_t)std::llrint(std::ldexp(tu.diag_re[i], Fc));
+    for (int64_t i = 0; i < op->dimDN; ++i) dq_d[i] = (int64_t)std::llrint(std::ldexp(td.diag_re[i], Fc));
+    bool ok = upload(&op->d_upEnt, tu.ent.data(), tu.ent.size()) == cudaSuccess &&
+              upload(&op->d_dnEnt, td.ent.data(), td.ent.size()) == cudaSuccess &&
+              upload(&op->d_upLen, tu.len.data(), tu.len.size()) == cudaSuccess &&
+              upload(&op->d_dnLen, td.len.data(), td.len.size()) == cudaSuccess &&
+              upload(&op->d_dUPq, dq_u.data(), dq_u.size()) == cudaSuccess &&
+              upload(&op->d_dDNq, dq_d.data(), dq_d.size()) == cudaSuccess &&
+              upload(&op->d_stUP, op->bup.state.data(), op->bup.state.size()) == cudaSuccess &&
+              upload(&op->d_stDN, op->bdn.state.data(), op->bdn.state.size()) == cudaSuccess &&
+              cudaMalloc(&op->d_emax, sizeof(int)) == cudaSuccess && cudaMalloc(&op->d_flag, sizeof(int)) == cudaSuccess;
+    if (!ok) { ed_op_destroy(op); return ED_ERR_ALLOC; }
+    a.upEnt = op->d_upEnt;
+    a.dnEnt = op->d_dnEnt;
+    a.upLen = op->d_upLen;
+    a.dnLen = op->d_dnLen;
+    a.dUPq = op->d_dUPq;
+    a.dDNq = op->d_dDNq;
+    a.stUP = op->d_stUP;
+    a.stDN = op->d_stDN;
+    const int W = cplx ? 2 : 1;
+    const int64_t row_bytes = op->dimDN * W * 8;
+    op->stage_smem = row_bytes <= 160 * 1024 ? (int)row_bytes : 0;
+    op->grid = ed::matvec_grid(op);
+    *out = op;
+    return ED_OK;
+}
+
+ed_status ed_op_destroy(ed_op* op) {
+    if (!op) return ED_OK;
+    cudaSetDevice(op->device);
+    ed_op_ext* ox = static_cast<ed_op_ext*>(op);
+    ed::lanczos_free_ws(ox->extra.lz_ws);
+    cudaFree(op->d_upEnt); cudaFree(op->d_dnEnt); cudaFree(op->d_upLen); cudaFree(op->d_dnLen);
+    cudaFree(op->d_dUPq); cudaFree(op->d_dDNq); cudaFree(op->d_stUP); cudaFree(op->d_stDN);
+    cudaFree(op->d_xq); cudaFree(op->d_emax); cudaFree(op->d_flag); cudaFree(op->d_io);
+    if (op->h_stage) cudaFreeHost(op->h_stage);
+    delete ox;
+    return ED_OK;
+}
+
+int64_t ed_op_rows(const ed_op* op) { return op ? op->D : 0; }
+int64_t ed_op_cols(const ed_op* op) { return op ? op->D : 0; }
+int64_t ed_op_dim_up(const ed_op* op) { return op ? op->dimUP : 0; }
+int64_t ed_op_dim_dn(const ed_op* op) { return op ? op->dimDN : 0; }
+int ed_op_is_complex(const ed_op* op) { return op && op->cplx ? 1 : 0; }
+
+ed_status ed_op_perform(ed_op* op, const double* x, double* y, int mem, void* stream) {
+    if (!op || !x || !y || (mem != ED_MEM_HOST && mem != ED_MEM_DEVICE)) return ED_ERR_ARG;
+    if (cudaSetDevice(op->device) != cudaSuccess) return ED_ERR_CUDA;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int W = op->cplx ? 2 : 1;
+    const int64_t DW = op->D * W;
+    if (!op->d_xq && cudaMalloc(&op->d_xq, sizeof(int64_t) * (size_t)DW) != cudaSuccess) return ED_ERR_ALLOC;
+    const double* dx = x;
+    double* dy = y;
+    if (mem == ED_MEM_HOST) {
+        const size_t need = sizeof(double) * (size_t)DW * 2;
+        if (op->d_io_bytes < need) {
+            cudaFree(op->d_io);
+            op->d_io = nullptr;
+            op->d_io_bytes = 0;
+            if (cudaMalloc(&op->d_io, need) != cudaSuccess) return ED_ERR_ALLOC;
+            op->d_io_bytes = need;
+        }
+        if (cudaMemcpyAsync(op->d_io, x, sizeof(double) * DW, cudaMemcpyHostToDevice, s) != cudaSuccess)
+            return ED_ERR_CUDA;
+        dx = op->d_io;
+        dy = op->d_io + DW;
+    }
+    if (ed::launch_emax(dx, DW, op->d_emax, op->d_flag, s) != cudaSuccess) return ED_ERR_CUDA;
+    if (ed::launch_to_fx(dx, DW, op->d_emax, op->d_xq, s) != cudaSuccess) return ED_ERR_CUDA;
+    cudaError_t e = ed::launch_matvec_f64(op, op->d_xq, op->d_emax, dy, s);
+    if (e != cudaSuccess) { op->last_error = cudaGetErrorString(e); return ED_ERR_CUDA; }
+    if (mem == ED_MEM_HOST) {
+        int flag = 0;
+        if (cudaMemcpyAsync(y, dy, sizeof(double) * DW, cudaMemcpyDeviceToHost, s) != cudaSuccess) return ED_ERR_CUDA;
+        if (cudaMemcpyAsync(&flag, op->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return ED_ERR_CUDA;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return ED_ERR_CUDA;
+        if (flag) return ED_ERR_NONFINITE;
+    }
+    return ED_OK;
+}
+
+ed_status ed_lanczos_run(ed_op* op, const ed_lanczos_cfg* cfg, const double* start, int start_mem, double* evec,
+                         int evec_mem, double* alpha, double* beta, ed_lanczos_result* res, void* stream) {
+    if (!op || !cfg) return ED_ERR_ARG;
+    if (cudaSetDevice(op->device) != cudaSuccess) return ED_ERR_CUDA;
+    ed_op_ext* ox = static_cast<ed_op_ext*>(op);
+    return ed::lanczos_run(op, &ox->extra.lz_ws, cfg, start, start_mem, evec, evec_mem, alpha, beta, res,
+                           reinterpret_cast<cudaStream_t>(stream));
+}
+
+ed_status ed_random_vector(int64_t n, uint64_t seed, double* out_host) {
+    if (n < 0 || (n && !out_host)) return ED_ERR_ARG;
+    for (int64_t b = 0; b * 4 < n; ++b) {
+        const ed::dev::Philox4 r = ed::dev::philox4x64_10((uint64_t)b, seed);
+        for (int w = 0; w < 4; ++w) {
+            const int64_t k = b * 4 + w;
+            if (k < n) out_host[k] = ed::dev::uniform_pm1(r.v[w]);
+        }
+    }
+    return ED_OK;
+}
+
+ed_status ed_random_vector_device(int64_t n, uint64_t seed, double* out_device, void* stream) {
+    if (n < 0 || (n && !out_device)) return ED_ERR_ARG;
+    if (n == 0) return ED_OK;
+    return ed::launch_random(out_device, n, seed, reinterpret_cast<cudaStream_t>(stream)) == cudaSuccess ? ED_OK
+                                                                                                       : ED_ERR_CUDA;
+}
+
+ed_status ed_tridiag_lowest(int n, const double* alpha, const double* offdiag, double* e0, double* z) {
+    if (n < 1 || !alpha || (n > 1 && !offdiag) || !e0) return ED_ERR_ARG;
+    double *d_a = nullptr, *d_o = nullptr, *d_out = nullptr;
+    void* scratch = nullptr;
+    ed_status st = ED_OK;
+    std::vector<double> out(n + 1);
+    if (cudaMalloc(&d_a, sizeof(double) * n) != cudaSuccess || cudaMalloc(&d_o, sizeof(double) * n) != cudaSuccess ||
+        cudaMalloc(&d_out, sizeof(double) * (n + 1)) != cudaSuccess ||
+        cudaMalloc(&scratch, ed::tridiag_scratch_bytes(n)) != cudaSuccess) {
+        st = ED_ERR_ALLOC;
+    } else {
+        cudaMemcpy(d_a, alpha, sizeof(double) * n, cudaMemcpyHostToDevice);
+        cudaMemset(d_o, 0, sizeof(double) * n);
+        if (n > 1) cudaMemcpy(d_o, offdiag, sizeof(double) * (n - 1), cudaMemcpyHostToDevice);
+        if (ed::launch_tridiag_lowest(n, d_a, d_o, d_out, scratch, 0) != cudaSuccess ||
+            cudaMemcpy(out.data(), d_out, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost) != cudaSuccess)
+            st = ED_ERR_CUDA;
+    }
+    cudaFree(d_a); cudaFree(d_o); cudaFree(d_out); cudaFree(scratch);
+    if (st == ED_OK) {
+        *e0 = out[0];
+        if (z) std::memcpy(z, out.data() + 1, sizeof(double) * n);
+    }
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,92 @@
+// ed_internal.hpp — the operator handle and the launchers behind the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "ed_tables.hpp"
+
+namespace ed {
+
+constexpr int kMaxCls = kMaxClasses;
+
+// Everything the matvec kernel needs, passed by value (< 4 KB).
+struct MvArgs {
+    const int64_t* xq;  // FX input, interleaved re,im when complex
+    int64_t dimUP, dimDN;
+    const uint32_t* upEnt;
+    const uint8_t* upLen;
+    const uint32_t* dnEnt;
+    const uint8_t* dnLen;
+    const int64_t* dUPq;  // folded diagonals, scale 2^-Fc
+    const int64_t* dDNq;
+    const uint64_t* stUP;
+    const uint64_t* stDN;
+    uint64_t mask;
+    int64_t Uq;           // U * 2^Fc
+    int Fc;
+    int nclsUP, nclsDN;
+    int unitUP, unitDN;   // single class with |coef| == 1 (coef_q == 2^Fc)
+    int mergeUD;          // single class each, equal coefficients
+    int bq_bits;          // bitlen of the per-unit row bound (acc <= 2^bq_bits * max|x_q|)
+    // output
+    double* y;            // FP64 output (perform path)
+    const int* p_emax;    // device: max biased exponent of the FP64 input
+    int64_t* uq;          // FX output (Lanczos path)
+    const uint64_t* p_mx; // device: max |x_q| of the FX input (Lanczos path)
+    // Lanczos per-step reduction outputs
+    void* lz;             // LzState* (device)
+    int step;
+    // coefficient classes, interleaved (re, im), scale 2^-Fc
+    int64_t coefUP[2 * kMaxCls];
+    int64_t coefDN[2 * kMaxCls];
+};
+
+}  // namespace ed
+
+struct ed_op {
+    int device = 0;
+    int n_sites = 0, n_up = 0, n_dn = 0;
+    bool cplx = false;
+    int64_t dimUP = 0, dimDN = 0, D = 0;
+    double U = 0.0;
+    uint64_t mask = 0;
+    ed::SpinBasis bup, bdn;
+    ed::SpinTable tup, tdn;
+    ed::MvArgs mv;  // static part of the matvec arguments
+    // device tables
+    uint32_t *d_upEnt = nullptr, *d_dnEnt = nullptr;
+    uint8_t *d_upLen = nullptr, *d_dnLen = nullptr;
+    int64_t *d_dUPq = nullptr, *d_dDNq = nullptr;
+    uint64_t *d_stUP = nullptr, *d_stDN = nullptr;
+    // perform-path workspace (grow-only)
+    int64_t* d_xq = nullptr;
+    int* d_emax = nullptr;
+    int* d_flag = nullptr;
+    double* h_stage = nullptr;  // pinned staging for host-pointer perform
+    size_t h_stage_bytes = 0;
+    double* d_io = nullptr;     // device x|y for host-pointer perform
+    size_t d_io_bytes = 0;
+    int stage_smem = 0;         // bytes of dynamic smem for the staged row (0 = no staging)
+    int grid = 0;               // matvec grid
+    std::string last_error;
+};
+
+namespace ed {
+
+// Launch-level API used by the C ABI and the Lanczos driver.
+cudaError_t launch_emax(const double* x, int64_t n, int* d_emax, int* d_flag, cudaStream_t s);
+cudaError_t launch_to_fx(const double* x, int64_t n, const int* d_emax, int64_t* xq, cudaStream_t s);
+// y = H x from the FX copy xq (exponent from d_emax), FP64 output.
+cudaError_t launch_matvec_f64(const ed_op* op, const int64_t* xq, const int* d_emax, double* y,
+                              cudaStream_t s);
+// u = H x in FX with the Lanczos-step epilogue (dot and max partials).
+// d_mx: device pointer to max|xq| (the Krylov slot's m entry).
+cudaError_t launch_matvec_lz(const ed_op* op, const int64_t* xq, int64_t* uq, void* lz,
+                             const uint64_t* d_mx, int step, cudaStream_t s);
+int matvec_grid(const ed_op* op);
+
+}  // namespace ed

@@ -1,0 +1,566 @@
+// ed_lanczos.cu — device-resident FX Lanczos (HubMatrix_GPU.cuh:477-613).
+//
+// One step = two launches:
+//   k_matvec<OUT=1>  u = H w_j (exact), alpha_j, axpy coefficients
+//   k_lz_axpy        w_{j+1} = a0 u + a1 w_j + a2 w_{j-1}, beta_{j+1}
+// Scalars never leave the device during the recurrence.  The Krylov vectors
+// are kept (ED_RITZ_STORED: one int64 vector per step, memory is plentiful
+// on this GPU) so the Ritz vector is a single weighted sum instead of the
+// reference's second Lanczos pass.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "ed_device.cuh"
+#include "ed_internal.hpp"
+#include "ed_lanczos.hpp"
+#include "ed_lanczos_dev.cuh"
+
+namespace ed {
+using namespace dev;
+
+size_t tridiag_scratch_bytes(int n);
+cudaError_t launch_tridiag_lowest(int n, const double* alpha, const double* off, double* out, void* scratch,
+                                  cudaStream_t s);
+
+constexpr int kLzThreads = 256;
+
+static int lz_grid(int64_t n) {
+    int64_t g = (n + 2 * kLzThreads - 1) / (2 * kLzThreads);
+    if (g > 152 * 8) g = 152 * 8;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// ------------------------------------------------------------------ kernels --
+
+__global__ void k_random(double* __restrict__ f, int64_t n, uint64_t seed) {
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b * 4 < n; b += (int64_t)gridDim.x * blockDim.x) {
+        const Philox4 r = philox4x64_10((uint64_t)b, seed);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            const int64_t k = b * 4 + w;
+            if (k < n) f[k] = uniform_pm1(r.v[w]);
+        }
+    }
+}
+
+template <typename Fin>
+__device__ __forceinline__ void lz_reduce_tail(i128 ss, uint64_t mx, LzState* lz, int ctr, Fin fin) {
+    __shared__ i128 s128[32];
+    __shared__ uint64_t s64[32];
+    const i128 bs = block_sum_i128(ss, s128);
+    const uint64_t bm = block_max_u64(mx, s64);
+    if (threadIdx.x == 0) {
+        lz->part_lo[blockIdx.x] = (uint64_t)bs;
+        lz->part_hi[blockIdx.x] = (uint64_t)((u128)bs >> 64);
+        lz->part_max[blockIdx.x] = bm;
+    }
+    if (elect_last_block(&lz->counter[ctr])) {
+        i128 s = 0;
+        uint64_t m = 0;
+        for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
+            s += (i128)(((u128)lz->part_hi[i] << 64) | lz->part_lo[i]);
+            m = lz->part_max[i] > m ? lz->part_max[i] : m;
+        }
+        s = block_sum_i128(s, s128);
+        m = block_max_u64(m, s64);
+        if (threadIdx.x == 0) {
+            fin(s, m);
+            lz->counter[ctr] = 0;
+        }
+    }
+}
+
+// FP64 start vector -> FX slot 0, |f| and max|q|.
+__global__ void __launch_bounds__(kLzThreads) k_lz_start(const double* __restrict__ f, int64_t n, const int* emax,
+                                                         const int* flag, int64_t* __restrict__ q0, LzState* lz) {
+    const int E = fx_exp_from_emax(*emax);
+    i128 ss = 0;
+    uint64_t mx = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t q = f64_to_fx(f[i], E);
+        q0[i] = q;
+        ss += mul_wide(q, q) >> 16;
+        const uint64_t a = (uint64_t)(q < 0 ? -q : q);
+        mx = a > mx ? a : mx;
+    }
+    lz_reduce_tail(ss, mx, lz, 2, [&](i128 s, uint64_t m) {
+        lz->e[0] = E;
+        lz->m[0] = m;
+        lz->beta[0] = sqrt(i128_to_f64(s, 2 * E + 16));
+        lz->min_bits = bitlen_u64(m);
+        lz->status = (*flag) ? 6 : (m == 0 ? 7 : 0);
+        lz->steps_done = 0;
+    });
+}
+
+// w_{j+1} = round((at0 u >> sh0 + at1 x >> sh1 + at2 p >> sh2) / 2^Fa)
+__global__ void __launch_bounds__(kLzThreads) k_lz_axpy(const int64_t* __restrict__ uq, const int64_t* __restrict__ xq,
+                                                        const int64_t* __restrict__ pq, int64_t* __restrict__ wq,
+                                                        int64_t n, LzState* lz, int j) {
+    const int64_t a0 = lz->at[0], a1 = lz->at[1], a2 = lz->at[2];
+    const int s0 = lz->sh[0], s1 = lz->sh[1], s2 = lz->sh[2], Fa = lz->Fa;
+    i128 ss = 0;
+    uint64_t mx = 0;
+    const int64_t npair = n >> 1;
+    const longlong2* u2 = reinterpret_cast<const longlong2*>(uq);
+    const longlong2* x2 = reinterpret_cast<const longlong2*>(xq);
+    const longlong2* p2 = reinterpret_cast<const longlong2*>(pq);
+    longlong2* w2 = reinterpret_cast<longlong2*>(wq);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npair; i += (int64_t)gridDim.x * blockDim.x) {
+        const longlong2 u = u2[i], x = x2[i], p = p2[i];
+        const i128 accx = (mul_wide(a0, u.x) >> s0) + (mul_wide(a1, x.x) >> s1) + (mul_wide(a2, p.x) >> s2);
+        const i128 accy = (mul_wide(a0, u.y) >> s0) + (mul_wide(a1, x.y) >> s1) + (mul_wide(a2, p.y) >> s2);
+        longlong2 w;
+        w.x = (int64_t)shr_round(accx, Fa);
+        w.y = (int64_t)shr_round(accy, Fa);
+        w2[i] = w;
+        ss += (mul_wide(w.x, w.x) >> 16) + (mul_wide(w.y, w.y) >> 16);
+        const uint64_t ax = (uint64_t)(w.x < 0 ? -w.x : w.x), ay = (uint64_t)(w.y < 0 ? -w.y : w.y);
+        mx = ax > mx ? ax : mx;
+        mx = ay > mx ? ay : mx;
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const int64_t i = n - 1;
+        const i128 acc = (mul_wide(a0, uq[i]) >> s0) + (mul_wide(a1, xq[i]) >> s1) + (mul_wide(a2, pq[i]) >> s2);
+        const int64_t w = (int64_t)shr_round(acc, Fa);
+        wq[i] = w;
+        ss += mul_wide(w, w) >> 16;
+        const uint64_t a = (uint64_t)(w < 0 ? -w : w);
+        mx = a > mx ? a : mx;
+    }
+    lz_reduce_tail(ss, mx, lz, 1, [&](i128 s, uint64_t m) { lz_after_axpy(lz, j, s, m); });
+}
+
+// |w|^2 and max|w| of slot j (after reorthogonalisation changed it).
+__global__ void __launch_bounds__(kLzThreads) k_lz_stats(const int64_t* __restrict__ wq, int64_t n, LzState* lz, int j) {
+    i128 ss = 0;
+    uint64_t mx = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t w = wq[i];
+        ss += mul_wide(w, w) >> 16;
+        const uint64_t a = (uint64_t)(w < 0 ? -w : w);
+        mx = a > mx ? a : mx;
+    }
+    lz_reduce_tail(ss, mx, lz, 3, [&](i128 s, uint64_t m) {
+        const int e = lz->e[j];
+        lz->m[j] = m;
+        lz->beta[j] = sqrt(i128_to_f64(s, 2 * e + 16));
+        const int bits = bitlen_u64(m);
+        if (bits < lz->min_bits) lz->min_bits = bits;
+        if (m == 0 && lz->status == 0) lz->status = 7;
+    });
+}
+
+// partial[k * gridDim.y + c] = sum over chunk c of (q_k q_w) >> 24, exact.
+__global__ void __launch_bounds__(kLzThreads) k_lz_dots(const int64_t* __restrict__ basis, int64_t n,
+                                                        const int64_t* __restrict__ w, uint64_t* part_lo,
+                                                        uint64_t* part_hi) {
+    const int k = blockIdx.x;
+    const int c = blockIdx.y, nc = gridDim.y;
+    const int64_t* q = basis + (int64_t)k * n;
+    i128 s = 0;
+    for (int64_t i = (int64_t)c * blockDim.x + threadIdx.x; i < n; i += (int64_t)nc * blockDim.x)
+        s += mul_wide(q[i], w[i]) >> 24;
+    __shared__ i128 s128[32];
+    s = block_sum_i128(s, s128);
+    if (threadIdx.x == 0) {
+        part_lo[k * nc + c] = (uint64_t)s;
+        part_hi[k * nc + c] = (uint64_t)((u128)s >> 64);
+    }
+}
+
+// w <- w - round(sum_k (rt_k q_k >> rs_k) / 2^F)
+__global__ void __launch_bounds__(kLzThreads) k_lz_reorth(int64_t* __restrict__ w, const int64_t* __restrict__ basis,
+                                                          int64_t n, int nk, const int64_t* __restrict__ rt,
+                                                          const int* __restrict__ rs, int F) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        i128 acc = 0;
+        for (int k = 0; k < nk; ++k) acc += mul_wide(rt[k], basis[(int64_t)k * n + i]) >> rs[k];
+        w[i] -= (int64_t)shr_round(acc, F);
+    }
+}
+
+// evec = sum_k (rt_k q_k >> rs_k) * 2^-F as FP64, plus |evec|^2 partials.
+__global__ void __launch_bounds__(kLzThreads) k_ritz(const int64_t* __restrict__ basis, int64_t n, int nk,
+                                                     const int64_t* __restrict__ rt, const int* __restrict__ rs, int F,
+                                                     double* __restrict__ out, double* __restrict__ part,
+                                                     unsigned int* counter, double* inv_norm) {
+    double ss = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        i128 acc = 0;
+        for (int k = 0; k < nk; ++k) acc += mul_wide(rt[k], basis[(int64_t)k * n + i]) >> rs[k];
+        const double v = i128_to_f64(acc, -F);
+        out[i] = v;
+        ss = fma(v, v, ss);
+    }
+    __shared__ double sd[32];
+    const double bs = block_sum_f64(ss, sd);
+    if (threadIdx.x == 0) part[blockIdx.x] = bs;
+    if (elect_last_block(counter)) {
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int i = 0; i < (int)gridDim.x; ++i) t += part[i];
+            *inv_norm = t > 0.0 ? 1.0 / sqrt(t) : 0.0;
+            *counter = 0;
+        }
+    }
+}
+
+__global__ void k_scale(double* __restrict__ v, int64_t n, const double* __restrict__ s) {
+    const double f = *s;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] *= f;
+}
+
+// ------------------------------------------------------------------- host --
+
+cudaError_t launch_random(double* f, int64_t n, uint64_t seed, cudaStream_t s) {
+    int64_t blocks = ((n + 3) / 4 + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    if (blocks < 1) blocks = 1;
+    k_random<<<(int)blocks, 256, 0, s>>>(f, n, seed);
+    return cudaGetLastError();
+}
+
+namespace {
+
+struct Workspace {
+    int device = -1;
+    size_t basis_slots = 0;
+    int64_t DW = 0;
+    int max_steps = 0;
+    int64_t* basis = nullptr;
+    int64_t* u = nullptr;
+    double* fbuf = nullptr;
+    LzState* lz = nullptr;  // device struct
+    LzState h;              // host mirror (pointers)
+    int* emax = nullptr;
+    int* flag = nullptr;
+    void* tri_scratch = nullptr;
+    double* tri_out = nullptr;
+    double* offd = nullptr;
+    uint64_t* dot_lo = nullptr;
+    uint64_t* dot_hi = nullptr;
+    int64_t* coef_rt = nullptr;
+    int* coef_rs = nullptr;
+    double* ritz_part = nullptr;
+    unsigned int* ritz_ctr = nullptr;
+    double* inv_norm = nullptr;
+    std::vector<cudaEvent_t> events;  // profiling pool (pairs)
+};
+
+#define LZ_CK(x)                                    \
+    do {                                            \
+        cudaError_t e_ = (x);                       \
+        if (e_ != cudaSuccess) {                    \
+            op->last_error = cudaGetErrorString(e_); \
+            return ED_ERR_CUDA;                     \
+        }                                           \
+    } while (0)
+
+void free_ws(Workspace* w) {
+    cudaFree(w->basis); cudaFree(w->u); cudaFree(w->fbuf); cudaFree(w->lz);
+    cudaFree(w->h.e); cudaFree(w->h.m); cudaFree(w->h.beta); cudaFree(w->h.alpha);
+    cudaFree(w->h.part_lo); cudaFree(w->h.part_hi); cudaFree(w->h.part_max); cudaFree(w->h.counter);
+    cudaFree(w->emax); cudaFree(w->flag); cudaFree(w->tri_scratch); cudaFree(w->tri_out); cudaFree(w->offd);
+    cudaFree(w->dot_lo); cudaFree(w->dot_hi); cudaFree(w->coef_rt); cudaFree(w->coef_rs);
+    cudaFree(w->ritz_part); cudaFree(w->ritz_ctr); cudaFree(w->inv_norm);
+    for (cudaEvent_t e : w->events) cudaEventDestroy(e);
+    *w = Workspace();
+}
+
+constexpr int kMaxPartials = 152 * 16;
+constexpr int kDotChunks = 64;
+
+ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_steps) {
+    if (w->basis && w->basis_slots >= slots && w->DW == DW && w->max_steps >= max_steps) return ED_OK;
+    free_ws(w);
+    w->device = op->device;
+    w->basis_slots = slots;
+    w->DW = DW;
+    w->max_steps = max_steps;
+    const size_t ns = (size_t)max_steps + 2;
+    LZ_CK(cudaMalloc(&w->basis, sizeof(int64_t) * slots * (size_t)DW));
+    LZ_CK(cudaMalloc(&w->u, sizeof(int64_t) * (size_t)DW));
+    LZ_CK(cudaMalloc(&w->fbuf, sizeof(double) * (size_t)DW));
+    LZ_CK(cudaMalloc(&w->lz, sizeof(LzState)));
+    std::memset(&w->h, 0, sizeof(LzState));
+    LZ_CK(cudaMalloc(&w->h.e, sizeof(int) * ns));
+    LZ_CK(cudaMalloc(&w->h.m, sizeof(uint64_t) * ns));
+    LZ_CK(cudaMalloc(&w->h.beta, sizeof(double) * ns));
+    LZ_CK(cudaMalloc(&w->h.alpha, sizeof(double) * ns));
+    LZ_CK(cudaMalloc(&w->h.part_lo, sizeof(uint64_t) * kMaxPartials));
+    LZ_CK(cudaMalloc(&w->h.part_hi, sizeof(uint64_t) * kMaxPartials));
+    LZ_CK(cudaMalloc(&w->h.part_max, sizeof(uint64_t) * kMaxPartials));
+    LZ_CK(cudaMalloc(&w->h.counter, sizeof(unsigned int) * 4));
+    LZ_CK(cudaMemset(w->h.counter, 0, sizeof(unsigned int) * 4));
+    LZ_CK(cudaMalloc(&w->emax, sizeof(int)));
+    LZ_CK(cudaMalloc(&w->flag, sizeof(int)));
+    LZ_CK(cudaMalloc(&w->tri_scratch, tridiag_scratch_bytes((int)ns)));
+    LZ_CK(cudaMalloc(&w->tri_out, sizeof(double) * (ns + 1)));
+    LZ_CK(cudaMalloc(&w->offd, sizeof(double) * ns));
+    LZ_CK(cudaMalloc(&w->dot_lo, sizeof(uint64_t) * ns * kDotChunks));
+    LZ_CK(cudaMalloc(&w->dot_hi, sizeof(uint64_t) * ns * kDotChunks));
+    LZ_CK(cudaMalloc(&w->coef_rt, sizeof(int64_t) * ns));
+    LZ_CK(cudaMalloc(&w->coef_rs, sizeof(int) * ns));
+    LZ_CK(cudaMalloc(&w->ritz_part, sizeof(double) * kMaxPartials));
+    LZ_CK(cudaMalloc(&w->ritz_ctr, sizeof(unsigned int)));
+    LZ_CK(cudaMemset(w->ritz_ctr, 0, sizeof(unsigned int)));
+    LZ_CK(cudaMalloc(&w->inv_norm, sizeof(double)));
+    LZ_CK(cudaMemcpy(w->lz, &w->h, sizeof(LzState), cudaMemcpyHostToDevice));
+    return ED_OK;
+}
+
+// Integer coefficients rt_k, shifts rs_k and common fractional bits F for
+// sum_k r_k q_k with real r_k (|q_k| < 2^54, at most 2^10 terms per 2^126).
+void fx_coefs(const std::vector<double>& r, std::vector<int64_t>* rt, std::vector<int>* rs, int* Fout) {
+    const int nk = (int)r.size();
+    int extra = 0;
+    while ((1 << (10 + extra)) < nk) ++extra;
+    std::vector<int> F(nk, 0);
+    int Fmin = 1 << 20;
+    for (int k = 0; k < nk; ++k) {
+        if (r[k] == 0.0) continue;
+        int ka;
+        std::frexp(std::fabs(r[k]), &ka);
+        F[k] = 62 - ka - extra;
+        Fmin = std::min(Fmin, F[k]);
+    }
+    if (Fmin == (1 << 20)) Fmin = 0;
+    rt->assign(nk, 0);
+    rs->assign(nk, 0);
+    for (int k = 0; k < nk; ++k) {
+        if (r[k] == 0.0 || F[k] - Fmin >= 120) continue;
+        (*rt)[k] = (int64_t)std::llrint(std::ldexp(r[k], F[k]));
+        (*rs)[k] = F[k] - Fmin;
+    }
+    *Fout = Fmin;
+}
+
+}  // namespace
+
+}  // namespace ed
+
+namespace ed {
+namespace {
+// The workspace hangs off the op handle through an opaque pointer so the
+// allocation survives across runs (no cudaMalloc inside a timed solve).
+struct WsHolder {
+    Workspace ws;
+};
+}  // namespace
+
+void lanczos_free_ws(void* p) {
+    if (!p) return;
+    WsHolder* h = reinterpret_cast<WsHolder*>(p);
+    free_ws(&h->ws);
+    delete h;
+}
+
+ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, const double* start, int start_mem,
+                      double* evec, int evec_mem, double* alpha_h, double* beta_h, ed_lanczos_result* res,
+                      cudaStream_t s) {
+    if (!cfg || cfg->max_steps < 1 || cfg->max_steps > 100000) return ED_ERR_ARG;
+    const int W = op->cplx ? 2 : 1;
+    const int64_t DW = op->D * W;
+    const int max_steps = cfg->max_steps;
+    const bool stored = cfg->ritz == ED_RITZ_STORED || cfg->reorth;
+    if (cfg->ritz == ED_RITZ_RECOMPUTE) return ED_ERR_NOT_BUILT;
+    const size_t slots = stored ? (size_t)max_steps + 1 : 3;
+    if (!*ws_slot) *ws_slot = new WsHolder();
+    Workspace* w = &reinterpret_cast<WsHolder*>(*ws_slot)->ws;
+    ed_status st = ensure_ws(op, w, slots, DW, max_steps);
+    if (st != ED_OK) return st;
+    LzState* lz = w->lz;
+    const LzState& H = w->h;
+    int64_t launches = 0;
+    const bool prof = cfg->profile != 0;
+    const size_t need_ev = prof ? (size_t)4 * max_steps : 0;
+    while (w->events.size() < need_ev) {
+        cudaEvent_t e;
+        LZ_CK(cudaEventCreate(&e));
+        w->events.push_back(e);
+    }
+    auto slot = [&](int j) -> int64_t* { return w->basis + (size_t)(stored ? j : j % 3) * (size_t)DW; };
+
+    // start vector
+    if (cfg->start == ED_START_USER) {
+        if (!start) return ED_ERR_ARG;
+        LZ_CK(cudaMemcpyAsync(w->fbuf, start, sizeof(double) * DW,
+                              start_mem == ED_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    } else {
+        LZ_CK(launch_random(w->fbuf, DW, cfg->seed, s));
+        ++launches;
+    }
+    LZ_CK(launch_emax(w->fbuf, DW, w->emax, w->flag, s));
+    k_lz_start<<<lz_grid(DW), kLzThreads, 0, s>>>(w->fbuf, DW, w->emax, w->flag, slot(0), lz);
+    LZ_CK(cudaGetLastError());
+    launches += 2;
+
+    const double eps = 2.220446049250313e-16;
+    const double tolconv = 0.01 * std::sqrt(eps);
+    std::vector<double> ha(max_steps + 2), hb(max_steps + 2);
+    int n = max_steps;
+    bool converged = false;
+    double e0 = 0.0, resid = 0.0;
+    std::vector<double> tri(max_steps + 2);
+    int status_dev = 0;
+
+    int steps_run = 0;
+    for (int j = 0; j < max_steps; ++j) {
+        if (prof) LZ_CK(cudaEventRecord(w->events[4 * j], s));
+        LZ_CK(launch_matvec_lz(op, slot(j), w->u, lz, H.m + j, j, s));
+        if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 1], s));
+        const int64_t* pj = j > 0 ? slot(j - 1) : slot(j);
+        if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 2], s));
+        k_lz_axpy<<<lz_grid(DW), kLzThreads, 0, s>>>(w->u, slot(j), pj, slot(j + 1), DW, lz, j);
+        LZ_CK(cudaGetLastError());
+        if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 3], s));
+        launches += 2;
+        steps_run = j + 1;
+        if (cfg->reorth) {
+            // classical Gram-Schmidt, twice, against v_0..v_j
+            const int nk = j + 1;
+            for (int pass = 0; pass < 2; ++pass) {
+                dim3 g(nk, kDotChunks);
+                k_lz_dots<<<g, kLzThreads, 0, s>>>(w->basis, DW, slot(j + 1), w->dot_lo, w->dot_hi);
+                LZ_CK(cudaGetLastError());
+                std::vector<uint64_t> lo((size_t)nk * kDotChunks), hi((size_t)nk * kDotChunks);
+                std::vector<int> ev(nk + 2);
+                std::vector<double> bv(nk + 2);
+                LZ_CK(cudaMemcpyAsync(lo.data(), w->dot_lo, sizeof(uint64_t) * lo.size(), cudaMemcpyDeviceToHost, s));
+                LZ_CK(cudaMemcpyAsync(hi.data(), w->dot_hi, sizeof(uint64_t) * hi.size(), cudaMemcpyDeviceToHost, s));
+                LZ_CK(cudaMemcpyAsync(ev.data(), H.e, sizeof(int) * (nk + 1), cudaMemcpyDeviceToHost, s));
+                LZ_CK(cudaMemcpyAsync(bv.data(), H.beta, sizeof(double) * (nk + 1), cudaMemcpyDeviceToHost, s));
+                LZ_CK(cudaStreamSynchronize(s));
+                const int ew = ev[nk];
+                std::vector<double> r(nk);
+                for (int k = 0; k < nk; ++k) {
+                    __int128 acc = 0;
+                    for (int c = 0; c < kDotChunks; ++c)
+                        acc += (__int128)(((unsigned __int128)hi[(size_t)k * kDotChunks + c] << 64) |
+                                          lo[(size_t)k * kDotChunks + c]);
+                    // <w_k, w> = acc 2^(e_k + e_w + 24); coefficient on q_k in
+                    // units of w's exponent: <w_k,w>/beta_k^2 * 2^(e_k - e_w)
+                    const double dotv = std::ldexp((double)acc, ev[k] + ew + 24);
+                    r[k] = dotv / (bv[k] * bv[k]) * std::ldexp(1.0, ev[k] - ew);
+                }
+                std::vector<int64_t> rt;
+                std::vector<int> rs;
+                int F;
+                fx_coefs(r, &rt, &rs, &F);
+                LZ_CK(cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * nk, cudaMemcpyHostToDevice, s));
+                LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * nk, cudaMemcpyHostToDevice, s));
+                k_lz_reorth<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), w->basis, DW, nk, w->coef_rt, w->coef_rs, F);
+                LZ_CK(cudaGetLastError());
+                launches += 2;
+            }
+            k_lz_stats<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), DW, lz, j + 1);
+            LZ_CK(cudaGetLastError());
+            ++launches;
+        }
+        if (cfg->mode == ED_LANCZOS_REFERENCE && j % 10 == 9) {
+            const int nn = j + 1;
+            LZ_CK(cudaMemcpyAsync(ha.data(), H.alpha, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
+            LZ_CK(cudaMemcpyAsync(hb.data(), H.beta, sizeof(double) * (nn + 1), cudaMemcpyDeviceToHost, s));
+            LZ_CK(cudaMemcpyAsync(&status_dev, &lz->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+            LZ_CK(cudaStreamSynchronize(s));
+            if (status_dev != 0) { n = nn; break; }
+            double anorm = std::fabs(ha[0] + hb[1]);
+            for (int k = 1; k < nn; ++k) anorm = std::max(anorm, hb[k] + std::fabs(ha[k] + hb[k + 1]));
+            LZ_CK(cudaMemcpyAsync(w->offd, H.beta + 1, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
+            LZ_CK(launch_tridiag_lowest(nn, H.alpha, w->offd, w->tri_out, w->tri_scratch, s));
+            launches += 12;
+            LZ_CK(cudaMemcpyAsync(tri.data(), w->tri_out, sizeof(double) * (nn + 1), cudaMemcpyDeviceToHost, s));
+            LZ_CK(cudaStreamSynchronize(s));
+            e0 = tri[0];
+            if (std::fabs(hb[nn] * tri[nn]) < tolconv * anorm && std::fabs(tri[1]) > tolconv * anorm) {
+                converged = true;
+                n = nn;
+                break;
+            }
+        }
+    }
+
+    // final T, status
+    LzState hs;
+    LZ_CK(cudaMemcpyAsync(&hs, lz, sizeof(LzState), cudaMemcpyDeviceToHost, s));
+    LZ_CK(cudaMemcpyAsync(ha.data(), H.alpha, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    LZ_CK(cudaMemcpyAsync(hb.data(), H.beta, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost, s));
+    LZ_CK(cudaStreamSynchronize(s));
+    int status = hs.status;
+    if (status == 7) {
+        // breakdown: T is exact up to the first vanishing beta
+        int nb = n;
+        for (int k = 0; k < n; ++k)
+            if (hb[k + 1] == 0.0) { nb = k + 1; break; }
+        n = std::max(1, nb);
+    } else if (status != 0) {
+        return ED_ERR_NONFINITE;
+    }
+    LZ_CK(cudaMemcpyAsync(w->offd, H.beta + 1, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
+    LZ_CK(launch_tridiag_lowest(n, H.alpha, w->offd, w->tri_out, w->tri_scratch, s));
+    launches += 12;
+    LZ_CK(cudaMemcpyAsync(tri.data(), w->tri_out, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost, s));
+    LZ_CK(cudaStreamSynchronize(s));
+    e0 = tri[0];
+    resid = std::fabs(hb[n] * tri[n]);
+
+    if (evec && cfg->ritz == ED_RITZ_STORED) {
+        std::vector<int> ev(n);
+        std::vector<uint64_t> mv(n);
+        LZ_CK(cudaMemcpyAsync(ev.data(), H.e, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+        LZ_CK(cudaStreamSynchronize(s));
+        std::vector<double> r(n);
+        for (int k = 0; k < n; ++k) r[k] = tri[1 + k] / hb[k] * std::ldexp(1.0, ev[k]);
+        std::vector<int64_t> rt;
+        std::vector<int> rs;
+        int F;
+        fx_coefs(r, &rt, &rs, &F);
+        LZ_CK(cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+        LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+        double* out = evec_mem == ED_MEM_DEVICE ? evec : w->fbuf;
+        const int g = lz_grid(DW);
+        k_ritz<<<g, kLzThreads, 0, s>>>(w->basis, DW, n, w->coef_rt, w->coef_rs, F, out, w->ritz_part, w->ritz_ctr,
+                                        w->inv_norm);
+        LZ_CK(cudaGetLastError());
+        k_scale<<<g, kLzThreads, 0, s>>>(out, DW, w->inv_norm);
+        LZ_CK(cudaGetLastError());
+        launches += 2;
+        if (evec_mem != ED_MEM_DEVICE)
+            LZ_CK(cudaMemcpyAsync(evec, out, sizeof(double) * DW, cudaMemcpyDeviceToHost, s));
+        LZ_CK(cudaStreamSynchronize(s));
+    }
+    if (alpha_h) std::memcpy(alpha_h, ha.data(), sizeof(double) * n);
+    if (beta_h) std::memcpy(beta_h, hb.data(), sizeof(double) * (n + 1));
+    double mv_ms = 0.0, ax_ms = 0.0;
+    if (prof) {
+        LZ_CK(cudaStreamSynchronize(s));
+        for (int j = 0; j < steps_run; ++j) {
+            float a = 0.f, b = 0.f;
+            LZ_CK(cudaEventElapsedTime(&a, w->events[4 * j], w->events[4 * j + 1]));
+            LZ_CK(cudaEventElapsedTime(&b, w->events[4 * j + 2], w->events[4 * j + 3]));
+            mv_ms += a;
+            ax_ms += b;
+        }
+    }
+    if (res) {
+        res->launches = launches;
+        res->matvec_ms = mv_ms;
+        res->axpy_ms = ax_ms;
+        res->n_matvec = steps_run;
+        res->e0 = e0;
+        res->steps = n;
+        res->converged = converged ? 1 : 0;
+        res->status = status == 7 ? ED_ERR_BREAKDOWN : ED_OK;
+        res->min_bits = hs.min_bits;
+        res->residual = resid;
+    }
+    return ED_OK;
+}
+
+}  // namespace ed

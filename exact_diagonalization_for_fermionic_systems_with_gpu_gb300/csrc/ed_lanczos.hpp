@@ -1,0 +1,38 @@
+// ed_lanczos.hpp — device-resident state of one Lanczos run.
+//
+// The Lanczos vectors are kept unnormalised (w_j, |w_j| = beta_j) in FX
+// format, one exponent per vector; v_j = w_j / beta_j is never formed.  All
+// scalar bookkeeping (alpha_j, beta_j, exponents, the integer coefficients
+// of the next axpy) happens on the device in the last block of each
+// reduction, so a step is two kernel launches with no host round trip.
+#pragma once
+
+#include <cstdint>
+
+namespace ed {
+
+struct LzState {
+    // per Krylov slot j (device arrays of length max_steps + 2)
+    int* e;          // exponent: w_j[i] = q_j[i] * 2^e[j]
+    uint64_t* m;     // max |q_j[i]|
+    double* beta;    // beta[j] = |w_j|; beta[0] = |start vector|
+    double* alpha;   // alpha[j] = <v_j, H v_j>
+    // grid-reduction partials, one entry per block
+    uint64_t* part_lo;
+    uint64_t* part_hi;
+    uint64_t* part_max;
+    unsigned int* counter;  // [4] last-block counters (matvec, axpy, start, misc)
+    // current step scalars
+    int s_u;         // right shift applied to the exact matvec accumulator
+    int e_u;         // exponent of u = H w_j
+    uint64_t m_u;    // max |u_q|
+    int Fa;          // fractional bits of the axpy coefficients
+    int e_w;         // exponent of w_{j+1}
+    int64_t at[3];   // integer axpy coefficients (u, w_j, w_{j-1})
+    int sh[3];       // extra right shift of each product to the common Fa
+    int status;      // 0 ok, 7 breakdown, 6 non-finite
+    int min_bits;    // fewest significant bits of any w_j
+    int steps_done;
+};
+
+}  // namespace ed

@@ -1,0 +1,98 @@
+// ed_lanczos_dev.cuh — scalar bookkeeping of the FX Lanczos recurrence,
+// run by one thread of the last block of each grid reduction.
+//
+// Recurrence (HubMatrix_GPU.cuh:573-582 restated on unnormalised vectors):
+//   v_j = w_j / beta_j,  u = H w_j (exact integer accumulation, then >> s_u)
+//   alpha_j   = <w_j, u> / beta_j^2
+//   w_{j+1}   = u/beta_j - (alpha_j/beta_j) w_j - (beta_j/beta_{j-1}) w_{j-1}
+//   beta_{j+1} = |w_{j+1}|
+// Every vector is int64 with its own exponent; the three real multipliers of
+// the axpy become int64 coefficients at[k] with per-term fractional bits so
+// that |w_{j+1} q| < 2^54 by construction (room for the matvec's sums).
+#pragma once
+
+#include "ed_device.cuh"
+#include "ed_lanczos.hpp"
+
+namespace ed {
+namespace dev {
+
+__device__ inline void lz_after_matvec(LzState* lz, int j, i128 alpha_raw, uint64_t m_u, int s_u, int Fc) {
+    const int eX = lz->e[j];
+    const uint64_t mX = lz->m[j];
+    const double bj = lz->beta[j];
+    const int e_u = eX - Fc + s_u;
+    lz->s_u = s_u;
+    lz->e_u = e_u;
+    lz->m_u = m_u;
+    if (!(bj > 0.0) || lz->status != 0) {
+        // after a breakdown (or a bad start) the recurrence only carries zeros
+        lz->alpha[j] = 0.0;
+        for (int k = 0; k < 3; ++k) { lz->at[k] = 0; lz->sh[k] = 0; }
+        lz->Fa = 0;
+        lz->e_w = eX;
+        return;
+    }
+    const double anum = i128_to_f64(alpha_raw, eX + e_u + 24);
+    const double aj = anum / (bj * bj);
+    lz->alpha[j] = aj;
+
+    double a[3];
+    uint64_t mm[3];
+    a[0] = ldexp(1.0, e_u) / bj;
+    mm[0] = m_u;
+    a[1] = -aj * ldexp(1.0, eX) / bj;
+    mm[1] = mX;
+    if (j > 0) {
+        a[2] = -bj * ldexp(1.0, lz->e[j - 1]) / lz->beta[j - 1];
+        mm[2] = lz->m[j - 1];
+    } else {
+        a[2] = 0.0;
+        mm[2] = 0;
+    }
+    double B = 0.0;
+    for (int k = 0; k < 3; ++k) B += fabs(a[k]) * (double)mm[k];
+    B *= (1.0 + 1e-9);
+    int kB = 0;
+    if (B > 0.0) frexp(B, &kB);  // B < 2^kB
+    const int e_w = kB - 54;
+    int F[3];
+    int Fmin = 1 << 20;
+    for (int k = 0; k < 3; ++k) {
+        F[k] = 0;
+        if (a[k] != 0.0 && mm[k] != 0) {
+            int ka;
+            frexp(fabs(a[k]) * ldexp(1.0, -e_w), &ka);  // |a_k| 2^-e_w < 2^ka
+            F[k] = 62 - ka;
+            Fmin = F[k] < Fmin ? F[k] : Fmin;
+        }
+    }
+    if (Fmin == (1 << 20)) Fmin = 62;
+    for (int k = 0; k < 3; ++k) {
+        int64_t at = 0;
+        int sh = 0;
+        if (a[k] != 0.0 && mm[k] != 0 && F[k] - Fmin < 120) {
+            at = llrint(ldexp(a[k], F[k] - e_w));
+            sh = F[k] - Fmin;
+        }
+        lz->at[k] = at;
+        lz->sh[k] = sh;
+    }
+    lz->Fa = Fmin;
+    lz->e_w = e_w;
+}
+
+__device__ inline void lz_after_axpy(LzState* lz, int j, i128 sumsq, uint64_t m_w) {
+    const int e_w = lz->e_w;
+    lz->e[j + 1] = e_w;
+    lz->m[j + 1] = m_w;
+    const double b2 = i128_to_f64(sumsq, 2 * e_w + 16);
+    lz->beta[j + 1] = sqrt(b2);
+    const int bits = bitlen_u64(m_w);
+    if (bits < lz->min_bits) lz->min_bits = bits;
+    if (m_w == 0 && lz->status == 0) lz->status = 7;  // breakdown
+    lz->steps_done = j + 1;
+}
+
+}  // namespace dev
+}  // namespace ed

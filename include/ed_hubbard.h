@@ -1,0 +1,208 @@
+/*
+ * ed_hubbard.h — C ABI of the GB300-native Hubbard exact-diagonalisation
+ * hot path: the Siro-Harju spin-split matvec
+ *     y = (H_up (x) 1 + 1 (x) H_dn + U * sum_i n_i,up n_i,dn) x
+ * over the fixed-(N_up, N_dn) product basis, and the Lanczos solver it drives.
+ *
+ * Conventions
+ *  - Every function returns an ed_status (0 = ED_OK) unless it returns a size;
+ *    nothing throws across this boundary.
+ *  - Vectors are FP64, length ed_op_rows(op) (complex operators: interleaved
+ *    re,im pairs, 2*rows doubles), indexed up-index-major exactly like the
+ *    reference: element (a_up, a_dn) sits at a_up * dim_dn + a_dn, where a_s
+ *    is the rank of the spin-s bitstring among N-bit words with Q_s bits set
+ *    in ascending-integer order (= the combinatorial-number-system rank).
+ *  - "stream" is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *  - Indices and sizes are 64-bit throughout.
+ *
+ * Reference interfaces replaced (paths inside the reference project
+ * jeechul/Exact_Diagonalization_for_Fermionic_systems_with_GPU):
+ *  - H_TBq (basis + per-spin tables)           MBL_test/include/fermi_operator.h:42-242
+ *  - Hubbard ctor / Hubbard_mv                 MBL_test/include/HubMatrix_GPU.cuh:30-182
+ *  - cuSpectra::Hubbard rows/cols/perform_op   TotalSpin/include/HubMatrix_TotalSpin.cuh:181-322
+ *  - Lanczos::random_vector / eigen            MBL_test/include/HubMatrix_GPU.cuh:477-613
+ *  - LAPACKf77::dsted (tridiagonal eigensolve)  MBL_test/include/MAGMA_LAPACK.h:296-326
+ */
+#ifndef ED_HUBBARD_H
+#define ED_HUBBARD_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int ed_status;
+
+enum {
+    ED_OK = 0,
+    ED_ERR_ARG = 1,          /* invalid argument (null pointer, bad size, bad site) */
+    ED_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    ED_ERR_ALLOC = 3,        /* device or host allocation failed */
+    ED_ERR_TABLE = 4,        /* a table row needs more slots than the layout has */
+    ED_ERR_RANGE = 5,        /* size beyond what the layout supports */
+    ED_ERR_NONFINITE = 6,    /* NaN or Inf in an input vector */
+    ED_ERR_BREAKDOWN = 7,    /* Lanczos residual vanished (invariant subspace) */
+    ED_ERR_NOT_CONVERGED = 8,/* convergence test not met within max_steps */
+    ED_ERR_TIMEOUT = 9,      /* a bounded device wait gave up */
+    ED_ERR_NOT_BUILT = 10    /* requested feature not available in this build */
+};
+
+/* Human-readable name of a status code (static storage). */
+const char* ed_status_string(ed_status s);
+/* ABI version: major*10000 + minor*100 + patch. */
+int ed_version(void);
+
+/* ------------------------------------------------------------------ basis --
+ * Combinatorial-number-system rank/unrank of N-bit words with Q bits set, in
+ * ascending-integer order.  Bit-identical to H_TBq::state / H_TBq::address
+ * (fermi_operator.h:44-53, 76-88).  Host functions. */
+int64_t ed_binom(int n, int k);
+/* words[i] = the ranks[i]-th word (0-based). */
+ed_status ed_basis_unrank(int n_sites, int n_part, const int64_t* ranks, int64_t count, uint64_t* words);
+/* ranks[i] = rank of words[i]; ED_ERR_ARG if a word has the wrong popcount. */
+ed_status ed_basis_rank(int n_sites, int n_part, const uint64_t* words, int64_t count, int64_t* ranks);
+/* Same two maps on the device (device pointers, asynchronous on stream). */
+ed_status ed_basis_unrank_device(int n_sites, int n_part, const int64_t* ranks, int64_t count, uint64_t* words, void* stream);
+ed_status ed_basis_rank_device(int n_sites, int n_part, const uint64_t* words, int64_t count, int64_t* ranks, void* stream);
+
+/* ------------------------------------------------------------- one-body terms
+ * A per-spin operator is an ordered list of terms, each one reference call:
+ *   ED_TERM_HOP      H_TBq::Make_H(i, j, t)   fermi_operator.h:100-115
+ *                    t (c+_i c_j + c+_j c_i), Jordan-Wigner sign
+ *                    (-1)^(particles strictly between i and j)
+ *   ED_TERM_CURRENT  H_TBq::Make_J(i, j, t)   fermi_operator.h:117-138
+ *                    row state empty at i, full at j -> +t; reverse -> -t
+ *   ED_TERM_DENSITY  H_TBq::Make_N(i, v)      fermi_operator.h:140-149
+ *                    v n_i (j ignored)
+ *   ED_TERM_PEIERLS  complex hop: t e^{+i phi} for the particle moving
+ *                    i -> j and t e^{-i phi} for j -> i (same sign rule);
+ *                    phi = 0 gives ED_TERM_HOP.  Requires ED_OP_COMPLEX.
+ * value = t (or v), phase = phi (PEIERLS only). */
+enum { ED_TERM_HOP = 0, ED_TERM_CURRENT = 1, ED_TERM_DENSITY = 2, ED_TERM_PEIERLS = 3 };
+
+typedef struct {
+    int32_t kind;
+    int32_t i, j;
+    int32_t pad_;
+    double value;
+    double phase;
+} ed_term;
+
+/* Reference ELL export: the exact tables H_TBq builds for the given term
+ * list, slot-major with z*Q+1 = 10*Q+1 slots (Ax[s*count + a], Aj[s*count + a],
+ * 0.0 marks an empty slot, first-empty-slot stacking, fermi_operator.h:64-73).
+ * Real terms only.  ax, aj: count*(10*Q+1) entries; state: count entries (any
+ * of the three may be NULL).  ED_ERR_TABLE if a row overflows its slots. */
+ed_status ed_tables_ell(int n_sites, int n_part, const ed_term* terms, int n_terms,
+                        double* ax, int64_t* aj, uint64_t* state);
+
+/* --------------------------------------------------------------- operator -- */
+typedef struct ed_op ed_op;
+
+enum { ED_OP_REAL = 0, ED_OP_COMPLEX = 1 };
+enum { ED_MEM_HOST = 0, ED_MEM_DEVICE = 1 };
+
+typedef struct {
+    int32_t n_sites;            /* N (<= 62) */
+    int32_t n_up, n_dn;         /* Q_up, Q_dn */
+    int32_t flags;              /* ED_OP_REAL | ED_OP_COMPLEX */
+    const ed_term* up_terms;    /* spin-up term list (H_TBq of the up spin) */
+    int32_t n_up_terms;
+    int32_t pad0_;
+    const ed_term* dn_terms;    /* spin-down term list */
+    int32_t n_dn_terms;
+    int32_t pad1_;
+    double U;                   /* on-site interaction */
+    uint64_t interaction_mask;  /* sites where U acts; 0 = all N sites
+                                   (the reference "dilution" word,
+                                   HubMatrix_GPU.cuh:72-95, 152-156) */
+} ed_model_desc;
+
+/* Build the operator on the given CUDA device: basis, per-spin tables and
+ * the folded diagonal are built on the host and uploaded once (the reference
+ * Hubbard ctor, HubMatrix_GPU.cuh:46-95). */
+ed_status ed_op_create(ed_op** op, const ed_model_desc* desc, int device);
+ed_status ed_op_destroy(ed_op* op);
+
+/* Hilbert-space dimension dim_up * dim_dn (64-bit: the reference's int
+ * rows() overflows at 2^31, HubMatrix_TotalSpin.cuh:279-280). */
+int64_t ed_op_rows(const ed_op* op);
+int64_t ed_op_cols(const ed_op* op);
+int64_t ed_op_dim_up(const ed_op* op);
+int64_t ed_op_dim_dn(const ed_op* op);
+int ed_op_is_complex(const ed_op* op);
+
+/* y = H x.  mem = ED_MEM_HOST: x, y are host pointers and the call is
+ * synchronous — the cuSpectra::Hubbard::perform_op semantics
+ * (HubMatrix_TotalSpin.cuh:282-311).  mem = ED_MEM_DEVICE: device pointers,
+ * asynchronous on stream — the Hubbard::Hubbard_mv semantics
+ * (HubMatrix_GPU.cuh:163-182) without its device-wide sync.  y is
+ * overwritten; x and y must not overlap. */
+ed_status ed_op_perform(ed_op* op, const double* x, double* y, int mem, void* stream);
+
+/* ---------------------------------------------------------------- Lanczos -- */
+enum { ED_LANCZOS_REFERENCE = 0,  /* stop test every 10 steps as in
+                                       HubMatrix_GPU.cuh:585-597 */
+       ED_LANCZOS_FIXED = 1 };    /* exactly max_steps steps */
+enum { ED_RITZ_NONE = 0, ED_RITZ_STORED = 1, /* from the stored Krylov basis */
+       ED_RITZ_RECOMPUTE = 2 };   /* second pass, as HubMatrix_GPU.cuh:600-612 */
+enum { ED_START_RANDOM = 0, ED_START_USER = 1 };
+
+typedef struct {
+    int32_t max_steps;     /* Lanczos steps (reference maxN = 1000) */
+    int32_t mode;          /* ED_LANCZOS_REFERENCE | ED_LANCZOS_FIXED */
+    int32_t reorth;        /* 1 = full reorthogonalisation (needs ED_RITZ_STORED
+                              storage; the basis is kept either way) */
+    int32_t ritz;          /* ED_RITZ_* */
+    int32_t start;         /* ED_START_RANDOM (counter-based, seed below) |
+                              ED_START_USER (start vector given) */
+    int32_t profile;       /* 1 = time every matvec / axpy launch with CUDA
+                              events on the launching stream (result fields
+                              matvec_ms, axpy_ms) */
+    uint64_t seed;         /* seed of the uniform(-1,1) start vector */
+} ed_lanczos_cfg;
+
+typedef struct {
+    double e0;             /* lowest Ritz value */
+    int32_t steps;         /* Lanczos steps taken (size of T) */
+    int32_t converged;     /* reference stop test met */
+    int32_t status;        /* ED_OK | ED_ERR_BREAKDOWN | ... */
+    int32_t min_bits;      /* fewest significant bits any Lanczos vector kept */
+    double residual;       /* |beta_{n} z_{n-1}| of the lowest Ritz pair */
+    int64_t launches;      /* kernels this call launched */
+    double matvec_ms;      /* profile: summed device time of the matvec launches */
+    double axpy_ms;        /* profile: summed device time of the axpy launches */
+    int32_t n_matvec;      /* matvec launches */
+    int32_t pad_;
+} ed_lanczos_result;
+
+/* Run Lanczos on op.  start: ED_START_USER start vector (rows doubles, mem
+ * as start_mem), else ignored.  evec: output Ritz vector (normalised; rows
+ * doubles at evec_mem) when cfg->ritz != ED_RITZ_NONE, may be NULL
+ * otherwise.  alpha (max_steps) and beta (max_steps+1, beta[0] = |f|) are
+ * optional HOST outputs of the tridiagonal T.  Synchronous. */
+ed_status ed_lanczos_run(ed_op* op, const ed_lanczos_cfg* cfg,
+                         const double* start, int start_mem,
+                         double* evec, int evec_mem,
+                         double* alpha, double* beta,
+                         ed_lanczos_result* res, void* stream);
+
+/* Same generator on the device: out (device, n doubles), async on stream. */
+ed_status ed_random_vector_device(int64_t n, uint64_t seed, double* out_device, void* stream);
+
+/* The start vector ED_START_RANDOM uses: uniform(-1,1) from a counter-based
+ * generator keyed by seed (Philox4x64-10, element k from counter k/4, word k%4), NOT
+ * normalised.  Host output. */
+ed_status ed_random_vector(int64_t n, uint64_t seed, double* out_host);
+
+/* Lowest eigenpair of the symmetric tridiagonal (alpha[0..n-1], off-diagonal
+ * beta[0..n-2]) computed by the device solver: eigenvalue e0 and eigenvector
+ * z (n doubles).  Host in/out; replaces LAPACKf77::dsted for the Lanczos T. */
+ed_status ed_tridiag_lowest(int n, const double* alpha, const double* offdiag,
+                            double* e0, double* z);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ED_HUBBARD_H */

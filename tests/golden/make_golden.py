@@ -1,0 +1,140 @@
+"""Generate the golden fixtures in this directory.
+
+Run from the repository root in a checkout where the reference sources are
+available (they are read by oracle/Makefile's `ref` target, which compiles
+the reference's own MBL_test/include/fermi_operator.h into
+oracle/_ref/ref_tables):
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+Outputs
+  tables_small.npz   reference H_TBq state/Ax/Aj arrays for small cases
+  tables_digest.json sha256 digests of the reference tables for large cases
+  energies.json      ground-state energies (dense or scipy eigsh on the
+                     reference tables) and entanglement entropies
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+from oracle import oracle as O  # noqa: E402
+from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+
+def digest(state, ax, aj) -> str:
+    h = hashlib.sha256()
+    h.update(np.ascontiguousarray(state, dtype=np.int64).tobytes())
+    h.update(np.ascontiguousarray(ax, dtype=np.float64).tobytes())
+    h.update(np.ascontiguousarray(aj, dtype=np.int64).tobytes())
+    return h.hexdigest()
+
+
+def disorder(seed: int, n: int, W: float) -> list:
+    """eps_i = W * uniform(-1,1) from Philox4x64-10(key=seed) — the same
+    stream ed_random_vector produces."""
+    bg = np.random.Philox(key=np.array([seed, 0], dtype=np.uint64))
+    r = bg.random_raw(n)
+    u = ((r >> np.uint64(12)) | np.uint64(0x3FF0000000000000)).view(np.float64) * 2.0 - 3.0
+    return [float(W * v) for v in u]
+
+
+# name -> (N, Q, terms)
+def cases_small():
+    eps = disorder(11, 8, 2.0)
+    return {
+        "chain8_q4": (8, 4, L.chain(8)),
+        "chain8_q3": (8, 3, L.chain(8)),
+        "chain8_q4_open_eps": (8, 4, L.chain(8, periodic=False, eps=eps)),
+        "chain8_q4_current": (8, 4, [("J", i, (i + 1) % 8, 1.0, 0.0) for i in range(8)]),
+        "kagome12_q6": (12, 6, L.kagome12()),
+        "kagome12_q5_kx": (12, 5, L.kagome12_kinetic_x()),
+        "kagome12_q6_jx": (12, 6, L.kagome12_current_x()),
+        "lieb12_q6": (12, 6, L.lieb12()),
+        "square3x4_q3": (12, 3, L.squared_3by4()),
+    }
+
+
+def cases_large():
+    out = {}
+    for q in (6, 7, 8, 4, 5):
+        out[f"chain12_open_q{q}_W6"] = (12, q, L.chain(12, periodic=False, eps=disorder(100, 12, 6.0)))
+    out["lieb18_q9"] = (18, 9, L.lieb18())
+    out["kagome12_q6_ky"] = (12, 6, L.kagome12_kinetic_y())
+    out["kagome12_q6_jy"] = (12, 6, L.kagome12_current_y())
+    return out
+
+
+def main() -> None:
+    if not O.REF_TABLES.exists():
+        raise SystemExit("oracle/_ref/ref_tables missing: run `make -C oracle ref` first")
+    small = {}
+    meta = {}
+    for name, (N, Q, terms) in cases_small().items():
+        state, address, ax, aj = O.ref_tables(N, Q, terms)
+        small[f"{name}__state"] = state.astype(np.int64)
+        small[f"{name}__ax"] = ax
+        small[f"{name}__aj"] = aj.astype(np.int32)
+        meta[name] = {"N": N, "Q": Q, "terms": terms}
+    np.savez_compressed(OUT / "tables_small.npz", **small)
+
+    digests = {}
+    for name, (N, Q, terms) in cases_large().items():
+        t0 = time.time()
+        state, address, ax, aj = O.ref_tables(N, Q, terms)
+        digests[name] = {"N": N, "Q": Q, "terms": terms, "sha256": digest(state, ax, aj),
+                         "count": int(state.size), "nnz": int((ax != 0).sum())}
+        print(name, f"{time.time() - t0:.1f}s", flush=True)
+    (OUT / "tables_digest.json").write_text(json.dumps({"small": meta, "large": digests}, indent=1))
+
+    import scipy.sparse.linalg as sla
+    en = {}
+    # L=8 periodic chain, 4+4: dense spectrum
+    for U in (4.0, 0.0):
+        H = O.hamiltonian(8, 4, 4, L.chain(8), L.chain(8), U).toarray()
+        w, v = np.linalg.eigh(H)
+        en[f"chain8_pbc_q44_U{U:g}"] = {"E0": float(w[0]), "E1": float(w[1])}
+        if U == 4.0:
+            s_vn, s_ref = O.entanglement_entropy(v[:, 0], 8, 4, 4, [0, 1, 2, 3])
+            en["chain8_pbc_q44_U4"].update({"EE_vN_A0123": s_vn, "EE_ref_A0123": s_ref})
+    # atomic limit t=0 with site energies: E0 = min over configurations
+    eps = disorder(11, 8, 2.0)
+    H = O.hamiltonian(8, 3, 2, [("N", i, 0, eps[i], 0.0) for i in range(8)],
+                      [("N", i, 0, eps[i], 0.0) for i in range(8)], 3.0)
+    en["atomic8_q32_U3"] = {"E0": float(H.diagonal().min()), "eps": eps}
+    # Kagome12 6+6 (reference lattice incl. the -2 r^2 on-site term), U=8 and U=4
+    for U in (8.0, 4.0):
+        t0 = time.time()
+        H = O.hamiltonian(12, 6, 6, L.kagome12(), L.kagome12(), U)
+        w = sla.eigsh(H, k=2, which="SA", tol=1e-13, maxiter=20000)[0]
+        en[f"kagome12_q66_U{U:g}"] = {"E0": float(np.sort(w)[0]), "E1": float(np.sort(w)[1])}
+        print("kagome", U, f"{time.time() - t0:.1f}s", flush=True)
+    # Lieb12 6+6 U=4
+    H = O.hamiltonian(12, 6, 6, L.lieb12(), L.lieb12(), 4.0)
+    w = sla.eigsh(H, k=1, which="SA", tol=1e-13, maxiter=20000)[0]
+    en["lieb12_q66_U4"] = {"E0": float(w[0])}
+    # MBL chain L=12 open, W=6, U=1, one realisation, three sectors
+    eps12 = disorder(100, 12, 6.0)
+    for qu, qd in ((6, 6), (7, 5), (8, 4)):
+        terms = L.chain(12, periodic=False, eps=eps12)
+        H = O.hamiltonian(12, qu, qd, terms, terms, 1.0)
+        w, v = sla.eigsh(H, k=1, which="SA", tol=1e-13, maxiter=20000)
+        s_vn, s_ref = O.entanglement_entropy(v[:, 0], 12, qu, qd, list(range(6)))
+        en[f"chain12_open_W6_seed100_q{qu}{qd}_U1"] = {"E0": float(w[0]), "EE_vN_A0to5": s_vn,
+                                                       "EE_ref_A0to5": s_ref, "eps": eps12}
+    (OUT / "energies.json").write_text(json.dumps(en, indent=1))
+    print(json.dumps(en, indent=1))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,149 @@
+"""GPU Lanczos (device recurrence, device tridiagonal eigensolve, Ritz
+vector) against the oracle and the golden energies.
+
+Tolerances: E0 to 1e-10 relative (the reference's stop test targets
+0.01*sqrt(eps)); Ritz vectors through their residual |Hv - E0 v| and the
+entanglement entropy to 1e-8.
+"""
+import numpy as np
+import pytest
+
+from conftest import philox_uniform, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def op_for(ed, N, qu, qd, terms_u, terms_d, U):
+    return ed.Hubbard(ed.H_TBq(N, qu).extend(terms_u), ed.H_TBq(N, qd).extend(terms_d), U)
+
+
+def test_chain8_fixed100_reorth(ed, orc, golden_energies):
+    """Plain small config: L=8 PBC, 4+4, U=4, 100 steps with full
+    reorthogonalisation, start vector Philox(seed 0); E0 and the half-chain
+    entanglement entropy of the Ritz vector."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    g = golden_energies["chain8_pbc_q44_U4"]
+    op = op_for(ed, 8, 4, 4, L.chain(8), L.chain(8), 4.0)
+    lz = ed.Lanczos(op.dimUP, op.dimDN)
+    e0, v = lz.eigen(op, max_steps=100, mode="fixed", reorth=True, seed=0)
+    assert abs(e0 - g["E0"]) < 1e-10 * abs(g["E0"]), e0 - g["E0"]
+    assert abs(np.linalg.norm(v) - 1.0) < 1e-12
+    r = op.matvec(v) - e0 * v
+    assert np.linalg.norm(r) < 1e-7
+    s_vn, s_ref = orc.entanglement_entropy(v, 8, 4, 4, [0, 1, 2, 3])
+    assert abs(s_vn - g["EE_vN_A0123"]) < 1e-8
+    assert abs(s_ref - g["EE_ref_A0123"]) < 1e-8 * abs(g["EE_ref_A0123"])
+
+
+def test_reference_mode_matches_oracle(ed, orc, golden_energies):
+    """Same start vector, the reference stop test (every 10 steps,
+    tolconv = 0.01 sqrt(eps)): the same number of steps, T to 1e-10 and E0."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    op = op_for(ed, 8, 4, 4, L.chain(8), L.chain(8), 4.0)
+    t = orc.Tables(8, 4, L.chain(8))
+    f = philox_uniform(235, op.rows())
+    e_o, a_o, b_o, v_o = orc.lanczos(t, t, 4.0, f, 1000, mode="reference")
+    lz = ed.Lanczos(op.dimUP, op.dimDN)
+    e0, v = lz.eigen(op, f=f, max_steps=1000, mode="reference")
+    assert lz.result.converged == 1
+    assert len(lz.a) == len(a_o)
+    k = min(30, len(a_o))
+    assert np.max(np.abs(np.array(lz.a[:k]) - a_o[:k])) < 1e-10
+    assert np.max(np.abs(np.array(lz.b[:k]) - b_o[:k])) < 1e-10
+    assert abs(e0 - e_o) < 1e-10 * abs(e_o)
+    assert abs(abs(v @ v_o) - 1.0) < 1e-8
+
+
+def test_kagome12_300_steps(ed, golden_energies):
+    """Kagome 12-site, 6+6, U=8, 300 fixed steps: E0 to 1e-10 and the Ritz vector."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    g = golden_energies["kagome12_q66_U8"]
+    op = op_for(ed, 12, 6, 6, L.kagome12(), L.kagome12(), 8.0)
+    lz = ed.Lanczos(op.dimUP, op.dimDN)
+    e0, v = lz.eigen(op, max_steps=300, mode="fixed", seed=0)
+    assert abs(e0 - g["E0"]) < 1e-10 * abs(g["E0"]), e0 - g["E0"]
+    assert np.linalg.norm(op.matvec(v) - e0 * v) < 1e-6
+    assert lz.result.min_bits >= 44
+
+
+@pytest.mark.parametrize("sector", [(6, 6), (7, 5), (8, 4)])
+def test_mbl_chain12_sectors(ed, orc, golden_energies, sector):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    qu, qd = sector
+    g = golden_energies[f"chain12_open_W6_seed100_q{qu}{qd}_U1"]
+    terms = L.chain(12, periodic=False, eps=g["eps"])
+    op = op_for(ed, 12, qu, qd, terms, terms, 1.0)
+    lz = ed.Lanczos(op.dimUP, op.dimDN)
+    e0, v = lz.eigen(op, max_steps=1000, mode="reference", seed=3)
+    assert abs(e0 - g["E0"]) < 1e-10 * abs(g["E0"])
+    s_vn, s_ref = orc.entanglement_entropy(v, 12, qu, qd, list(range(6)))
+    assert abs(s_vn - g["EE_vN_A0to5"]) < 1e-8
+    assert abs(s_ref - g["EE_ref_A0to5"]) < 1e-8 * max(1.0, abs(g["EE_ref_A0to5"]))
+
+
+def test_lieb12(ed, golden_energies):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    g = golden_energies["lieb12_q66_U4"]
+    op = op_for(ed, 12, 6, 6, L.lieb12(), L.lieb12(), 4.0)
+    e0, _ = ed.Lanczos().eigen(op, max_steps=1000, mode="reference", ritz="none", seed=1)
+    assert abs(e0 - g["E0"]) < 1e-10 * abs(g["E0"])
+
+
+def test_atomic_limit_saturated_krylov(ed, golden_energies):
+    """No hopping: the Krylov space saturates after a few steps (beta -> 0);
+    further steps must not corrupt E0."""
+    g = golden_energies["atomic8_q32_U3"]
+    eps = g["eps"]
+    terms = [("N", i, 0, eps[i], 0.0) for i in range(8)]
+    op = op_for(ed, 8, 3, 2, terms, terms, 3.0)
+    e0, _ = ed.Lanczos().eigen(op, max_steps=60, mode="fixed", ritz="none", seed=2)
+    assert abs(e0 - g["E0"]) < 1e-10 * max(1.0, abs(g["E0"]))
+
+
+def test_complex_peierls_lanczos(ed, orc):
+    """Complex (twisted) operator: E0 from the device Lanczos equals scipy."""
+    import scipy.sparse.linalg as sla
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    terms = L.kagome12(flux=0.4)
+    op = op_for(ed, 12, 5, 4, terms, terms, 4.0)
+    H = orc.hamiltonian(12, 5, 4, terms, terms, 4.0)
+    w = sla.eigsh(H, k=1, which="SA", tol=1e-13)[0][0]
+    e0, v = ed.Lanczos().eigen(op, max_steps=1000, mode="reference", seed=5)
+    assert abs(e0 - w) < 1e-10 * abs(w)
+    assert np.linalg.norm(H @ v - e0 * v) < 1e-6
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 100, 301, 1000])
+def test_device_tridiagonal_vs_scipy(ed, n):
+    from scipy.linalg import eigh_tridiagonal
+    rng = np.random.default_rng(n)
+    a = rng.normal(size=n) * 3
+    b = np.abs(rng.normal(size=max(n - 1, 0))) + 1e-3
+    lam, z = ed.tridiag_lowest(a, b)
+    w, V = eigh_tridiagonal(a, b) if n > 1 else (a, np.ones((1, 1)))
+    assert abs(lam - w[0]) < 1e-12 * max(1.0, np.max(np.abs(w)))
+    assert abs(abs(z @ V[:, 0]) - 1.0) < 1e-9
+
+
+def test_start_vector_user_vs_random_same(ed):
+    """ED_START_RANDOM(seed) is exactly the Philox vector a caller would pass."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    op = op_for(ed, 8, 4, 4, L.chain(8), L.chain(8), 4.0)
+    lz1, lz2 = ed.Lanczos(), ed.Lanczos()
+    e1, _ = lz1.eigen(op, max_steps=40, mode="fixed", ritz="none", seed=9)
+    e2, _ = lz2.eigen(op, f=philox_uniform(9, op.rows()), max_steps=40, mode="fixed", ritz="none")
+    assert lz1.a == lz2.a and lz1.b == lz2.b and e1 == e2
+
+
+def test_lanczos_profile_and_launch_count(ed):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, _capi
+    import ctypes as C
+    op = op_for(ed, 12, 6, 6, L.kagome12(), L.kagome12(), 8.0)
+    lib = _capi.load()
+    cfg = _capi.ed_lanczos_cfg(max_steps=50, mode=1, reorth=0, ritz=1, start=0, profile=1, seed=0)
+    res = _capi.ed_lanczos_result()
+    v = np.empty(op.rows())
+    assert lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0, C.c_void_p(v.ctypes.data), 0, None, None,
+                              C.byref(res), None) == 0
+    assert res.n_matvec == 50 and res.matvec_ms > 0 and res.axpy_ms > 0
+    assert res.launches == 3 + 2 * 50 + 12 + 2

@@ -1,0 +1,158 @@
+"""GPU parity of the spin-split matvec against the CPU oracle.
+
+Real operators are compared with the restated reference kernel
+(oracle/hubbard_oracle.c, Hubbard_mv_); complex (Peierls) operators with the
+oracle's independent scipy construction.  Tolerance: the GPU sums +-x
+exactly in int64 fixed point and rounds once, so the normwise relative
+difference to the FP64 oracle is set by the oracle's own rounding:
+|y_gpu - y_oracle| / |y_oracle| < 1e-13.
+"""
+import numpy as np
+import pytest
+
+from conftest import philox_uniform, rel_err
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-13
+
+
+def make_op(ed, N, qu, qd, up_terms, dn_terms, U, dilution=None):
+    hu = ed.H_TBq(N, qu).extend(up_terms)
+    hd = ed.H_TBq(N, qd).extend(dn_terms)
+    return ed.Hubbard(hu, hd, U, dilution=dilution)
+
+
+def real_cases():
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    eps8 = list(philox_uniform(11, 8, 2.0))
+    eps12 = list(philox_uniform(100, 12, 6.0))
+    return [
+        ("chain8_pbc_44_U4", 8, 4, 4, L.chain(8), L.chain(8), 4.0, None),
+        ("chain8_pbc_35_U2.5_diluted", 8, 3, 5, L.chain(8), L.chain(8, eps=eps8), 2.5, 0b10110111),
+        ("kagome12_66_U8", 12, 6, 6, L.kagome12(), L.kagome12(), 8.0, None),
+        ("kagome12_54_Kx", 12, 5, 4, L.kagome12_kinetic_x(), L.kagome12_kinetic_x(), 0.0, None),
+        ("kagome12_54_Jx", 12, 5, 4, L.kagome12_current_x(), L.kagome12_current_x(), 0.0, None),
+        ("chain12_open_W6_66", 12, 6, 6, L.chain(12, False, eps=eps12), L.chain(12, False, eps=eps12), 1.0, None),
+        ("chain12_open_W6_75", 12, 7, 5, L.chain(12, False, eps=eps12), L.chain(12, False, eps=eps12), 1.0, None),
+        ("chain12_open_W6_84", 12, 8, 4, L.chain(12, False, eps=eps12), L.chain(12, False, eps=eps12), 1.0, None),
+        ("lieb12_66_U4", 12, 6, 6, L.lieb12(), L.lieb12(), 4.0, None),
+        ("square3x4_43_U3", 12, 4, 3, L.squared_3by4(), L.squared_3by4(), 3.0, None),
+        ("atomic8_32_U3", 8, 3, 2, [("N", i, 0, eps8[i], 0.0) for i in range(8)],
+         [("N", i, 0, eps8[i], 0.0) for i in range(8)], 3.0, None),
+        ("random_hop10_46", 10, 4, 6, [("H", i, (i + 3) % 10, 0.3 + 0.1 * i, 0.0) for i in range(10)],
+         [("H", i, (i + 1) % 10, -1.0, 0.0) for i in range(10)] + [("J", 0, 5, 0.7, 0.0)], 1.7, None),
+    ]
+
+
+@pytest.mark.parametrize("case", real_cases(), ids=lambda c: c[0])
+def test_matvec_real_vs_oracle(ed, orc, case):
+    name, N, qu, qd, ut, dt, U, dil = case
+    op = make_op(ed, N, qu, qd, ut, dt, U, dil)
+    tu, td = orc.Tables(N, qu, ut), orc.Tables(N, qd, dt)
+    rng = np.random.default_rng(7)
+    for trial in range(2):
+        x = rng.standard_normal(op.rows())
+        y = op.matvec(x)
+        yo = orc.matvec(tu, td, U, x, mask=(orc.mask_all(N) if dil is None else dil))
+        assert rel_err(y, yo) < TOL, (name, rel_err(y, yo))
+
+
+def test_matvec_device_path_matches_host_path(ed):
+    import torch
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    op = make_op(ed, 12, 6, 6, L.kagome12(), L.kagome12(), 8.0)
+    x = np.random.default_rng(1).standard_normal(op.rows())
+    y_host = op.matvec(x)
+    xt = torch.from_numpy(x).cuda()
+    yt = torch.empty_like(xt)
+    op.Hubbard_mv(xt, yt)
+    torch.cuda.synchronize()
+    assert np.array_equal(yt.cpu().numpy(), y_host)
+
+
+def test_matvec_hermitian_and_scale_invariant(ed):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    op = make_op(ed, 12, 6, 5, L.kagome12(), L.kagome12(), 4.0)
+    rng = np.random.default_rng(3)
+    x, z = rng.standard_normal(op.rows()), rng.standard_normal(op.rows())
+    hx, hz = op.matvec(x), op.matvec(z)
+    assert abs(z @ hx - x @ hz) < 1e-12 * np.linalg.norm(hx) * np.linalg.norm(z)
+    # exact power-of-two scaling of the input scales the output exactly
+    for k in (-900, -3, 1, 700):
+        assert np.array_equal(op.matvec(x * 2.0 ** k), hx * 2.0 ** k), k
+    assert np.array_equal(op.matvec(np.zeros(op.rows())), np.zeros(op.rows()))
+
+
+def test_matvec_nonfinite_input_is_reported(ed):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300._capi import EdError
+    op = make_op(ed, 8, 4, 4, L.chain(8), L.chain(8), 4.0)
+    x = np.ones(op.rows())
+    x[17] = np.nan
+    with pytest.raises(EdError) as e:
+        op.matvec(x)
+    assert e.value.status == 6
+
+
+def test_matvec_wide_dynamic_range(ed, orc):
+    """Elements spanning 2^-40..1: the FX input quantisation (54 bits below
+    the largest element) keeps the normwise error at FP64 level."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    op = make_op(ed, 8, 4, 4, L.chain(8), L.chain(8), 4.0)
+    t = orc.Tables(8, 4, L.chain(8))
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal(op.rows()) * 2.0 ** rng.integers(-40, 1, op.rows())
+    assert rel_err(op.matvec(x), orc.matvec(t, t, 4.0, x)) < TOL
+
+
+@pytest.mark.parametrize("flux", [0.0, 0.37, np.pi / 2])
+def test_matvec_complex_peierls(ed, orc, flux):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    terms = L.kagome12(flux=flux) if flux else [("P",) + t[1:] if t[0] == "H" else t for t in L.kagome12()]
+    op = make_op(ed, 12, 4, 3, terms, terms, 4.0)
+    assert op.is_complex
+    H = orc.hamiltonian(12, 4, 3, terms, terms, 4.0)
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal(op.rows()) + 1j * rng.standard_normal(op.rows())
+    assert rel_err(op.matvec(x), H @ x) < TOL
+    # Hermitian: <z, H x> = conj(<x, H z>)
+    z = rng.standard_normal(op.rows()) + 1j * rng.standard_normal(op.rows())
+    a, b = np.vdot(z, op.matvec(x)), np.vdot(x, op.matvec(z))
+    assert abs(a - np.conj(b)) < 1e-12 * abs(a)
+
+
+def test_complex_operator_zero_flux_equals_real(ed):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    real = make_op(ed, 12, 5, 5, L.kagome12(), L.kagome12(), 8.0)
+    pt = [("P",) + t[1:] if t[0] == "H" else t for t in L.kagome12()]
+    cplx = make_op(ed, 12, 5, 5, pt, pt, 8.0)
+    x = np.random.default_rng(6).standard_normal(real.rows())
+    yr = real.matvec(x)
+    yc = cplx.matvec(x.astype(np.complex128))
+    assert np.array_equal(yc.real, yr) and not np.any(yc.imag)
+
+
+def test_basis_rank_unrank_device(ed, edlib):
+    import ctypes as C
+    import torch
+    for N, Q in ((12, 6), (18, 9), (40, 9)):
+        count = ed.binom(N, Q)
+        r = torch.randint(0, count, (100000,), dtype=torch.int64, device="cuda")
+        w = torch.empty_like(r)
+        r2 = torch.empty_like(r)
+        assert edlib.ed_basis_unrank_device(N, Q, C.c_void_p(r.data_ptr()), r.numel(), C.c_void_p(w.data_ptr()), None) == 0
+        assert edlib.ed_basis_rank_device(N, Q, C.c_void_p(w.data_ptr()), w.numel(), C.c_void_p(r2.data_ptr()), None) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(r, r2)
+        host = ed.basis_unrank(N, Q, r[:2000].cpu().numpy())
+        assert np.array_equal(host.view(np.int64), w[:2000].cpu().numpy())
+
+
+def test_device_random_vector_matches_host(ed, edlib):
+    import ctypes as C
+    import torch
+    n = 1_000_003
+    t = torch.empty(n, dtype=torch.float64, device="cuda")
+    assert edlib.ed_random_vector_device(n, 42, C.c_void_p(t.data_ptr()), None) == 0
+    torch.cuda.synchronize()
+    assert np.array_equal(t.cpu().numpy(), philox_uniform(42, n))
