@@ -62,8 +62,9 @@ __device__ __forceinline__ void lz_reduce_tail(i128 ss, uint64_t mx, LzState* lz
         i128 s = 0;
         uint64_t m = 0;
         for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-            s += (i128)(((u128)lz->part_hi[i] << 64) | lz->part_lo[i]);
-            m = lz->part_max[i] > m ? lz->part_max[i] : m;
+            s += (i128)(((u128)__ldcg(lz->part_hi + i) << 64) | __ldcg(lz->part_lo + i));
+            const uint64_t pm = __ldcg(lz->part_max + i);
+            m = pm > m ? pm : m;
         }
         s = block_sum_i128(s, s128);
         m = block_max_u64(m, s64);
@@ -157,11 +158,11 @@ __global__ void __launch_bounds__(kLzThreads) k_lz_stats(const int64_t* __restri
 
 // partial[k * gridDim.y + c] = sum over chunk c of (q_k q_w) >> 24, exact.
 __global__ void __launch_bounds__(kLzThreads) k_lz_dots(const int64_t* __restrict__ basis, int64_t n,
-                                                        const int64_t* __restrict__ w, uint64_t* part_lo,
-                                                        uint64_t* part_hi) {
+                                                        int64_t stride, const int64_t* __restrict__ w,
+                                                        uint64_t* part_lo, uint64_t* part_hi) {
     const int k = blockIdx.x;
     const int c = blockIdx.y, nc = gridDim.y;
-    const int64_t* q = basis + (int64_t)k * n;
+    const int64_t* q = basis + (int64_t)k * stride;
     i128 s = 0;
     for (int64_t i = (int64_t)c * blockDim.x + threadIdx.x; i < n; i += (int64_t)nc * blockDim.x)
         s += mul_wide(q[i], w[i]) >> 24;
@@ -175,24 +176,26 @@ __global__ void __launch_bounds__(kLzThreads) k_lz_dots(const int64_t* __restric
 
 // w <- w - round(sum_k (rt_k q_k >> rs_k) / 2^F)
 __global__ void __launch_bounds__(kLzThreads) k_lz_reorth(int64_t* __restrict__ w, const int64_t* __restrict__ basis,
-                                                          int64_t n, int nk, const int64_t* __restrict__ rt,
-                                                          const int* __restrict__ rs, int F) {
+                                                          int64_t n, int64_t stride, int nk,
+                                                          const int64_t* __restrict__ rt, const int* __restrict__ rs,
+                                                          int F) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         i128 acc = 0;
-        for (int k = 0; k < nk; ++k) acc += mul_wide(rt[k], basis[(int64_t)k * n + i]) >> rs[k];
+        for (int k = 0; k < nk; ++k) acc += mul_wide(rt[k], basis[(int64_t)k * stride + i]) >> rs[k];
         w[i] -= (int64_t)shr_round(acc, F);
     }
 }
 
 // evec = sum_k (rt_k q_k >> rs_k) * 2^-F as FP64, plus |evec|^2 partials.
-__global__ void __launch_bounds__(kLzThreads) k_ritz(const int64_t* __restrict__ basis, int64_t n, int nk,
-                                                     const int64_t* __restrict__ rt, const int* __restrict__ rs, int F,
-                                                     double* __restrict__ out, double* __restrict__ part,
-                                                     unsigned int* counter, double* inv_norm) {
+__global__ void __launch_bounds__(kLzThreads) k_ritz(const int64_t* __restrict__ basis, int64_t n, int64_t stride,
+                                                     int nk, const int64_t* __restrict__ rt,
+                                                     const int* __restrict__ rs, int F, double* __restrict__ out,
+                                                     double* __restrict__ part, unsigned int* counter,
+                                                     double* inv_norm) {
     double ss = 0.0;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         i128 acc = 0;
-        for (int k = 0; k < nk; ++k) acc += mul_wide(rt[k], basis[(int64_t)k * n + i]) >> rs[k];
+        for (int k = 0; k < nk; ++k) acc += mul_wide(rt[k], basis[(int64_t)k * stride + i]) >> rs[k];
         const double v = i128_to_f64(acc, -F);
         out[i] = v;
         ss = fma(v, v, ss);
@@ -203,7 +206,7 @@ __global__ void __launch_bounds__(kLzThreads) k_ritz(const int64_t* __restrict__
     if (elect_last_block(counter)) {
         if (threadIdx.x == 0) {
             double t = 0.0;
-            for (int i = 0; i < (int)gridDim.x; ++i) t += part[i];
+            for (int i = 0; i < (int)gridDim.x; ++i) t += __ldcg(part + i);
             *inv_norm = t > 0.0 ? 1.0 / sqrt(t) : 0.0;
             *counter = 0;
         }
@@ -232,6 +235,7 @@ struct Workspace {
     int device = -1;
     size_t basis_slots = 0;
     int64_t DW = 0;
+    int64_t stride = 0;  // slot stride in elements: DW rounded up to 32 (256-byte aligned slots)
     int max_steps = 0;
     int64_t* basis = nullptr;
     int64_t* u = nullptr;
@@ -282,9 +286,10 @@ ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_s
     w->device = op->device;
     w->basis_slots = slots;
     w->DW = DW;
+    w->stride = (DW + 31) / 32 * 32;
     w->max_steps = max_steps;
     const size_t ns = (size_t)max_steps + 2;
-    LZ_CK(cudaMalloc(&w->basis, sizeof(int64_t) * slots * (size_t)DW));
+    LZ_CK(cudaMalloc(&w->basis, sizeof(int64_t) * slots * (size_t)w->stride));
     LZ_CK(cudaMalloc(&w->u, sizeof(int64_t) * (size_t)DW));
     LZ_CK(cudaMalloc(&w->fbuf, sizeof(double) * (size_t)DW));
     LZ_CK(cudaMalloc(&w->lz, sizeof(LzState)));
@@ -385,8 +390,11 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         LZ_CK(cudaEventCreate(&e));
         w->events.push_back(e);
     }
-    auto slot = [&](int j) -> int64_t* { return w->basis + (size_t)(stored ? j : j % 3) * (size_t)DW; };
+    auto slot = [&](int j) -> int64_t* { return w->basis + (size_t)(stored ? j : j % 3) * (size_t)w->stride; };
 
+    // a failed earlier call may have left a last-block counter mid-count
+    LZ_CK(cudaMemsetAsync(H.counter, 0, sizeof(unsigned int) * 4, s));
+    LZ_CK(cudaMemsetAsync(w->ritz_ctr, 0, sizeof(unsigned int), s));
     // start vector
     if (cfg->start == ED_START_USER) {
         if (!start) return ED_ERR_ARG;
@@ -427,7 +435,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             const int nk = j + 1;
             for (int pass = 0; pass < 2; ++pass) {
                 dim3 g(nk, kDotChunks);
-                k_lz_dots<<<g, kLzThreads, 0, s>>>(w->basis, DW, slot(j + 1), w->dot_lo, w->dot_hi);
+                k_lz_dots<<<g, kLzThreads, 0, s>>>(w->basis, DW, w->stride, slot(j + 1), w->dot_lo, w->dot_hi);
                 LZ_CK(cudaGetLastError());
                 std::vector<uint64_t> lo((size_t)nk * kDotChunks), hi((size_t)nk * kDotChunks);
                 std::vector<int> ev(nk + 2);
@@ -455,7 +463,8 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
                 fx_coefs(r, &rt, &rs, &F);
                 LZ_CK(cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * nk, cudaMemcpyHostToDevice, s));
                 LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * nk, cudaMemcpyHostToDevice, s));
-                k_lz_reorth<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), w->basis, DW, nk, w->coef_rt, w->coef_rs, F);
+                k_lz_reorth<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), w->basis, DW, w->stride, nk, w->coef_rt,
+                                                               w->coef_rs, F);
                 LZ_CK(cudaGetLastError());
                 launches += 2;
             }
@@ -525,8 +534,8 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
         double* out = evec_mem == ED_MEM_DEVICE ? evec : w->fbuf;
         const int g = lz_grid(DW);
-        k_ritz<<<g, kLzThreads, 0, s>>>(w->basis, DW, n, w->coef_rt, w->coef_rs, F, out, w->ritz_part, w->ritz_ctr,
-                                        w->inv_norm);
+        k_ritz<<<g, kLzThreads, 0, s>>>(w->basis, DW, w->stride, n, w->coef_rt, w->coef_rs, F, out, w->ritz_part,
+                                        w->ritz_ctr, w->inv_norm);
         LZ_CK(cudaGetLastError());
         k_scale<<<g, kLzThreads, 0, s>>>(out, DW, w->inv_norm);
         LZ_CK(cudaGetLastError());

@@ -241,8 +241,9 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec(const MvArgs a) {
             i128 s = 0;
             uint64_t m = 0;
             for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-                s += (i128)(((u128)lz->part_hi[i] << 64) | lz->part_lo[i]);
-                m = lz->part_max[i] > m ? lz->part_max[i] : m;
+                s += (i128)(((u128)__ldcg(lz->part_hi + i) << 64) | __ldcg(lz->part_lo + i));
+                const uint64_t pm = __ldcg(lz->part_max + i);
+                m = pm > m ? pm : m;
             }
             s = block_sum_i128(s, s128);
             m = block_max_u64(m, s64);
