@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
@@ -230,6 +231,7 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
     op->dimDN = op->bdn.count;
     if (op->dimUP > (1LL << 24) || op->dimDN > (1LL << 24)) { delete op; return ED_ERR_RANGE; }
     op->D = op->dimUP * op->dimDN;
+    if (op->D >= (1LL << 32)) { delete op; return ED_ERR_RANGE; }  // 32-bit element offsets
     std::string err;
     ed_status st = ed::build_spin(op->bup, desc->up_terms, desc->n_up_terms, cplx, &op->tup, nullptr, &err);
     if (st == ED_OK) st = ed::build_spin(op->bdn, desc->dn_terms, desc->n_dn_terms, cplx, &op->tdn, nullptr, &err);
@@ -284,16 +286,44 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
               upload(&op->d_dnEnt, td.ent.data(), td.ent.size()) == cudaSuccess &&
               upload(&op->d_upLen, tu.len.data(), tu.len.size()) == cudaSuccess &&
               upload(&op->d_dnLen, td.len.data(), td.len.size()) == cudaSuccess &&
+              upload(&op->d_upNpos, tu.npos.data(), tu.npos.size()) == cudaSuccess &&
+              upload(&op->d_dnNpos, td.npos.data(), td.npos.size()) == cudaSuccess &&
               upload(&op->d_dUPq, dq_u.data(), dq_u.size()) == cudaSuccess &&
               upload(&op->d_dDNq, dq_d.data(), dq_d.size()) == cudaSuccess &&
               upload(&op->d_stUP, op->bup.state.data(), op->bup.state.size()) == cudaSuccess &&
               upload(&op->d_stDN, op->bdn.state.data(), op->bdn.state.size()) == cudaSuccess &&
               cudaMalloc(&op->d_emax, sizeof(int)) == cudaSuccess && cudaMalloc(&op->d_flag, sizeof(int)) == cudaSuccess;
+    // CSR copies (row-contiguous entries) for the shared-memory kernel
+    auto csr = [](const ed::SpinTable& t, std::vector<uint32_t>* ptr, std::vector<uint32_t>* ent) {
+        ptr->assign(t.count + 1, 0);
+        ent->clear();
+        ent->reserve((size_t)t.nnz);
+        for (int64_t r = 0; r < t.count; ++r) {
+            for (int k = 0; k < t.len[r]; ++k) ent->push_back(t.ent[(size_t)k * t.count + r]);
+            (*ptr)[r + 1] = (uint32_t)ent->size();
+        }
+    };
+    std::vector<uint32_t> up_ptr, up_ent, dn_ptr, dn_ent;
+    csr(tu, &up_ptr, &up_ent);
+    csr(td, &dn_ptr, &dn_ent);
+    ok = ok && upload(&op->d_upPtr, up_ptr.data(), up_ptr.size()) == cudaSuccess &&
+         upload(&op->d_upEntC, up_ent.data(), up_ent.size()) == cudaSuccess &&
+         upload(&op->d_dnPtr, dn_ptr.data(), dn_ptr.size()) == cudaSuccess &&
+         upload(&op->d_dnEntC, dn_ent.data(), dn_ent.size()) == cudaSuccess &&
+         cudaMalloc(&op->d_err, sizeof(int)) == cudaSuccess && cudaMemset(op->d_err, 0, sizeof(int)) == cudaSuccess;
     if (!ok) { ed_op_destroy(op); return ED_ERR_ALLOC; }
+    a.upPtr = op->d_upPtr;
+    a.upEntC = op->d_upEntC;
+    a.dnPtr = op->d_dnPtr;
+    a.dnEntC = op->d_dnEntC;
+    a.dnNnz = (uint32_t)dn_ent.size();
+    a.err = op->d_err;
     a.upEnt = op->d_upEnt;
     a.dnEnt = op->d_dnEnt;
     a.upLen = op->d_upLen;
     a.dnLen = op->d_dnLen;
+    a.upNpos = op->d_upNpos;
+    a.dnNpos = op->d_dnNpos;
     a.dUPq = op->d_dUPq;
     a.dDNq = op->d_dDNq;
     a.stUP = op->d_stUP;
@@ -302,6 +332,10 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
     const int64_t row_bytes = op->dimDN * W * 8;
     op->stage_smem = row_bytes <= 160 * 1024 ? (int)row_bytes : 0;
     op->grid = ed::matvec_grid(op);
+    op->mv_threads = ed::matvec_threads(op->dimDN);
+    op->mv_fast = a.nclsUP <= 1 && a.nclsDN <= 1;
+    op->tma_smem = std::getenv("ED_NO_TMA") ? 0 : ed::tma_plan(op, &a);
+    if (op->tma_smem > 0) op->tma_grid = ed::tma_grid(op);
     *out = op;
     return ED_OK;
 }
@@ -312,6 +346,9 @@ ed_status ed_op_destroy(ed_op* op) {
     ed_op_ext* ox = static_cast<ed_op_ext*>(op);
     ed::lanczos_free_ws(ox->extra.lz_ws);
     cudaFree(op->d_upEnt); cudaFree(op->d_dnEnt); cudaFree(op->d_upLen); cudaFree(op->d_dnLen);
+    cudaFree(op->d_upNpos); cudaFree(op->d_dnNpos);
+    cudaFree(op->d_upPtr); cudaFree(op->d_upEntC); cudaFree(op->d_dnPtr); cudaFree(op->d_dnEntC);
+    cudaFree(op->d_err);
     cudaFree(op->d_dUPq); cudaFree(op->d_dDNq); cudaFree(op->d_stUP); cudaFree(op->d_stDN);
     cudaFree(op->d_xq); cudaFree(op->d_emax); cudaFree(op->d_flag); cudaFree(op->d_io);
     if (op->h_stage) cudaFreeHost(op->h_stage);

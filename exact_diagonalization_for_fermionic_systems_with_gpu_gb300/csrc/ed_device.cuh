@@ -120,6 +120,18 @@ __device__ __forceinline__ i128 shr_round(i128 v, int s) {
     return (v + ((i128)1 << (s - 1))) >> s;
 }
 
+// round(v / 2^s) as int64 for a (warp-uniform) s >= 0 when the result is
+// known to fit in 64 bits: one 128-bit add and a funnel shift.
+__device__ __forceinline__ int64_t shr_round_i64(i128 v, int s) {
+    if (s <= 0) return (int64_t)v;
+    if (s < 64) {
+        const u128 t = (u128)v + ((u128)1 << (s - 1));
+        const uint64_t lo = (uint64_t)t, hi = (uint64_t)(t >> 64);
+        return (int64_t)((lo >> s) | (hi << (64 - s)));
+    }
+    return (int64_t)((v + ((i128)1 << (s - 1))) >> s);
+}
+
 __device__ __forceinline__ int bitlen_u64(uint64_t v) { return v ? 64 - __clzll((long long)v) : 0; }
 
 // ---------------------------------------------------------- warp / block ops --
@@ -211,16 +223,18 @@ __device__ __forceinline__ double block_sum_f64(double v, double* scratch) {
 // "Last block done" election for single-pass grid reductions: every block
 // publishes its partial, fences, and bumps the counter; the block that sees
 // gridDim.x-1 finishes the reduction and resets the counter for reuse.
+// The block's partial must have been written by thread 0 (only that thread
+// fences before bumping the counter).
 __device__ __forceinline__ bool elect_last_block(unsigned int* counter) {
     __shared__ bool is_last;
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
-        unsigned int prev = atomicAdd(counter, 1u);
+        __threadfence();
+        const unsigned int prev = atomicAdd(counter, 1u);
         is_last = (prev == gridDim.x - 1);
+        if (is_last) __threadfence();
     }
     __syncthreads();
-    if (is_last) __threadfence();
     return is_last;
 }
 

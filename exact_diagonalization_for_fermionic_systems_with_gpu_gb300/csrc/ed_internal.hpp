@@ -19,8 +19,10 @@ struct MvArgs {
     int64_t dimUP, dimDN;
     const uint32_t* upEnt;
     const uint8_t* upLen;
+    const uint8_t* upNpos;
     const uint32_t* dnEnt;
     const uint8_t* dnLen;
+    const uint8_t* dnNpos;
     const int64_t* dUPq;  // folded diagonals, scale 2^-Fc
     const int64_t* dDNq;
     const uint64_t* stUP;
@@ -32,6 +34,15 @@ struct MvArgs {
     int unitUP, unitDN;   // single class with |coef| == 1 (coef_q == 2^Fc)
     int mergeUD;          // single class each, equal coefficients
     int bq_bits;          // bitlen of the per-unit row bound (acc <= 2^bq_bits * max|x_q|)
+    // CSR copies of the tables (shared-memory kernel)
+    const uint32_t* upPtr;
+    const uint32_t* upEntC;
+    const uint32_t* dnPtr;
+    const uint32_t* dnEntC;
+    uint32_t dnNnz;
+    int* err;             // device word set when a bounded wait gives up
+    // shared-memory plan of the TMA kernel (byte offsets)
+    int sm_row0, sm_row1, sm_dnptr, sm_dnent, sm_dnnpos, sm_ddnq, sm_stdn;
     // output
     double* y;            // FP64 output (perform path)
     const int* p_emax;    // device: max biased exponent of the FP64 input
@@ -60,6 +71,9 @@ struct ed_op {
     // device tables
     uint32_t *d_upEnt = nullptr, *d_dnEnt = nullptr;
     uint8_t *d_upLen = nullptr, *d_dnLen = nullptr;
+    uint8_t *d_upNpos = nullptr, *d_dnNpos = nullptr;
+    uint32_t *d_upPtr = nullptr, *d_upEntC = nullptr, *d_dnPtr = nullptr, *d_dnEntC = nullptr;
+    int* d_err = nullptr;
     int64_t *d_dUPq = nullptr, *d_dDNq = nullptr;
     uint64_t *d_stUP = nullptr, *d_stDN = nullptr;
     // perform-path workspace (grow-only)
@@ -72,6 +86,10 @@ struct ed_op {
     size_t d_io_bytes = 0;
     int stage_smem = 0;         // bytes of dynamic smem for the staged row (0 = no staging)
     int grid = 0;               // matvec grid
+    int mv_threads = 256;       // matvec CTA size
+    bool mv_fast = false;       // at most one coefficient class per spin
+    int tma_smem = 0;           // >0: the shared-memory/TMA matvec is used
+    int tma_grid = 0;
     std::string last_error;
 };
 
@@ -88,5 +106,9 @@ cudaError_t launch_matvec_f64(const ed_op* op, const int64_t* xq, const int* d_e
 cudaError_t launch_matvec_lz(const ed_op* op, const int64_t* xq, int64_t* uq, void* lz,
                              const uint64_t* d_mx, int step, cudaStream_t s);
 int matvec_grid(const ed_op* op);
+int matvec_threads(int64_t dimDN);
+int tma_plan(const ed_op* op, MvArgs* a);
+int tma_grid(const ed_op* op);
+cudaError_t launch_matvec_tma(const ed_op* op, const MvArgs& a, int out, cudaStream_t s);
 
 }  // namespace ed

@@ -28,9 +28,12 @@ cudaError_t launch_tridiag_lowest(int n, const double* alpha, const double* off,
 
 constexpr int kLzThreads = 256;
 
+// Element-wise Lanczos kernels: about 8 elements per thread and at most four
+// 256-thread CTAs per SM, so each thread keeps several loads in flight and
+// the last-block reduction has few partials.
 static int lz_grid(int64_t n) {
-    int64_t g = (n + 2 * kLzThreads - 1) / (2 * kLzThreads);
-    if (g > 152 * 8) g = 152 * 8;
+    int64_t g = (n + 8 * kLzThreads - 1) / (8 * kLzThreads);
+    if (g > 152 * 4) g = 152 * 4;
     return (int)(g < 1 ? 1 : g);
 }
 
@@ -98,12 +101,12 @@ __global__ void __launch_bounds__(kLzThreads) k_lz_start(const double* __restric
     });
 }
 
-// w_{j+1} = round((at0 u >> sh0 + at1 x >> sh1 + at2 p >> sh2) / 2^Fa)
+// w_{j+1} = round((at0 u + at1 x + at2 p) / 2^Fa)
 __global__ void __launch_bounds__(kLzThreads) k_lz_axpy(const int64_t* __restrict__ uq, const int64_t* __restrict__ xq,
                                                         const int64_t* __restrict__ pq, int64_t* __restrict__ wq,
                                                         int64_t n, LzState* lz, int j) {
     const int64_t a0 = lz->at[0], a1 = lz->at[1], a2 = lz->at[2];
-    const int s0 = lz->sh[0], s1 = lz->sh[1], s2 = lz->sh[2], Fa = lz->Fa;
+    const int Fa = lz->Fa;
     i128 ss = 0;
     uint64_t mx = 0;
     const int64_t npair = n >> 1;
@@ -112,12 +115,10 @@ __global__ void __launch_bounds__(kLzThreads) k_lz_axpy(const int64_t* __restric
     const longlong2* p2 = reinterpret_cast<const longlong2*>(pq);
     longlong2* w2 = reinterpret_cast<longlong2*>(wq);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npair; i += (int64_t)gridDim.x * blockDim.x) {
-        const longlong2 u = u2[i], x = x2[i], p = p2[i];
-        const i128 accx = (mul_wide(a0, u.x) >> s0) + (mul_wide(a1, x.x) >> s1) + (mul_wide(a2, p.x) >> s2);
-        const i128 accy = (mul_wide(a0, u.y) >> s0) + (mul_wide(a1, x.y) >> s1) + (mul_wide(a2, p.y) >> s2);
+        const longlong2 u = __ldg(u2 + i), x = __ldg(x2 + i), p = __ldg(p2 + i);
         longlong2 w;
-        w.x = (int64_t)shr_round(accx, Fa);
-        w.y = (int64_t)shr_round(accy, Fa);
+        w.x = shr_round_i64(mul_wide(a0, u.x) + mul_wide(a1, x.x) + mul_wide(a2, p.x), Fa);
+        w.y = shr_round_i64(mul_wide(a0, u.y) + mul_wide(a1, x.y) + mul_wide(a2, p.y), Fa);
         w2[i] = w;
         ss += (mul_wide(w.x, w.x) >> 16) + (mul_wide(w.y, w.y) >> 16);
         const uint64_t ax = (uint64_t)(w.x < 0 ? -w.x : w.x), ay = (uint64_t)(w.y < 0 ? -w.y : w.y);
@@ -126,8 +127,7 @@ __global__ void __launch_bounds__(kLzThreads) k_lz_axpy(const int64_t* __restric
     }
     if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
         const int64_t i = n - 1;
-        const i128 acc = (mul_wide(a0, uq[i]) >> s0) + (mul_wide(a1, xq[i]) >> s1) + (mul_wide(a2, pq[i]) >> s2);
-        const int64_t w = (int64_t)shr_round(acc, Fa);
+        const int64_t w = shr_round_i64(mul_wide(a0, uq[i]) + mul_wide(a1, xq[i]) + mul_wide(a2, pq[i]), Fa);
         wq[i] = w;
         ss += mul_wide(w, w) >> 16;
         const uint64_t a = (uint64_t)(w < 0 ? -w : w);

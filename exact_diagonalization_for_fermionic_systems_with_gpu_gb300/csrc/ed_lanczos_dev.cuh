@@ -56,27 +56,17 @@ __device__ inline void lz_after_matvec(LzState* lz, int j, i128 alpha_raw, uint6
     int kB = 0;
     if (B > 0.0) frexp(B, &kB);  // B < 2^kB
     const int e_w = kB - 54;
-    int F[3];
-    int Fmin = 1 << 20;
+    // One common number of fractional bits for the three integer
+    // coefficients: the largest |a_k| 2^-e_w sets it so every |at_k| < 2^62.
+    double amax = 0.0;
+    for (int k = 0; k < 3; ++k)
+        if (mm[k] != 0) amax = fmax(amax, fabs(a[k]) * ldexp(1.0, -e_w));
+    int ka = 0;
+    if (amax > 0.0) frexp(amax, &ka);  // amax < 2^ka
+    const int Fmin = 62 - ka;
     for (int k = 0; k < 3; ++k) {
-        F[k] = 0;
-        if (a[k] != 0.0 && mm[k] != 0) {
-            int ka;
-            frexp(fabs(a[k]) * ldexp(1.0, -e_w), &ka);  // |a_k| 2^-e_w < 2^ka
-            F[k] = 62 - ka;
-            Fmin = F[k] < Fmin ? F[k] : Fmin;
-        }
-    }
-    if (Fmin == (1 << 20)) Fmin = 62;
-    for (int k = 0; k < 3; ++k) {
-        int64_t at = 0;
-        int sh = 0;
-        if (a[k] != 0.0 && mm[k] != 0 && F[k] - Fmin < 120) {
-            at = llrint(ldexp(a[k], F[k] - e_w));
-            sh = F[k] - Fmin;
-        }
-        lz->at[k] = at;
-        lz->sh[k] = sh;
+        lz->at[k] = (mm[k] != 0 && a[k] != 0.0) ? llrint(ldexp(a[k], Fmin - e_w)) : 0;
+        lz->sh[k] = 0;
     }
     lz->Fa = Fmin;
     lz->e_w = e_w;

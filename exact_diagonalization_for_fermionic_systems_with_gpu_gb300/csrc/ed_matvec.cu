@@ -13,15 +13,18 @@
 // partial sum once, 64x64->128 bits, so the only rounding is the final one.
 #include <cuda_runtime.h>
 
+#include <cmath>
+
 #include "ed_device.cuh"
 #include "ed_internal.hpp"
 #include "ed_lanczos.hpp"
 #include "ed_lanczos_dev.cuh"
+#include "ed_matvec_common.cuh"
 
 namespace ed {
 using namespace dev;
 
-constexpr int kMvThreads = 256;
+constexpr int kMvMaxThreads = 512;
 constexpr int kUpStage = 256;  // up-table entries staged per row (max row length 255)
 
 // --------------------------------------------------------------- FX input --
@@ -67,40 +70,19 @@ cudaError_t launch_to_fx(const double* x, int64_t n, const int* d_emax, int64_t*
 
 // ------------------------------------------------------------------ matvec --
 
-__device__ __forceinline__ int64_t apply_sign(int64_t v, uint32_t e) {
-    int64_t m = (int64_t)((int32_t)e >> 31);  // 0 or -1
-    return (v ^ m) - m;
-}
-
-template <bool CPLX>
-__device__ __forceinline__ void apply_class(i128& ar, i128& ai, int64_t sr, int64_t si,
-                                            const int64_t* __restrict__ coef, int c, bool unit, int Fc) {
-    if (unit) {
-        ar += ((i128)sr) << Fc;
-        if (CPLX) ai += ((i128)si) << Fc;
-        return;
-    }
-    const int64_t cr = coef[2 * c];
-    ar += mul_wide(sr, cr);
-    if (CPLX) {
-        const int64_t ci = coef[2 * c + 1];
-        ai += mul_wide(si, cr);
-        if (ci != 0) {
-            ar -= mul_wide(si, ci);
-            ai += mul_wide(sr, ci);
-        }
-    }
-}
-
 // OUT = 0: FP64 y (operator apply); OUT = 1: FX u with the Lanczos epilogue.
-template <bool CPLX, bool STAGE, int OUT>
-__global__ void __launch_bounds__(kMvThreads) k_matvec(const MvArgs a) {
+// FAST: at most one coefficient class per spin; each row's entries are
+// ordered positive-then-negative, so a hop is one load and one 64-bit add.
+template <bool CPLX, bool STAGE, int OUT, bool FAST>
+__global__ void __launch_bounds__(kMvMaxThreads) k_matvec(const MvArgs a) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     constexpr int W = CPLX ? 2 : 1;
-    uint32_t* ups = reinterpret_cast<uint32_t*>(smem_raw);                 // kUpStage entries
-    int64_t* xs = reinterpret_cast<int64_t*>(smem_raw + kUpStage * sizeof(uint32_t));  // staged row
+    uint32_t* uoff = reinterpret_cast<uint32_t*>(smem_raw);                          // kUpStage
+    uint32_t* uent = uoff + kUpStage;                                                  // kUpStage
+    int64_t* xs = reinterpret_cast<int64_t*>(smem_raw + 2 * kUpStage * sizeof(uint32_t));  // staged row
 
-    const int64_t dimUP = a.dimUP, dimDN = a.dimDN;
+    const uint32_t dimUP = (uint32_t)a.dimUP, dimDN = (uint32_t)a.dimDN;
+    const int64_t* __restrict__ xq = a.xq;
     int E_out = 0, s_u = 0;
     if (OUT == 0) {
         E_out = fx_exp_from_emax(*a.p_emax) - a.Fc;
@@ -114,84 +96,105 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec(const MvArgs a) {
     const bool unitU = a.unitUP != 0 && a.nclsUP == 1;
     const bool unitD = a.unitDN != 0 && a.nclsDN == 1;
 
-    for (int64_t u = blockIdx.x; u < dimUP; u += gridDim.x) {
+    for (uint32_t u = blockIdx.x; u < dimUP; u += gridDim.x) {
         const int lenU = a.upLen[u];
+        const int nposU = FAST ? (int)a.upNpos[u] : 0;
         __syncthreads();  // the previous row's staged data is no longer read
-        for (int k = threadIdx.x; k < lenU; k += blockDim.x) ups[k] = a.upEnt[(int64_t)k * dimUP + u];
-        const int64_t* xrow = a.xq + u * dimDN * W;
+        for (int k = threadIdx.x; k < lenU; k += blockDim.x) {
+            const uint32_t e = a.upEnt[(size_t)k * dimUP + u];
+            uoff[k] = (e & kColMask) * dimDN;
+            if (!FAST) uent[k] = e;
+        }
+        const int64_t* xrow = xq + (size_t)u * dimDN * W;
         if (STAGE) {
-            const int64_t nrow = dimDN * W;
+            const uint32_t nrow = dimDN * W;
             if ((nrow & 1) == 0) {
                 const longlong2* src = reinterpret_cast<const longlong2*>(xrow);
                 longlong2* dst = reinterpret_cast<longlong2*>(xs);
-                for (int64_t i = threadIdx.x; i < nrow / 2; i += blockDim.x) dst[i] = src[i];
+                for (uint32_t i = threadIdx.x; i < nrow / 2; i += blockDim.x) dst[i] = __ldg(src + i);
             } else {
-                for (int64_t i = threadIdx.x; i < nrow; i += blockDim.x) xs[i] = xrow[i];
+                for (uint32_t i = threadIdx.x; i < nrow; i += blockDim.x) xs[i] = __ldg(xrow + i);
             }
             xrow = xs;
         }
         __syncthreads();
         const uint64_t stu = a.stUP[u];
         const int64_t du = a.dUPq[u];
+        const uint32_t ubase = u * dimDN;
 
-        for (int64_t d = threadIdx.x; d < dimDN; d += blockDim.x) {
+        for (uint32_t d = threadIdx.x; d < dimDN; d += blockDim.x) {
             i128 ar = 0, ai = 0;
             const int lenD = a.dnLen[d];
-            if (merge) {
-                int64_t sr = 0, si = 0;
-                for (int k = 0; k < lenU; ++k) {
-                    const uint32_t e = ups[k];
-                    const int64_t idx = ((int64_t)(e & kColMask) * dimDN + d) * W;
-                    if (CPLX) {
-                        const longlong2 v = *reinterpret_cast<const longlong2*>(a.xq + idx);
-                        sr += apply_sign(v.x, e);
-                        si += apply_sign(v.y, e);
-                    } else {
-                        sr += apply_sign(a.xq[idx], e);
-                    }
+            const uint32_t* __restrict__ de = a.dnEnt + d;
+            if (FAST) {
+                int64_t upr = 0, upi = 0, unr = 0, uni = 0;  // up term, + and - entries
+                int k = 0;
+#pragma unroll 4
+                for (; k < nposU; ++k) {
+                    int64_t r, i;
+                    load_x<CPLX>(xq, uoff[k] + d, r, i);
+                    upr += r;
+                    if (CPLX) upi += i;
                 }
-                for (int k = 0; k < lenD; ++k) {
-                    const uint32_t e = a.dnEnt[(int64_t)k * dimDN + d];
-                    const int64_t c = (int64_t)(e & kColMask) * W;
-                    sr += apply_sign(xrow[c], e);
-                    if (CPLX) si += apply_sign(xrow[c + 1], e);
+#pragma unroll 4
+                for (; k < lenU; ++k) {
+                    int64_t r, i;
+                    load_x<CPLX>(xq, uoff[k] + d, r, i);
+                    unr += r;
+                    if (CPLX) uni += i;
                 }
-                apply_class<CPLX>(ar, ai, sr, si, a.coefUP, 0, unitU, a.Fc);
+                int64_t dpr = 0, dpi = 0, dnr = 0, dni = 0;  // down term
+                const int nposD = a.dnNpos[d];
+                int kk = 0;
+#pragma unroll 4
+                for (; kk < nposD; ++kk) {
+                    const uint32_t c = (__ldg(de + (size_t)kk * dimDN) & kColMask) * W;
+                    dpr += xrow[c];
+                    if (CPLX) dpi += xrow[c + 1];
+                }
+#pragma unroll 4
+                for (; kk < lenD; ++kk) {
+                    const uint32_t c = (__ldg(de + (size_t)kk * dimDN) & kColMask) * W;
+                    dnr += xrow[c];
+                    if (CPLX) dni += xrow[c + 1];
+                }
+                if (merge) {
+                    apply_class<CPLX>(ar, ai, (upr + dpr) - (unr + dnr), (upi + dpi) - (uni + dni), a.coefUP, 0,
+                                      unitU, a.Fc);
+                } else {
+                    if (lenU) apply_class<CPLX>(ar, ai, upr - unr, upi - uni, a.coefUP, 0, unitU, a.Fc);
+                    if (lenD) apply_class<CPLX>(ar, ai, dpr - dnr, dpi - dni, a.coefDN, 0, unitD, a.Fc);
+                }
             } else {
-                // up term, entries sorted by class
+                // general tables: entries sorted by class, sign per entry
                 {
                     int cur = -1;
                     int64_t sr = 0, si = 0;
                     for (int k = 0; k < lenU; ++k) {
-                        const uint32_t e = ups[k];
+                        const uint32_t e = uent[k];
                         const int c = (int)((e >> kClassShift) & kClassMask);
                         if (c != cur) {
                             if (cur >= 0) apply_class<CPLX>(ar, ai, sr, si, a.coefUP, cur, unitU, a.Fc);
                             sr = 0; si = 0; cur = c;
                         }
-                        const int64_t idx = ((int64_t)(e & kColMask) * dimDN + d) * W;
-                        if (CPLX) {
-                            const longlong2 v = *reinterpret_cast<const longlong2*>(a.xq + idx);
-                            sr += apply_sign(v.x, e);
-                            si += apply_sign(v.y, e);
-                        } else {
-                            sr += apply_sign(a.xq[idx], e);
-                        }
+                        int64_t r, i;
+                        load_x<CPLX>(xq, uoff[k] + d, r, i);
+                        sr += apply_sign(r, e);
+                        if (CPLX) si += apply_sign(i, e);
                     }
                     if (cur >= 0) apply_class<CPLX>(ar, ai, sr, si, a.coefUP, cur, unitU, a.Fc);
                 }
-                // down term
                 {
                     int cur = -1;
                     int64_t sr = 0, si = 0;
                     for (int k = 0; k < lenD; ++k) {
-                        const uint32_t e = a.dnEnt[(int64_t)k * dimDN + d];
+                        const uint32_t e = __ldg(de + (size_t)k * dimDN);
                         const int c = (int)((e >> kClassShift) & kClassMask);
                         if (c != cur) {
                             if (cur >= 0) apply_class<CPLX>(ar, ai, sr, si, a.coefDN, cur, unitD, a.Fc);
                             sr = 0; si = 0; cur = c;
                         }
-                        const int64_t col = (int64_t)(e & kColMask) * W;
+                        const uint32_t col = (e & kColMask) * W;
                         sr += apply_sign(xrow[col], e);
                         if (CPLX) si += apply_sign(xrow[col + 1], e);
                     }
@@ -201,22 +204,22 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec(const MvArgs a) {
             // diagonal: folded site potentials + U * double occupancy
             const int64_t xr = xrow[d * W];
             const int64_t xi = CPLX ? xrow[d * W + 1] : 0;
-            const int64_t dq = du + a.dDNq[d] + a.Uq * (int64_t)__popcll(stu & a.stDN[d] & a.mask);
+            const int64_t dq = du + __ldg(a.dDNq + d) + a.Uq * (int64_t)__popcll(stu & __ldg(a.stDN + d) & a.mask);
             ar += mul_wide(dq, xr);
             if (CPLX) ai += mul_wide(dq, xi);
 
-            const int64_t o = (u * dimDN + d) * W;
+            const size_t o = (size_t)(ubase + d) * W;
             if (OUT == 0) {
                 a.y[o] = i128_to_f64(ar, E_out);
                 if (CPLX) a.y[o + 1] = i128_to_f64(ai, E_out);
             } else {
-                const int64_t qr = (int64_t)shr_round(ar, s_u);
+                const int64_t qr = shr_round_i64(ar, s_u);
                 a.uq[o] = qr;
                 dot += mul_wide(xr, qr) >> 24;
                 uint64_t aq = (uint64_t)(qr < 0 ? -qr : qr);
                 mx = aq > mx ? aq : mx;
                 if (CPLX) {
-                    const int64_t qi = (int64_t)shr_round(ai, s_u);
+                    const int64_t qi = shr_round_i64(ai, s_u);
                     a.uq[o + 1] = qi;
                     dot += mul_wide(xi, qi) >> 24;
                     aq = (uint64_t)(qi < 0 ? -qi : qi);
@@ -226,33 +229,7 @@ __global__ void __launch_bounds__(kMvThreads) k_matvec(const MvArgs a) {
         }
     }
 
-    if (OUT == 1) {
-        __shared__ i128 s128[32];
-        __shared__ uint64_t s64[32];
-        LzState* lz = reinterpret_cast<LzState*>(a.lz);
-        const i128 bs = block_sum_i128(dot, s128);
-        const uint64_t bm = block_max_u64(mx, s64);
-        if (threadIdx.x == 0) {
-            lz->part_lo[blockIdx.x] = (uint64_t)bs;
-            lz->part_hi[blockIdx.x] = (uint64_t)((u128)bs >> 64);
-            lz->part_max[blockIdx.x] = bm;
-        }
-        if (elect_last_block(&lz->counter[0])) {
-            i128 s = 0;
-            uint64_t m = 0;
-            for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) {
-                s += (i128)(((u128)__ldcg(lz->part_hi + i) << 64) | __ldcg(lz->part_lo + i));
-                const uint64_t pm = __ldcg(lz->part_max + i);
-                m = pm > m ? pm : m;
-            }
-            s = block_sum_i128(s, s128);
-            m = block_max_u64(m, s64);
-            if (threadIdx.x == 0) {
-                lz_after_matvec(lz, a.step, s, m, s_u, a.Fc);
-                lz->counter[0] = 0;
-            }
-        }
-    }
+    if (OUT == 1) mv_lanczos_epilogue(a, dot, mx, s_u);
 }
 
 // ------------------------------------------------------------------ launch --
@@ -264,20 +241,41 @@ int matvec_grid(const ed_op* op) {
     return (int)(g < 1 ? 1 : g);
 }
 
-template <bool CPLX, int OUT>
-static cudaError_t launch_mv(const ed_op* op, const MvArgs& a, cudaStream_t s) {
-    const int smem = kUpStage * (int)sizeof(uint32_t) + op->stage_smem;
+// Threads per CTA: a multiple of 32 in [128, 512] that covers the down index
+// in as few passes as possible with little idle tail.
+int matvec_threads(int64_t dimDN) {
+    int best = 256;
+    double best_eff = 0.0;
+    for (int t = 128; t <= kMvMaxThreads; t += 32) {
+        const int64_t passes = (dimDN + t - 1) / t;
+        const double eff = (double)dimDN / (double)(passes * t);
+        if (eff > best_eff + 1e-9 || (std::fabs(eff - best_eff) < 1e-9 && t > best)) {
+            best_eff = eff;
+            best = t;
+        }
+    }
+    return best;
+}
+
+template <bool CPLX, int OUT, bool FAST>
+static cudaError_t launch_mv3(const ed_op* op, const MvArgs& a, cudaStream_t s) {
+    const int smem = 2 * kUpStage * (int)sizeof(uint32_t) + op->stage_smem;
     if (op->stage_smem > 0) {
-        auto kern = k_matvec<CPLX, true, OUT>;
+        auto kern = k_matvec<CPLX, true, OUT, FAST>;
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
             if (e != cudaSuccess) return e;
         }
-        kern<<<op->grid, kMvThreads, smem, s>>>(a);
+        kern<<<op->grid, op->mv_threads, smem, s>>>(a);
     } else {
-        k_matvec<CPLX, false, OUT><<<op->grid, kMvThreads, smem, s>>>(a);
+        k_matvec<CPLX, false, OUT, FAST><<<op->grid, op->mv_threads, smem, s>>>(a);
     }
     return cudaGetLastError();
+}
+
+template <bool CPLX, int OUT>
+static cudaError_t launch_mv(const ed_op* op, const MvArgs& a, cudaStream_t s) {
+    return op->mv_fast ? launch_mv3<CPLX, OUT, true>(op, a, s) : launch_mv3<CPLX, OUT, false>(op, a, s);
 }
 
 cudaError_t launch_matvec_f64(const ed_op* op, const int64_t* xq, const int* d_emax, double* y,
@@ -286,6 +284,7 @@ cudaError_t launch_matvec_f64(const ed_op* op, const int64_t* xq, const int* d_e
     a.xq = xq;
     a.p_emax = d_emax;
     a.y = y;
+    if (op->tma_smem > 0) return launch_matvec_tma(op, a, 0, s);
     return op->cplx ? launch_mv<true, 0>(op, a, s) : launch_mv<false, 0>(op, a, s);
 }
 
@@ -297,6 +296,7 @@ cudaError_t launch_matvec_lz(const ed_op* op, const int64_t* xq, int64_t* uq, vo
     a.lz = lz;
     a.step = step;
     a.p_mx = d_mx;
+    if (op->tma_smem > 0) return launch_matvec_tma(op, a, 1, s);
     return op->cplx ? launch_mv<true, 1>(op, a, s) : launch_mv<false, 1>(op, a, s);
 }
 

@@ -221,9 +221,12 @@ ed_status build_spin(const SpinBasis& basis, const ed_term* terms, int n_terms,
             tmp.push_back({c, w});
             row_abs += std::abs(e.value);
         }
+        // order within a row: by class, positive entries before negative
+        // ones (the sums are exact integers, so the order is free)
         std::stable_sort(tmp.begin(), tmp.end(),
                          [](const std::pair<int, uint32_t>& x, const std::pair<int, uint32_t>& y) {
-                             return x.first < y.first;
+                             if (x.first != y.first) return x.first < y.first;
+                             return (x.second & kSignBit) < (y.second & kSignBit);
                          });
         for (auto& p : tmp) packed[a].push_back(p.second);
         max_len = std::max(max_len, (int)packed[a].size());
@@ -238,9 +241,15 @@ ed_status build_spin(const SpinBasis& basis, const ed_term* terms, int n_terms,
     table->max_len = max_len;
     table->ent.assign((size_t)std::max(max_len, 1) * count, 0u);
     table->len.assign(count, 0);
+    table->npos.assign(count, 0);
     for (int64_t a = 0; a < count; ++a) {
         table->len[a] = (uint8_t)packed[a].size();
-        for (size_t s = 0; s < packed[a].size(); ++s) table->ent[s * count + a] = packed[a][s];
+        int np = 0;
+        for (size_t s = 0; s < packed[a].size(); ++s) {
+            table->ent[s * count + a] = packed[a][s];
+            if (!(packed[a][s] & kSignBit)) ++np;
+        }
+        table->npos[a] = (uint8_t)np;
     }
     if (ell && ell->overflow) return ED_ERR_TABLE;
     return ED_OK;

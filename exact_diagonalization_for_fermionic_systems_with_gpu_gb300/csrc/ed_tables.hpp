@@ -57,6 +57,8 @@ struct SpinTable {
     int max_len = 0;                      // slots per row in the slot-major layout
     std::vector<uint32_t> ent;            // ent[s * count + a], s < max_len
     std::vector<uint8_t> len;             // entries in row a
+    std::vector<uint8_t> npos;            // single-class tables: the first npos[a]
+                                          // entries of row a are +, the rest -
     std::vector<double> diag_re, diag_im; // folded diagonal (Make_N terms)
     std::vector<std::complex<double>> coef; // class -> coefficient (sign stripped)
     bool complex_coef = false;            // any class with a nonzero imaginary part

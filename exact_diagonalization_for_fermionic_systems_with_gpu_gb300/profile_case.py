@@ -1,0 +1,78 @@
+"""Small, fixed workloads for profiling the kernels under ncu.
+
+    python -m exact_diagonalization_for_fermionic_systems_with_gpu_gb300.profile_case \
+        --case kagome12 --what lanczos --steps 20
+
+--what lanczos : one fixed-step Lanczos solve (matvec + axpy kernels)
+--what perform : --steps operator applies through the FP64 C-ABI path
+Cases: kagome12 (6+6, dim 853,776, L2-resident vectors), chain14 (7+7 open
+chain with disorder, dim 11,778,624, vectors larger than L2), lieb18
+(9+9, dim 2.36e9; perform only, ~57 GB of device memory).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import time
+
+import numpy as np
+
+from . import lattices as L
+from .hubbard import H_TBq, Hubbard, random_vector
+from . import _capi
+
+
+def build_case(name: str):
+    if name == "kagome12":
+        t = L.kagome12()
+        return Hubbard(H_TBq(12, 6).extend(t), H_TBq(12, 6).extend(t), 8.0)
+    if name == "chain14":
+        eps = random_vector(14, 100) * 6.0
+        t = L.chain(14, periodic=False, eps=eps)
+        return Hubbard(H_TBq(14, 7).extend(t), H_TBq(14, 7).extend(t), 1.0)
+    if name == "lieb18":
+        t = L.lieb18()
+        return Hubbard(H_TBq(18, 9).extend(t), H_TBq(18, 9).extend(t), 4.0)
+    if name == "kagome12_flux":
+        t = L.kagome12(flux=0.3)
+        return Hubbard(H_TBq(12, 6).extend(t), H_TBq(12, 6).extend(t), 4.0)
+    raise SystemExit(f"unknown case {name}")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default="kagome12")
+    ap.add_argument("--what", default="lanczos", choices=["lanczos", "perform"])
+    ap.add_argument("--steps", type=int, default=20)
+    args = ap.parse_args()
+    import torch
+    op = build_case(args.case)
+    lib = _capi.load()
+    t0 = time.perf_counter()
+    if args.what == "lanczos":
+        cfg = _capi.ed_lanczos_cfg(max_steps=args.steps, mode=_capi.ED_LANCZOS_FIXED, reorth=0,
+                                   ritz=_capi.ED_RITZ_NONE, start=_capi.ED_START_RANDOM, profile=1, seed=0)
+        res = _capi.ed_lanczos_result()
+        _capi.check(lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0, None, 0, None, None, C.byref(res), None),
+                    "ed_lanczos_run")
+        print(f"E0 {res.e0:.12f} steps {res.steps} matvec {res.matvec_ms / res.n_matvec * 1e3:.1f} us "
+              f"axpy {res.axpy_ms / res.n_matvec * 1e3:.1f} us")
+    else:
+        dt = torch.complex128 if op.is_complex else torch.float64
+        x = torch.empty(op.rows(), dtype=torch.float64 if not op.is_complex else torch.float64,
+                        device="cuda")
+        n = op.rows() * (2 if op.is_complex else 1)
+        x = torch.empty(n, dtype=torch.float64, device="cuda")
+        _capi.check(lib.ed_random_vector_device(n, 1, C.c_void_p(x.data_ptr()), None), "random")
+        x = x.view(dt) if op.is_complex else x
+        y = torch.empty_like(x)
+        for _ in range(args.steps):
+            op.Hubbard_mv(x, y)
+        torch.cuda.synchronize()
+        print(f"{args.steps} applies, |y| = {float(torch.linalg.vector_norm(y)):.6e}")
+    print(f"wall {time.perf_counter() - t0:.2f} s")
+    op.close()
+
+
+if __name__ == "__main__":
+    main()
