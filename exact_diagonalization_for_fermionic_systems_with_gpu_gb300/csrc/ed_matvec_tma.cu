@@ -26,7 +26,7 @@ using namespace dev;
 
 constexpr int kTmaThreads = 512;
 constexpr int kTmaUpStage = 256;
-constexpr long long kMaxSpin = 1LL << 26;
+constexpr long long kMaxSpin = 1LL << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
