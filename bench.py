@@ -203,12 +203,15 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
 
     cfg = _capi.ed_lanczos_cfg(max_steps=STEPS, mode=_capi.ED_LANCZOS_FIXED, reorth=0, ritz=_capi.ED_RITZ_STORED,
-                               start=_capi.ED_START_RANDOM, profile=1, seed=SEED)
+                               start=_capi.ED_START_RANDOM, profile=0, seed=SEED)
+    # same solve with CUDA events around every matvec / axpy launch (roofline)
+    cfg_prof = _capi.ed_lanczos_cfg(max_steps=STEPS, mode=_capi.ED_LANCZOS_FIXED, reorth=0,
+                                    ritz=_capi.ED_RITZ_STORED, start=_capi.ED_START_RANDOM, profile=1, seed=SEED)
     evec_dev = torch.empty(D, dtype=torch.float64, device="cuda")
     res = _capi.ed_lanczos_result()
 
-    def solve_device():
-        st = lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0, C.c_void_p(evec_dev.data_ptr()),
+    def solve_device(c=cfg):
+        st = lib.ed_lanczos_run(op.handle, C.byref(c), None, 0, C.c_void_p(evec_dev.data_ptr()),
                                 _capi.ED_MEM_DEVICE, None, None, C.byref(res), None)
         _capi.check(st, "ed_lanczos_run")
         return res.e0
@@ -230,14 +233,20 @@ def main():
             ev1.record()
             torch.cuda.synchronize()
             ms.append(ev0.elapsed_time(ev1))
-            mv_ms += res.matvec_ms
-            ax_ms += res.axpy_ms
-            nmv += res.n_matvec
             launches += res.launches
     torch.cuda.synchronize()
     barrier(world)
     ms_per_step = max_over_ranks(world, sum(ms) / len(ms))
     value = world * STEPS / (ms_per_step / 1000.0)
+    # per-kernel device time: events on the launching stream around each
+    # matvec / axpy of additional solves (not part of `value`)
+    for _ in range(3):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        solve_device(cfg_prof)
+        mv_ms += res.matvec_ms
+        ax_ms += res.axpy_ms
+        nmv += res.n_matvec
 
     # e2e: host start vector in, host Ritz vector out, through the C ABI
     f_host = torch.from_numpy(ed.random_vector(D, SEED)).pin_memory()

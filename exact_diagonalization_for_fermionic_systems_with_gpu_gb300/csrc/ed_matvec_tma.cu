@@ -110,10 +110,19 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_matvec_tma(const MvArgs a) {
         if (blockIdx.x < dimUP)
             tma_row_load(row0, xq + (size_t)blockIdx.x * dimDN * W, row_bytes, &bar[0]);
     }
-    // down-spin operator into shared memory (overlaps the first row copy)
-    for (uint32_t i = tid; i <= dimDN; i += T) dptr[i] = __ldg(a.dnPtr + i);
+    // down-spin operator into shared memory (overlaps the first row copy);
+    // 16-byte loads, several in flight per thread
     const uint32_t nnz = a.dnNnz;
-    for (uint32_t i = tid; i < nnz; i += T) dent[i] = __ldg(a.dnEntC + i);
+    {
+        const uint32_t n4 = nnz / 4;
+        const uint4* s4 = reinterpret_cast<const uint4*>(a.dnEntC);
+        uint4* d4 = reinterpret_cast<uint4*>(dent);
+#pragma unroll 4
+        for (uint32_t i = tid; i < n4; i += T) d4[i] = __ldg(s4 + i);
+        for (uint32_t i = 4 * n4 + tid; i < nnz; i += T) dent[i] = __ldg(a.dnEntC + i);
+    }
+    for (uint32_t i = tid; i <= dimDN; i += T) dptr[i] = __ldg(a.dnPtr + i);
+#pragma unroll 2
     for (uint32_t i = tid; i < dimDN; i += T) {
         dnpos[i] = FAST ? __ldg(a.dnNpos + i) : 0;
         ddq[i] = __ldg(a.dDNq + i);
