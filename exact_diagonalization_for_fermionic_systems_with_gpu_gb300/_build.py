@@ -19,7 +19,8 @@ LIBDIR = PKG / "_lib"
 BUILD = PKG / "_build"
 LIBNAME = "libedgb300.so"
 
-SOURCES = ["ed_tables.cpp", "ed_matvec.cu", "ed_matvec_tma.cu", "ed_lanczos.cu", "ed_tridiag.cu", "ed_capi.cu"]
+SOURCES = ["ed_tables.cpp", "ed_matvec.cu", "ed_matvec_tma.cu", "ed_lanczos.cu", "ed_tridiag.cu", "ed_capi.cu",
+           "ed_observables.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", str(ROOT / "include")]
@@ -63,7 +64,7 @@ def build(force: bool = False) -> Path:
         objs = list(ex.map(_compile, SOURCES))
     LIBDIR.mkdir(parents=True, exist_ok=True)
     tmp = LIBDIR / (LIBNAME + ".tmp")
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lcusolver"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

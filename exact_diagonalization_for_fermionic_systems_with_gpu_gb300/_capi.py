@@ -54,6 +54,15 @@ class ed_lanczos_result(C.Structure):
                 ("matvec_ms", C.c_double), ("axpy_ms", C.c_double), ("n_matvec", C.c_int32), ("pad_", C.c_int32)]
 
 
+class ed_kubo_cfg(C.Structure):
+    _fields_ = [("lanczos_steps", C.c_int32), ("n_omega", C.c_int32), ("omega_step", C.c_double),
+                ("delta", C.c_double), ("omega_cutoff", C.c_double), ("volume", C.c_double)]
+
+
+class ed_kubo_result(C.Structure):
+    _fields_ = [("drude", C.c_double), ("kinetic", C.c_double), ("vertex", C.c_double)]
+
+
 # name -> (restype, argtypes); the list is also the export check used by the tests
 SIGNATURES = {
     "ed_status_string": (C.c_char_p, [C.c_int]),
@@ -78,6 +87,19 @@ SIGNATURES = {
     "ed_random_vector": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p]),
     "ed_random_vector_device": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p, C.c_void_p]),
     "ed_tridiag_lowest": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ed_vec_dot": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "ed_vec_zdot": (C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "ed_op_expect": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "ed_site_densities": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]),
+    "ed_continued_fraction": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_double, C.c_double, C.c_int,
+                                        C.c_void_p, C.c_void_p]),
+    "ed_drude_kubo": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                C.POINTER(ed_kubo_cfg), C.POINTER(ed_kubo_result), C.c_void_p, C.c_void_p]),
+    "ed_response": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p,
+                              C.c_void_p, C.c_void_p]),
+    "ed_entanglement_entropy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_void_p, C.c_void_p,
+                                          C.c_void_p]),
 }
 
 

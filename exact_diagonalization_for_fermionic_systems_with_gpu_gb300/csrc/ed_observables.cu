@@ -1,0 +1,620 @@
+// ed_observables.cu — what the drivers compute from a ground state:
+// dot products, expectation values, site densities and double occupancies
+// (Hellmann-Feynman derivatives), the continued-fraction correlator and the
+// Kubo Drude weight (HubMatrix_GPU.cuh:820-849,
+// drude_v2_cal_Kagome_randomHop.cu:183-220), the second-order flux response
+// by a Lanczos solve of the linear-response equation, and the half-system
+// entanglement entropy (entangle_entropy.h:22-44,177-197 + cusolverDnDgesvd).
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/ed_hubbard.h"
+#include "ed_device.cuh"
+#include "ed_internal.hpp"
+
+namespace ed {
+using namespace dev;
+
+constexpr int kObThreads = 256;
+constexpr int kObBlocks = 152 * 2;
+
+// ----------------------------------------------------------------- dots --
+// Deterministic FP64 dot: fixed grid, per-block sums in fixed order, then
+// one block sums the block results in index order.
+__global__ void k_dot(const double* __restrict__ x, const double* __restrict__ y, int64_t n, int conj_pairs,
+                      double* part) {
+    double re = 0.0, im = 0.0;
+    if (conj_pairs) {
+        for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+            const double xr = x[2 * k], xi = x[2 * k + 1], yr = y[2 * k], yi = y[2 * k + 1];
+            re = fma(xr, yr, fma(xi, yi, re));
+            im = fma(xr, yi, fma(-xi, yr, im));
+        }
+    } else {
+        for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+            re = fma(x[k], y[k], re);
+    }
+    __shared__ double sd[32];
+    const double br = block_sum_f64(re, sd);
+    const double bi = block_sum_f64(im, sd);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = br;
+        part[2 * blockIdx.x + 1] = bi;
+    }
+}
+
+__global__ void k_dot_final(const double* part, int nb, double* out) {
+    if (threadIdx.x == 0) {
+        double r = 0.0, i = 0.0;
+        for (int b = 0; b < nb; ++b) { r += part[2 * b]; i += part[2 * b + 1]; }
+        out[0] = r;
+        out[1] = i;
+    }
+}
+
+// y = x - c * p (complex pairs when cplx), c = (cr, ci)
+__global__ void k_project(const double* __restrict__ x, const double* __restrict__ p, const double* __restrict__ c,
+                          int64_t n, int cplx, double* __restrict__ y) {
+    const double cr = c[0], ci = c[1];
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        if (cplx) {
+            const double pr = p[2 * k], pi = p[2 * k + 1];
+            y[2 * k] = x[2 * k] - (cr * pr - ci * pi);
+            y[2 * k + 1] = x[2 * k + 1] - (cr * pi + ci * pr);
+        } else {
+            y[k] = x[k] - cr * p[k];
+        }
+    }
+}
+
+// ------------------------------------------------------ site densities --
+// |psi|^2 in 2^-60 fixed point; P_up[u] (row sums, block-exact), P_dn[d]
+// (column sums) and per-site double occupancy as exact int64 atomics, so the
+// result does not depend on scheduling.
+__global__ void k_densities(const double* __restrict__ psi, int64_t dimUP, int64_t dimDN, int cplx,
+                            const uint64_t* __restrict__ stUP, const uint64_t* __restrict__ stDN,
+                            unsigned long long* __restrict__ pup, unsigned long long* __restrict__ pdn,
+                            unsigned long long* __restrict__ docc) {
+    __shared__ unsigned long long sdocc[64];
+    __shared__ unsigned long long srow[32];
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) sdocc[i] = 0;
+    __syncthreads();
+    for (int64_t u = blockIdx.x; u < dimUP; u += gridDim.x) {
+        const uint64_t su = stUP[u];
+        unsigned long long rsum = 0;
+        for (int64_t d = threadIdx.x; d < dimDN; d += blockDim.x) {
+            const int64_t k = u * dimDN + d;
+            double w;
+            if (cplx) w = fma(psi[2 * k], psi[2 * k], psi[2 * k + 1] * psi[2 * k + 1]);
+            else w = psi[k] * psi[k];
+            const unsigned long long q = (unsigned long long)f64_to_fx(w, -60);
+            rsum += q;
+            atomicAdd(pdn + d, q);
+            uint64_t both = su & stDN[d];
+            while (both) {
+                const int i = __ffsll((long long)both) - 1;
+                atomicAdd(sdocc + i, q);
+                both &= both - 1;
+            }
+        }
+        // exact block sum of the row
+        for (int off = 16; off > 0; off >>= 1) rsum += __shfl_down_sync(0xffffffffu, rsum, off);
+        if ((threadIdx.x & 31) == 0) srow[threadIdx.x >> 5] = rsum;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long t = 0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += srow[w];
+            pup[u] = t;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < 64; i += blockDim.x)
+        if (sdocc[i]) atomicAdd(docc + i, sdocc[i]);
+}
+
+// ------------------------------------------------- continued fraction --
+// g(w) = norm2 / (w + E - a0 - b1^2 / (w + E - a1 - ...)), evaluated from
+// the bottom like HubMatrix_GPU.cuh:830-834; one thread per frequency.
+__global__ void k_cfrac(int n, const double* __restrict__ a, const double* __restrict__ b, double norm2, double energy,
+                        int nw, const double* __restrict__ w, double* __restrict__ g) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nw) return;
+    const double wr = w[2 * idx], wi = w[2 * idx + 1];
+    double zr = wr + energy - a[n - 1], zi = wi;
+    double den = zr * zr + zi * zi;
+    double gr = zr / den, gi = -zi / den;
+    for (int i = n - 2; i >= 0; --i) {
+        const double bb = b[i + 1] * b[i + 1];
+        const double tr = wr + energy - a[i] - gr * bb, ti = wi - gi * bb;
+        den = tr * tr + ti * ti;
+        gr = tr / den;
+        gi = -ti / den;
+    }
+    g[2 * idx] = norm2 * gr;
+    g[2 * idx + 1] = norm2 * gi;
+}
+
+// ------------------------------------------------- entanglement matrix --
+// psi[u, d] -> block s = (nA_up(u), nA_dn(d)), stored column-major with the
+// larger dimension as rows (gesvd needs m >= n).
+struct EeMeta {
+    const int32_t* nA_up;   // per up state: particles in A
+    const int32_t* ia_up;   // rank of its A part among A parts with that count
+    const int32_t* ib_up;   // rank of its B part
+    const int32_t* nA_dn;
+    const int32_t* ia_dn;
+    const int32_t* ib_dn;
+    const int64_t* blk_off;  // [(QA_up+1)*(QA_dn+1)] element offset of block
+    const int32_t* blk_rowsA;  // rows of the A side (rA)
+    const int32_t* blk_colsB;  // cols of the B side (cB)
+    const int32_t* dimA_dn;    // A-part count of the down spin for each nA_dn
+    const int32_t* dimB_dn;    // B-part count of the down spin for each nA_dn
+    int nqd;                   // QA_dn + 1 (stride of the block table)
+};
+
+__global__ void k_ee_scatter(const double* __restrict__ psi, int64_t dimUP, int64_t dimDN, EeMeta m,
+                             double* __restrict__ blocks) {
+    const int64_t n = dimUP * dimDN;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = k / dimDN, d = k - u * dimDN;
+        const int au = m.nA_up[u], ad = m.nA_dn[d];
+        const int s = au * m.nqd + ad;
+        const int64_t rA = m.blk_rowsA[s], cB = m.blk_colsB[s];
+        const int64_t row = (int64_t)m.ia_up[u] * m.dimA_dn[ad] + m.ia_dn[d];
+        const int64_t col = (int64_t)m.ib_up[u] * m.dimB_dn[ad] + m.ib_dn[d];
+        int64_t pos;
+        if (rA >= cB) pos = col * rA + row;  // column-major rA x cB
+        else pos = row * cB + col;           // column-major cB x rA (the transpose)
+        blocks[m.blk_off[s] + pos] = psi[k];
+    }
+}
+
+cudaError_t launch_random(double* f, int64_t n, uint64_t seed, cudaStream_t s);
+
+}  // namespace ed
+
+namespace {
+
+using ed::kObBlocks;
+using ed::kObThreads;
+
+struct ObScratch {
+    double* part = nullptr;
+    double* out = nullptr;
+};
+
+int ob_grid(int64_t n) {
+    int64_t g = (n + kObThreads - 1) / kObThreads;
+    if (g > kObBlocks) g = kObBlocks;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// dot into a host pair (re, im); x, y device
+ed_status dev_dot(const double* x, const double* y, int64_t n, bool cplx, double* out2, cudaStream_t s) {
+    double *part = nullptr, *res = nullptr;
+    const int g = ob_grid(n);
+    if (cudaMallocAsync(&part, sizeof(double) * 2 * g, s) != cudaSuccess) return ED_ERR_ALLOC;
+    if (cudaMallocAsync(&res, sizeof(double) * 2, s) != cudaSuccess) { cudaFreeAsync(part, s); return ED_ERR_ALLOC; }
+    ed::k_dot<<<g, kObThreads, 0, s>>>(x, y, n, cplx ? 1 : 0, part);
+    ed::k_dot_final<<<1, 32, 0, s>>>(part, g, res);
+    cudaError_t e = cudaMemcpyAsync(out2, res, sizeof(double) * 2, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(part, s);
+    cudaFreeAsync(res, s);
+    return e == cudaSuccess ? ED_OK : ED_ERR_CUDA;
+}
+
+// Copy a vector to the device when it lives on the host; *dev is the
+// device pointer to use, *owned the buffer to free.
+ed_status to_device(const double* p, int64_t nd, int mem, const double** dev, double** owned, cudaStream_t s) {
+    *owned = nullptr;
+    if (mem == ED_MEM_DEVICE) { *dev = p; return ED_OK; }
+    if (cudaMallocAsync(owned, sizeof(double) * nd, s) != cudaSuccess) return ED_ERR_ALLOC;
+    if (cudaMemcpyAsync(*owned, p, sizeof(double) * nd, cudaMemcpyHostToDevice, s) != cudaSuccess) return ED_ERR_CUDA;
+    *dev = *owned;
+    return ED_OK;
+}
+
+int64_t binom_i(int n, int k) { return ed::binom(n, k); }
+
+uint64_t pext64(uint64_t x, uint64_t mask) {
+    uint64_t r = 0;
+    int k = 0;
+    while (mask) {
+        const int p = __builtin_ctzll(mask);
+        if ((x >> p) & 1ULL) r |= 1ULL << k;
+        ++k;
+        mask &= mask - 1;
+    }
+    return r;
+}
+
+int64_t cns_rank(uint64_t w) {
+    int64_t r = 0;
+    int k = 0;
+    while (w) {
+        const int p = __builtin_ctzll(w);
+        r += ed::binom(p, k + 1);
+        ++k;
+        w &= w - 1;
+    }
+    return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+ed_status ed_vec_dot(int64_t n, const double* x, const double* y, int mem, double* out, void* stream) {
+    if (n < 0 || !out || (n && (!x || !y)) || (mem != ED_MEM_HOST && mem != ED_MEM_DEVICE)) return ED_ERR_ARG;
+    if (mem == ED_MEM_HOST) {
+        double s = 0.0;
+        for (int64_t k = 0; k < n; ++k) s = std::fma(x[k], y[k], s);
+        *out = s;
+        return ED_OK;
+    }
+    double r[2];
+    ed_status st = dev_dot(x, y, n, false, r, reinterpret_cast<cudaStream_t>(stream));
+    if (st == ED_OK) *out = r[0];
+    return st;
+}
+
+ed_status ed_vec_zdot(int64_t n, const double* x, const double* y, int mem, double* out, void* stream) {
+    if (n < 0 || !out || (n && (!x || !y)) || (mem != ED_MEM_HOST && mem != ED_MEM_DEVICE)) return ED_ERR_ARG;
+    if (mem == ED_MEM_HOST) {
+        double re = 0.0, im = 0.0;
+        for (int64_t k = 0; k < n; ++k) {
+            re = std::fma(x[2 * k], y[2 * k], std::fma(x[2 * k + 1], y[2 * k + 1], re));
+            im = std::fma(x[2 * k], y[2 * k + 1], std::fma(-x[2 * k + 1], y[2 * k], im));
+        }
+        out[0] = re;
+        out[1] = im;
+        return ED_OK;
+    }
+    return dev_dot(x, y, n, true, out, reinterpret_cast<cudaStream_t>(stream));
+}
+
+ed_status ed_op_expect(ed_op* op, const double* psi, int mem, double* out, void* stream) {
+    if (!op || !psi || !out) return ED_ERR_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int W = op->cplx ? 2 : 1;
+    const int64_t nd = op->D * W;
+    const double* dpsi;
+    double* owned;
+    ed_status st = to_device(psi, nd, mem, &dpsi, &owned, s);
+    double* hpsi = nullptr;
+    if (st == ED_OK && cudaMallocAsync(&hpsi, sizeof(double) * nd, s) != cudaSuccess) st = ED_ERR_ALLOC;
+    if (st == ED_OK) st = ed_op_perform(op, dpsi, hpsi, ED_MEM_DEVICE, stream);
+    double r[2] = {0.0, 0.0};
+    if (st == ED_OK) st = dev_dot(dpsi, hpsi, op->D, op->cplx, r, s);
+    if (!op->cplx) r[1] = 0.0;
+    if (hpsi) cudaFreeAsync(hpsi, s);
+    if (owned) cudaFreeAsync(owned, s);
+    cudaStreamSynchronize(s);
+    if (st == ED_OK) {
+        out[0] = r[0];
+        out[1] = r[1];
+    }
+    return st;
+}
+
+ed_status ed_site_densities(ed_op* op, const double* psi, int mem, double* n_up, double* n_dn, double* docc,
+                            void* stream) {
+    if (!op || !psi) return ED_ERR_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int W = op->cplx ? 2 : 1;
+    const int64_t nd = op->D * W;
+    const double* dpsi;
+    double* owned;
+    ed_status st = to_device(psi, nd, mem, &dpsi, &owned, s);
+    if (st != ED_OK) return st;
+    unsigned long long* acc = nullptr;
+    const size_t nacc = (size_t)op->dimUP + (size_t)op->dimDN + 64;
+    if (cudaMallocAsync(&acc, sizeof(unsigned long long) * nacc, s) != cudaSuccess) {
+        if (owned) cudaFreeAsync(owned, s);
+        return ED_ERR_ALLOC;
+    }
+    cudaMemsetAsync(acc, 0, sizeof(unsigned long long) * nacc, s);
+    int64_t g = op->dimUP < kObBlocks * 4 ? op->dimUP : kObBlocks * 4;
+    ed::k_densities<<<(int)g, kObThreads, 0, s>>>(dpsi, op->dimUP, op->dimDN, op->cplx ? 1 : 0, op->d_stUP,
+                                                  op->d_stDN, acc, acc + op->dimUP, acc + op->dimUP + op->dimDN);
+    std::vector<unsigned long long> h(nacc);
+    cudaError_t e = cudaMemcpyAsync(h.data(), acc, sizeof(unsigned long long) * nacc, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFreeAsync(acc, s);
+    if (owned) cudaFreeAsync(owned, s);
+    if (e != cudaSuccess) return ED_ERR_CUDA;
+    const int N = op->n_sites;
+    const double scale = std::ldexp(1.0, -60);
+    std::vector<long double> nu(N, 0.0L), ndn(N, 0.0L);
+    for (int64_t u = 0; u < op->dimUP; ++u) {
+        uint64_t w = op->bup.state[u];
+        while (w) {
+            const int i = __builtin_ctzll(w);
+            nu[i] += (long double)h[u];
+            w &= w - 1;
+        }
+    }
+    for (int64_t d = 0; d < op->dimDN; ++d) {
+        uint64_t w = op->bdn.state[d];
+        while (w) {
+            const int i = __builtin_ctzll(w);
+            ndn[i] += (long double)h[op->dimUP + d];
+            w &= w - 1;
+        }
+    }
+    for (int i = 0; i < N; ++i) {
+        if (n_up) n_up[i] = (double)(nu[i] * scale);
+        if (n_dn) n_dn[i] = (double)(ndn[i] * scale);
+        if (docc) docc[i] = (double)h[op->dimUP + op->dimDN + i] * scale;
+    }
+    return ED_OK;
+}
+
+ed_status ed_continued_fraction(int n, const double* alpha, const double* beta, double norm2, double energy, int nw,
+                                const double* omega, double* g) {
+    if (n < 1 || nw < 0 || !alpha || !beta || (nw && (!omega || !g))) return ED_ERR_ARG;
+    if (nw == 0) return ED_OK;
+    double *d = nullptr;
+    const size_t tot = (size_t)n + (size_t)n + 1 + 4 * (size_t)nw;
+    if (cudaMalloc(&d, sizeof(double) * tot) != cudaSuccess) return ED_ERR_ALLOC;
+    double *da = d, *db = d + n, *dw = d + 2 * n + 1, *dg = dw + 2 * nw;
+    cudaMemcpy(da, alpha, sizeof(double) * n, cudaMemcpyHostToDevice);
+    cudaMemcpy(db, beta, sizeof(double) * (n + 1), cudaMemcpyHostToDevice);
+    cudaMemcpy(dw, omega, sizeof(double) * 2 * nw, cudaMemcpyHostToDevice);
+    ed::k_cfrac<<<(nw + 127) / 128, 128>>>(n, da, db, norm2, energy, nw, dw, dg);
+    cudaError_t e = cudaMemcpy(g, dg, sizeof(double) * 2 * nw, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? ED_OK : ED_ERR_CUDA;
+}
+
+ed_status ed_drude_kubo(ed_op* H, ed_op* J, ed_op* K, const double* psi, double e0, const ed_kubo_cfg* cfg,
+                        ed_kubo_result* res, double* sigma_out, void* stream) {
+    if (!H || !J || !K || !psi || !cfg || !res || cfg->lanczos_steps < 1 || cfg->n_omega < 1) return ED_ERR_ARG;
+    if (H->cplx || J->cplx || K->cplx || H->D != J->D || H->D != K->D) return ED_ERR_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int64_t D = H->D;
+    double* phi = nullptr;
+    if (cudaMallocAsync(&phi, sizeof(double) * D, s) != cudaSuccess) return ED_ERR_ALLOC;
+    // phi = J|psi> (compute_sigma_omega, HubMatrix_GPU.cuh:838-846)
+    ed_status st = ed_op_perform(J, psi, phi, ED_MEM_DEVICE, stream);
+    // Lanczos::tridiagonal from phi/|phi| (fixed steps, no Ritz vector)
+    const int n = cfg->lanczos_steps;
+    std::vector<double> a(n), b(n + 1);
+    ed_lanczos_result lr;
+    if (st == ED_OK) {
+        ed_lanczos_cfg lc;
+        std::memset(&lc, 0, sizeof(lc));
+        lc.max_steps = n;
+        lc.mode = ED_LANCZOS_FIXED;
+        lc.ritz = ED_RITZ_NONE;
+        lc.start = ED_START_USER;
+        st = ed_lanczos_run(H, &lc, phi, ED_MEM_DEVICE, nullptr, ED_MEM_DEVICE, a.data(), b.data(), &lr, stream);
+    }
+    if (st == ED_OK) {
+        const int m = lr.steps;
+        const double norm2 = b[0] * b[0];  // |phi|^2 (lanctri.norm returns the squared norm)
+        std::vector<double> w(2 * cfg->n_omega), g(2 * cfg->n_omega);
+        for (int i = 0; i < cfg->n_omega; ++i) {
+            w[2 * i] = cfg->omega_step * (double)(i + 1);
+            w[2 * i + 1] = cfg->delta;
+        }
+        std::vector<double> bb(m + 1);
+        for (int i = 0; i <= m; ++i) bb[i] = b[i];
+        st = ed_continued_fraction(m, a.data(), bb.data(), norm2, e0, cfg->n_omega, w.data(), g.data());
+        if (st == ED_OK) {
+            double vertex = 0.0;
+            for (int i = 0; i < cfg->n_omega; ++i) {
+                const double sigma = -1.0 / (M_PI * w[2 * i]) * g[2 * i + 1];
+                if (sigma_out) sigma_out[i] = sigma;
+                if (w[2 * i] > cfg->omega_cutoff) vertex += sigma * cfg->omega_step;
+            }
+            double kin[2];
+            st = ed_op_expect(K, psi, ED_MEM_DEVICE, kin, stream);
+            if (st == ED_OK) {
+                res->kinetic = kin[0];
+                res->vertex = vertex;
+                res->drude = (-kin[0] - 2.0 * vertex) / cfg->volume;
+            }
+        }
+    }
+    cudaFreeAsync(phi, s);
+    cudaStreamSynchronize(s);
+    return st;
+}
+
+ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double e0, int steps, double* first,
+                      double* second, void* stream) {
+    if (!H || !dH || !psi || steps < 1 || (second && !d2H)) return ED_ERR_ARG;
+    if (dH->D != H->D || dH->cplx != H->cplx || (d2H && (d2H->D != H->D || d2H->cplx != H->cplx))) return ED_ERR_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const bool cplx = H->cplx;
+    const int64_t nd = H->D * (cplx ? 2 : 1);
+    double *phi = nullptr, *b = nullptr, *coef = nullptr;
+    if (cudaMallocAsync(&phi, sizeof(double) * nd, s) != cudaSuccess ||
+        cudaMallocAsync(&b, sizeof(double) * nd, s) != cudaSuccess ||
+        cudaMallocAsync(&coef, sizeof(double) * 2, s) != cudaSuccess)
+        return ED_ERR_ALLOC;
+    ed_status st = ed_op_perform(dH, psi, phi, ED_MEM_DEVICE, stream);
+    double ov[2] = {0.0, 0.0}, nn[2] = {0.0, 0.0};
+    if (st == ED_OK) st = dev_dot(psi, phi, H->D, cplx, ov, s);  // <psi|dH psi>
+    if (st == ED_OK) st = dev_dot(psi, psi, H->D, cplx, nn, s);
+    if (st == ED_OK && first) *first = ov[0] / nn[0];
+    if (st == ED_OK && second) {
+        // b = Q dH psi = dH psi - psi <psi|dH psi>/<psi|psi>
+        double c[2] = {ov[0] / nn[0], cplx ? ov[1] / nn[0] : 0.0};
+        cudaMemcpyAsync(coef, c, sizeof(double) * 2, cudaMemcpyHostToDevice, s);
+        ed::k_project<<<ob_grid(H->D), kObThreads, 0, s>>>(phi, psi, coef, H->D, cplx ? 1 : 0, b);
+        std::vector<double> a(steps), bt(steps + 1);
+        ed_lanczos_cfg lc;
+        std::memset(&lc, 0, sizeof(lc));
+        lc.max_steps = steps;
+        lc.mode = ED_LANCZOS_FIXED;
+        lc.ritz = ED_RITZ_NONE;
+        lc.start = ED_START_USER;
+        ed_lanczos_result lr;
+        st = ed_lanczos_run(H, &lc, b, ED_MEM_DEVICE, nullptr, ED_MEM_DEVICE, a.data(), bt.data(), &lr, stream);
+        if (st == ED_OK) {
+            // <b|(H - E0)^-1|b> = -|b|^2 * g(0) with g from the continued
+            // fraction at w = 0 (no broadening): 1/(E0 - a0 - b1^2/(E0 - a1 - ...))
+            const int m = lr.steps;
+            long double gz = 1.0L / ((long double)e0 - a[m - 1]);
+            for (int i = m - 2; i >= 0; --i)
+                gz = 1.0L / ((long double)e0 - a[i] - gz * (long double)bt[i + 1] * bt[i + 1]);
+            const double resp = -(double)((long double)bt[0] * bt[0] * gz) / nn[0];
+            double d2[2] = {0.0, 0.0};
+            st = ed_op_expect(d2H, psi, ED_MEM_DEVICE, d2, stream);
+            if (st == ED_OK) *second = d2[0] / nn[0] - 2.0 * resp;
+        }
+    }
+    cudaFreeAsync(phi, s);
+    cudaFreeAsync(b, s);
+    cudaFreeAsync(coef, s);
+    cudaStreamSynchronize(s);
+    return st;
+}
+
+ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_t a_mask, double* s_vn, double* s_ref,
+                                  void* stream) {
+    if (!op || !psi) return ED_ERR_ARG;
+    if (op->cplx) return ED_ERR_NOT_BUILT;
+    const int N = op->n_sites;
+    const uint64_t all = (N >= 64) ? ~0ULL : ((1ULL << N) - 1ULL);
+    a_mask &= all;
+    const uint64_t b_mask = all ^ a_mask;
+    const int nA = __builtin_popcountll(a_mask), nB = N - nA;
+    const int Qu = op->n_up, Qd = op->n_dn;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    // labels per spin state (entangle_entropy.h:22-44, with per-sector ranks)
+    auto labels = [&](const ed::SpinBasis& bs, std::vector<int32_t>* na, std::vector<int32_t>* ia,
+                      std::vector<int32_t>* ib) {
+        na->resize(bs.count);
+        ia->resize(bs.count);
+        ib->resize(bs.count);
+        for (int64_t r = 0; r < bs.count; ++r) {
+            const uint64_t w = bs.state[r];
+            const uint64_t pa = pext64(w, a_mask), pb = pext64(w, b_mask);
+            (*na)[r] = __builtin_popcountll(pa);
+            (*ia)[r] = (int32_t)cns_rank(pa);
+            (*ib)[r] = (int32_t)cns_rank(pb);
+        }
+    };
+    std::vector<int32_t> nau, iau, ibu, nad, iad, ibd;
+    labels(op->bup, &nau, &iau, &ibu);
+    labels(op->bdn, &nad, &iad, &ibd);
+    const int nqu = std::min(Qu, nA) + 1, nqd = std::min(Qd, nA) + 1;
+    std::vector<int64_t> off(nqu * nqd, 0);
+    std::vector<int32_t> rA(nqu * nqd, 0), cB(nqu * nqd, 0), dimA_dn(nqd), dimB_dn(nqd);
+    int64_t total = 0;
+    for (int kd = 0; kd < nqd; ++kd) {
+        dimA_dn[kd] = (int32_t)binom_i(nA, kd);
+        dimB_dn[kd] = (int32_t)binom_i(nB, Qd - kd);
+    }
+    for (int ku = 0; ku < nqu; ++ku)
+        for (int kd = 0; kd < nqd; ++kd) {
+            const int sidx = ku * nqd + kd;
+            rA[sidx] = (int32_t)(binom_i(nA, ku) * binom_i(nA, kd));
+            cB[sidx] = (int32_t)(binom_i(nB, Qu - ku) * binom_i(nB, Qd - kd));
+            off[sidx] = total;
+            total += (int64_t)rA[sidx] * cB[sidx];
+        }
+    // device copies
+    const double* dpsi;
+    double* owned;
+    ed_status st = to_device(psi, op->D, mem, &dpsi, &owned, s);
+    if (st != ED_OK) return st;
+    std::vector<int32_t> meta_i;
+    auto push = [&](const std::vector<int32_t>& v) { meta_i.insert(meta_i.end(), v.begin(), v.end()); };
+    push(nau); push(iau); push(ibu); push(nad); push(iad); push(ibd); push(rA); push(cB); push(dimA_dn); push(dimB_dn);
+    int32_t* dmi = nullptr;
+    int64_t* doff = nullptr;
+    double* blocks = nullptr;
+    if (cudaMalloc(&dmi, sizeof(int32_t) * meta_i.size()) != cudaSuccess ||
+        cudaMalloc(&doff, sizeof(int64_t) * off.size()) != cudaSuccess ||
+        cudaMalloc(&blocks, sizeof(double) * std::max<int64_t>(total, 1)) != cudaSuccess) {
+        cudaFree(dmi); cudaFree(doff);
+        if (owned) cudaFreeAsync(owned, s);
+        return ED_ERR_ALLOC;
+    }
+    cudaMemcpyAsync(dmi, meta_i.data(), sizeof(int32_t) * meta_i.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(blocks, 0, sizeof(double) * std::max<int64_t>(total, 1), s);
+    ed::EeMeta m;
+    size_t p = 0;
+    m.nA_up = dmi + p; p += nau.size();
+    m.ia_up = dmi + p; p += iau.size();
+    m.ib_up = dmi + p; p += ibu.size();
+    m.nA_dn = dmi + p; p += nad.size();
+    m.ia_dn = dmi + p; p += iad.size();
+    m.ib_dn = dmi + p; p += ibd.size();
+    m.blk_rowsA = dmi + p; p += rA.size();
+    m.blk_colsB = dmi + p; p += cB.size();
+    m.dimA_dn = dmi + p; p += dimA_dn.size();
+    m.dimB_dn = dmi + p; p += dimB_dn.size();
+    m.blk_off = doff;
+    m.nqd = nqd;
+    ed::k_ee_scatter<<<ob_grid(op->D), kObThreads, 0, s>>>(dpsi, op->dimUP, op->dimDN, m, blocks);
+    // singular values of every block (cusolverDnDgesvd, jobu = jobvt = 'N',
+    // as entangle_entropy.h:231-291)
+    cusolverDnHandle_t h = nullptr;
+    double svn = 0.0, sref = 0.0;
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) st = ED_ERR_CUDA;
+    if (st == ED_OK) cusolverDnSetStream(h, s);
+    int lwork_max = 0;
+    for (size_t k = 0; st == ED_OK && k < off.size(); ++k) {
+        const int mm = std::max(rA[k], cB[k]), nn = std::min(rA[k], cB[k]);
+        if (nn == 0) continue;
+        int lw = 0;
+        if (cusolverDnDgesvd_bufferSize(h, mm, nn, &lw) != CUSOLVER_STATUS_SUCCESS) st = ED_ERR_CUDA;
+        lwork_max = std::max(lwork_max, lw);
+    }
+    double *work = nullptr, *sv = nullptr, *rwork = nullptr;
+    int* info = nullptr;
+    int max_n = 0;
+    for (size_t k = 0; k < off.size(); ++k) max_n = std::max(max_n, (int)std::min(rA[k], cB[k]));
+    if (st == ED_OK && (cudaMalloc(&work, sizeof(double) * std::max(lwork_max, 1)) != cudaSuccess ||
+                        cudaMalloc(&sv, sizeof(double) * std::max(max_n, 1)) != cudaSuccess ||
+                        cudaMalloc(&rwork, sizeof(double) * std::max(max_n, 1)) != cudaSuccess ||
+                        cudaMalloc(&info, sizeof(int)) != cudaSuccess))
+        st = ED_ERR_ALLOC;
+    std::vector<double> hs(std::max(max_n, 1));
+    for (size_t k = 0; st == ED_OK && k < off.size(); ++k) {
+        const int mm = std::max(rA[k], cB[k]), nn = std::min(rA[k], cB[k]);
+        if (nn == 0) continue;
+        if (cusolverDnDgesvd(h, 'N', 'N', mm, nn, blocks + off[k], mm, sv, nullptr, mm, nullptr, nn, work, lwork_max,
+                             rwork, info) != CUSOLVER_STATUS_SUCCESS) {
+            st = ED_ERR_CUDA;
+            break;
+        }
+        if (cudaMemcpyAsync(hs.data(), sv, sizeof(double) * nn, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            st = ED_ERR_CUDA;
+            break;
+        }
+        for (int i = 0; i < nn; ++i) {
+            const double x = hs[i];
+            if (x > 0.0) {
+                sref += -x * std::log(x);
+                const double q = x * x;
+                if (q > 0.0) svn += -q * std::log(q);
+            }
+        }
+    }
+    if (h) cusolverDnDestroy(h);
+    cudaFree(work); cudaFree(sv); cudaFree(rwork); cudaFree(info);
+    cudaFree(blocks); cudaFree(dmi); cudaFree(doff);
+    if (owned) cudaFreeAsync(owned, s);
+    cudaStreamSynchronize(s);
+    if (st == ED_OK) {
+        if (s_vn) *s_vn = svn;
+        if (s_ref) *s_ref = sref;
+    }
+    return st;
+}
+
+}  // extern "C"

@@ -114,3 +114,24 @@ def squared_3by4(t: float = -1.0) -> List[Term]:
     bonds = [(0, 1), (1, 2), (2, 3), (4, 5), (5, 6), (6, 7), (8, 9), (9, 10), (10, 11),
              (0, 4), (4, 8), (1, 5), (5, 9), (2, 6), (6, 10), (3, 7), (7, 11)]
     return [("H", i, j, t, 0.0) for i, j in bonds]
+
+
+def kagome12_flux_derivatives(flux: float, rand: Sequence[float] | None = None):
+    """d/dPhi and d^2/dPhi^2 of the twisted Kagome12 hopping: with bond phase
+    Phi*dx_b, dH/dPhi carries t_b dx_b e^{i(Phi dx_b + pi/2)} and d2H/dPhi2
+    t_b dx_b^2 e^{i(Phi dx_b + pi)} on every bond (the on-site term does not
+    depend on Phi).  At Phi = 0, d2H/dPhi2 = -K_x (KagomeKinetic12) and
+    dH/dPhi = -i J_x (KagomeCurrent12)."""
+    r = [1.0] * 12 if rand is None else list(rand)
+    d1, d2 = [], []
+    for b, (i, j) in enumerate(zip(KAGOME12_FIRST, KAGOME12_SECOND)):
+        t = -r[i] * r[j]
+        dx = KAGOME12_DX[b]
+        d1.append(("P", i, j, t * dx, flux * dx + math.pi / 2))
+        d2.append(("P", i, j, t * dx * dx, flux * dx + math.pi))
+    return d1, d2
+
+
+def hopping_only(terms: List[Term]) -> List[Term]:
+    """The kinetic part of a term list (drops Make_N terms)."""
+    return [t for t in terms if t[0] != "N"]

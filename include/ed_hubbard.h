@@ -202,6 +202,68 @@ ed_status ed_random_vector(int64_t n, uint64_t seed, double* out_host);
 ed_status ed_tridiag_lowest(int n, const double* alpha, const double* offdiag,
                             double* e0, double* z);
 
+/* ------------------------------------------------------------ observables --
+ * What the reference drivers compute from a ground state.  psi is the Ritz
+ * vector (rows doubles, or 2*rows for complex operators) at `mem`. */
+
+/* <x, y> of n doubles (Thrust_Lin::thrust_Dotprod, HubMatrix_GPU.cuh:451-455),
+ * deterministic reduction order. */
+ed_status ed_vec_dot(int64_t n, const double* x, const double* y, int mem, double* out, void* stream);
+/* sum_k conj(x_k) y_k over n complex numbers (interleaved); out[0] = re,
+ * out[1] = im (HubMatrix_GPU.cuh:457-463). */
+ed_status ed_vec_zdot(int64_t n, const double* x, const double* y, int mem, double* out, void* stream);
+/* <psi|O|psi> (out[0] = re, out[1] = im), the Hubbard_mv + thrust_Dotprod
+ * pair the drivers use for K_x and S^2 (drude_v2_cal_Kagome_randomHop.cu:213-214). */
+ed_status ed_op_expect(ed_op* op, const double* psi, int mem, double* out, void* stream);
+/* Per-site <n_i,up>, <n_i,dn> and <n_i,up n_i,dn> of psi (N entries each,
+ * any pointer may be NULL): the Hellmann-Feynman derivatives dE0/d eps_i and
+ * dE0/dU_i.  Accumulated exactly in 2^-60 fixed point. */
+ed_status ed_site_densities(ed_op* op, const double* psi, int mem, double* n_up, double* n_dn, double* docc,
+                            void* stream);
+/* g(w) = norm2 / (w + E - a_0 - b_1^2/(w + E - a_1 - ...)) for nw complex
+ * frequencies (re, im pairs), beta[0] unused
+ * (correlator_continued_fraction, HubMatrix_GPU.cuh:820-835).  Host in/out. */
+ed_status ed_continued_fraction(int n, const double* alpha, const double* beta, double norm2, double energy, int nw,
+                                const double* omega, double* g);
+
+typedef struct {
+    int32_t lanczos_steps;   /* Lanczos::tridiagonal length (reference 200) */
+    int32_t n_omega;         /* NOMEGA (reference 8000) */
+    double omega_step;       /* OMEGA_STEP (0.004) */
+    double delta;            /* DELTA, imaginary part of w (0.01) */
+    double omega_cutoff;     /* OMEGA_CUTOFF (0.01) */
+    double volume;           /* VOL */
+} ed_kubo_cfg;
+
+typedef struct {
+    double drude;            /* (-<K> - 2 Vertex) / VOL */
+    double kinetic;          /* <psi|K|psi> */
+    double vertex;           /* sum_{w > cutoff} sigma(w) dw */
+} ed_kubo_result;
+
+/* drude_weight_Jx (drude_v2_cal_Kagome_randomHop.cu:183-220): sigma(w) =
+ * -Im Lambda(w)/(pi w) with Lambda the continued fraction of the
+ * lanczos_steps-step tridiagonalisation of H from J|psi>.  Real operators,
+ * psi on the device; sigma_out (n_omega doubles, host) may be NULL. */
+ed_status ed_drude_kubo(ed_op* H, ed_op* J, ed_op* K, const double* psi, double e0, const ed_kubo_cfg* cfg,
+                        ed_kubo_result* res, double* sigma_out, void* stream);
+/* First- and second-order energy response to a parameter theta with
+ * dH = dH/dtheta and d2H = d2H/dtheta2 (psi normalised ground state, device):
+ *   first  = <psi|dH|psi>                                  (Hellmann-Feynman)
+ *   second = <psi|d2H|psi> - 2 <b|(H - E0)^-1|b>,  b = (1 - |psi><psi|) dH psi,
+ * the resolvent from a `steps`-step Lanczos on H started at b.  For the flux
+ * theta = Phi this is d2E0/dPhi2, the Drude weight without broadening. */
+ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double e0, int steps, double* first,
+                      double* second, void* stream);
+/* Entanglement entropy of psi for the sites in a_mask: the matrix
+ * psi[(a_up a_dn), (b_up b_dn)] (entangle_entropy.h:177-197) is block-diagonal
+ * in the particle numbers of A; singular values s of every block by
+ * cusolverDnDgesvd.  s_vn = -sum s^2 ln s^2 (von Neumann entropy of the
+ * reduced density matrix), s_ref = -sum s ln s (the sum the reference
+ * drivers print, Hubbard_EE_test.cu:80-83).  Real operators. */
+ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_t a_mask, double* s_vn,
+                                  double* s_ref, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,141 @@
+"""Observables on the GPU against the oracle: site densities and
+Hellmann-Feynman derivatives (checked by central finite differences), the
+entanglement entropy, the reference's Kubo Drude weight, and the
+second-order flux response against a dense sum over states."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import philox_uniform
+
+pytestmark = pytest.mark.gpu
+
+
+def ground(ed, N, qu, qd, terms, U, steps=300, seed=1, dn_terms=None):
+    op = ed.Hubbard(ed.H_TBq(N, qu).extend(terms), ed.H_TBq(N, qd).extend(dn_terms or terms), U)
+    e0, v = ed.Lanczos().eigen(op, max_steps=steps, mode="fixed", seed=seed)
+    return op, e0, v
+
+
+def numpy_densities(orc, N, qu, qd, psi):
+    su = orc.Tables(N, qu).state
+    sd = orc.Tables(N, qd).state
+    P = np.abs(psi.reshape(su.size, sd.size)) ** 2
+    bu = (su[:, None] >> np.arange(N)) & 1
+    bd = (sd[:, None] >> np.arange(N)) & 1
+    return P.sum(1) @ bu, P.sum(0) @ bd, np.einsum("ud,ui,di->i", P, bu, bd)
+
+
+def test_site_densities(ed, orc):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    op, e0, v = ground(ed, 12, 5, 4, L.kagome12(), 4.0)
+    nu, nd, dd = ob.site_densities(op, v)
+    ru, rd, rdd = numpy_densities(orc, 12, 5, 4, v)
+    assert np.max(np.abs(nu - ru)) < 1e-12 and np.max(np.abs(nd - rd)) < 1e-12 and np.max(np.abs(dd - rdd)) < 1e-12
+    assert abs(nu.sum() - 5) < 1e-12 and abs(nd.sum() - 4) < 1e-12
+
+
+def test_hellmann_feynman_matches_finite_differences(ed):
+    """dE0/dU = sum_i <n_up n_dn>, dE0/d eps_i = <n_i>, dE0/dt = <H_kin>/t on
+    the disordered L=12 chain, against central differences (h = 1e-4)."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    eps = list(philox_uniform(100, 12, 6.0))
+    U, t, h = 1.0, -1.0, 1e-4
+
+    def e0_of(U=U, t=t, eps=eps):
+        terms = L.chain(12, periodic=False, t=t, eps=eps)
+        return ground(ed, 12, 6, 6, terms, U, steps=300)[1]
+
+    op, e0, v = ground(ed, 12, 6, 6, L.chain(12, periodic=False, eps=eps), U)
+    nu, nd, dd = ob.site_densities(op, v)
+    d_u = (e0_of(U=U + h) - e0_of(U=U - h)) / (2 * h)
+    assert abs(dd.sum() - d_u) < 1e-6
+    i = 5
+    ep, em = list(eps), list(eps)
+    ep[i] += h
+    em[i] -= h
+    d_eps = (e0_of(eps=ep) - e0_of(eps=em)) / (2 * h)
+    assert abs(nu[i] + nd[i] - d_eps) < 1e-6
+    kin = ed.Hubbard(ed.H_TBq(12, 6).extend(L.chain(12, periodic=False, t=t)),
+                     ed.H_TBq(12, 6).extend(L.chain(12, periodic=False, t=t)), 0.0)
+    d_t = (e0_of(t=t + h) - e0_of(t=t - h)) / (2 * h)
+    assert abs(ob.expect(kin, v) / t - d_t) < 1e-6
+
+
+def test_entanglement_entropy_device(ed, orc, golden_energies):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    g = golden_energies["chain8_pbc_q44_U4"]
+    op = ed.Hubbard(ed.H_TBq(8, 4).extend(L.chain(8)), ed.H_TBq(8, 4).extend(L.chain(8)), 4.0)
+    e0, v = ed.Lanczos().eigen(op, max_steps=100, mode="fixed", reorth=True, seed=0)
+    s_vn, s_ref = ob.entanglement_entropy(op, v, [0, 1, 2, 3])
+    assert abs(s_vn - g["EE_vN_A0123"]) < 1e-8
+    assert abs(s_ref - g["EE_ref_A0123"]) < 1e-8 * abs(g["EE_ref_A0123"])
+    # the same psi through the oracle's dense reshape + numpy SVD
+    for qu, qd, sites in ((6, 6, range(6)), (8, 4, range(6)), (7, 5, (0, 2, 4, 6, 8, 10))):
+        gg = golden_energies["chain12_open_W6_seed100_q66_U1"]
+        terms = L.chain(12, periodic=False, eps=gg["eps"])
+        op2, e2, v2 = ground(ed, 12, qu, qd, terms, 1.0)
+        a, b = ob.entanglement_entropy(op2, v2, list(sites))
+        ra, rb = orc.entanglement_entropy(v2, 12, qu, qd, list(sites))
+        assert abs(a - ra) < 1e-10 and abs(b - rb) < 1e-9 * max(1.0, rb)
+
+
+def test_drude_kubo_matches_oracle(ed, orc):
+    """The reference's drude_weight_Jx on Kagome12 3+3 (U=4): the device
+    result equals the oracle's restatement (oracle Lanczos, continued
+    fraction and sums) on the same ground state."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    N, q, U = 12, 3, 4.0
+    vol = 8.0 * math.sqrt(3.0)
+    H, e0, v = ground(ed, N, q, q, L.kagome12(), U)
+    J = ed.Hubbard(ed.H_TBq(N, q).extend(L.kagome12_current_x()), ed.H_TBq(N, q).extend(L.kagome12_current_x()), 0.0)
+    K = ed.Hubbard(ed.H_TBq(N, q).extend(L.kagome12_kinetic_x()), ed.H_TBq(N, q).extend(L.kagome12_kinetic_x()), 0.0)
+    D, kin, vert, sigma = ob.drude_kubo(H, J, K, v, e0, vol, want_sigma=True)
+    # oracle
+    tH = orc.Tables(N, q, L.kagome12())
+    tJ = orc.Tables(N, q, L.kagome12_current_x())
+    tK = orc.Tables(N, q, L.kagome12_kinetic_x())
+    phi = orc.matvec(tJ, tJ, 0.0, v)
+    _, a, b, _ = orc.lanczos(tH, tH, U, phi, 200, mode="fixed", want_evec=False)
+    w = 0.004 * np.arange(1, 8001) + 0.01j
+    lam = orc.continued_fraction(a, b, float(phi @ phi), e0, w)
+    sig = -lam.imag / (np.pi * w.real)
+    vertex = float(np.sum(sig[w.real > 0.01]) * 0.004)
+    kinetic = float(v @ orc.matvec(tK, tK, 0.0, v))
+    Dref = (-kinetic - 2 * vertex) / vol
+    assert abs(kin - kinetic) < 1e-12 * abs(kinetic)
+    assert abs(vert - vertex) < 1e-8 * abs(vertex)
+    assert abs(D - Dref) < 1e-8 * max(abs(Dref), 1e-3)
+    assert np.max(np.abs(sigma - sig)) < 1e-8 * np.max(np.abs(sig))
+
+
+@pytest.mark.parametrize("flux", [0.3, 1.1])
+def test_flux_response_vs_dense_sum_over_states(ed, orc, flux):
+    """dE0/dPhi and d2E0/dPhi2 from the device (Hellmann-Feynman + a
+    200-step linear-response Lanczos) against the dense sum over states on
+    Kagome12 2+2 with Peierls phases, and against central differences."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    N, q, U = 12, 2, 4.0
+    terms = L.kagome12(flux=flux)
+    d1t, d2t = L.kagome12_flux_derivatives(flux)
+    H, e0, v = ground(ed, N, q, q, terms, U, steps=300)
+    dH = ed.Hubbard(ed.H_TBq(N, q).extend(d1t), ed.H_TBq(N, q).extend(d1t), 0.0)
+    d2H = ed.Hubbard(ed.H_TBq(N, q).extend(d2t), ed.H_TBq(N, q).extend(d2t), 0.0)
+    first, second = ob.response(H, dH, d2H, v, e0, steps=200)
+    Hd = orc.hamiltonian(N, q, q, terms, terms, U).toarray()
+    w, V = np.linalg.eigh(Hd)
+    assert w[1] - w[0] > 1e-6
+    g = V[:, 0]
+    A1 = orc.hamiltonian(N, q, q, d1t, d1t, 0.0).toarray()
+    A2 = orc.hamiltonian(N, q, q, d2t, d2t, 0.0).toarray()
+    m = V.conj().T @ (A1 @ g)
+    exact1 = float(np.real(np.vdot(g, A1 @ g)))
+    exact2 = float(np.real(np.vdot(g, A2 @ g)) - 2 * np.sum(np.abs(m[1:]) ** 2 / (w[1:] - w[0])))
+    assert abs(first - exact1) < 1e-9 * max(1.0, abs(exact1))
+    assert abs(second - exact2) < 1e-8 * max(1.0, abs(exact2))
+    h = 1e-4
+    ep = ground(ed, N, q, q, L.kagome12(flux=flux + h), U)[1]
+    em = ground(ed, N, q, q, L.kagome12(flux=flux - h), U)[1]
+    assert abs((ep - em) / (2 * h) - first) < 1e-6
+    assert abs((ep - 2 * e0 + em) / h ** 2 - second) < 1e-4 * max(1.0, abs(second))
