@@ -1,0 +1,151 @@
+// ed_hubbard.hpp — header-only C++ surface over the C ABI in ed_hubbard.h,
+// shaped like the reference's own classes so its drivers switch by changing
+// types, not call sites:
+//   ed::H_TBq                Make_H / Make_J / Make_N, state  (fermi_operator.h:42-242)
+//   ed::Hubbard              Hubbard(HqUP, HqDN, U[, dilution]), Hubbard_mv(x, y) on
+//                            device pointers                  (HubMatrix_GPU.cuh:30-182)
+//   ed::SpectraHubbard<T>    Scalar, rows(), cols(), perform_op(x, y) on host
+//                            pointers — the Spectra operator concept
+//                                                             (HubMatrix_TotalSpin.cuh:181-322)
+//   ed::Lanczos              random_vector / eigen            (HubMatrix_GPU.cuh:477-613)
+// Errors surface as ed::Error (std::runtime_error) carrying the ed_status.
+#pragma once
+
+#include <cmath>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "ed_hubbard.h"
+
+namespace ed {
+
+struct Error : std::runtime_error {
+    ed_status status;
+    Error(ed_status s, const char* where)
+        : std::runtime_error(std::string(where) + ": " + ed_status_string(s)), status(s) {}
+};
+
+inline void check(ed_status s, const char* where) {
+    if (s != ED_OK) throw Error(s, where);
+}
+
+class H_TBq {
+public:
+    int N, Q;
+    H_TBq(int n, int q) : N(n), Q(q) {}
+    void Make_H(int i, int j, double t) { terms_.push_back({ED_TERM_HOP, i, j, 0, t, 0.0}); }
+    void Make_J(int i, int j, double t) { terms_.push_back({ED_TERM_CURRENT, i, j, 0, t, 0.0}); }
+    void Make_N(int i, double v) { terms_.push_back({ED_TERM_DENSITY, i, 0, 0, v, 0.0}); }
+    void Make_Peierls(int i, int j, double t, double phase) {
+        terms_.push_back({ED_TERM_PEIERLS, i, j, 0, t, phase});
+    }
+    void clear() { terms_.clear(); }
+    int64_t count() const { return ed_binom(N, Q); }
+    std::vector<uint64_t> state() const {
+        std::vector<int64_t> r(count());
+        for (int64_t k = 0; k < (int64_t)r.size(); ++k) r[k] = k;
+        std::vector<uint64_t> w(r.size());
+        check(ed_basis_unrank(N, Q, r.data(), (int64_t)r.size(), w.data()), "ed_basis_unrank");
+        return w;
+    }
+    const std::vector<ed_term>& terms() const { return terms_; }
+
+private:
+    std::vector<ed_term> terms_;
+};
+
+class Hubbard {
+public:
+    Hubbard(const H_TBq& up, const H_TBq& dn, double U = 0.0, uint64_t dilution = 0, int device = 0,
+            bool complex_op = false) {
+        ed_model_desc d{};
+        d.n_sites = up.N;
+        d.n_up = up.Q;
+        d.n_dn = dn.Q;
+        d.flags = complex_op ? ED_OP_COMPLEX : ED_OP_REAL;
+        d.up_terms = up.terms().data();
+        d.n_up_terms = (int32_t)up.terms().size();
+        d.dn_terms = dn.terms().data();
+        d.n_dn_terms = (int32_t)dn.terms().size();
+        d.U = U;
+        d.interaction_mask = dilution;
+        check(ed_op_create(&op_, &d, device), "ed_op_create");
+    }
+    Hubbard(const Hubbard&) = delete;
+    Hubbard& operator=(const Hubbard&) = delete;
+    ~Hubbard() { ed_op_destroy(op_); }
+    // y = H x on device vectors, asynchronous on `stream` (cudaStream_t)
+    void Hubbard_mv(const double* x, double* y, void* stream = nullptr) {
+        check(ed_op_perform(op_, x, y, ED_MEM_DEVICE, stream), "Hubbard_mv");
+    }
+    int64_t rows() const { return ed_op_rows(op_); }
+    int64_t cols() const { return ed_op_cols(op_); }
+    int64_t dimUP() const { return ed_op_dim_up(op_); }
+    int64_t dimDN() const { return ed_op_dim_dn(op_); }
+    ed_op* handle() const { return op_; }
+
+private:
+    ed_op* op_ = nullptr;
+};
+
+// The Spectra operator concept on host pointers (synchronous, y overwritten):
+// usable as Spectra::SymEigsSolver<ed::SpectraHubbard<double>>.
+template <typename FloatType = double>
+class SpectraHubbard {
+    static_assert(sizeof(FloatType) == sizeof(double), "FP64 operator");
+
+public:
+    using Scalar = FloatType;
+    explicit SpectraHubbard(Hubbard& h) : h_(h) {}
+    int64_t rows() const { return h_.rows(); }
+    int64_t cols() const { return h_.cols(); }
+    void perform_op(const Scalar* x, Scalar* y) const {
+        check(ed_op_perform(h_.handle(), reinterpret_cast<const double*>(x), reinterpret_cast<double*>(y),
+                            ED_MEM_HOST, nullptr),
+              "perform_op");
+    }
+
+private:
+    Hubbard& h_;
+};
+
+class Lanczos {
+public:
+    std::vector<double> a, b;  // T: alpha, beta (b[0] = |f|)
+    ed_lanczos_result result{};
+    // uniform(-1,1) from Philox4x64-10(seed), normalised
+    static std::vector<double> random_vector(int64_t n, uint64_t seed = 0) {
+        std::vector<double> f(n);
+        check(ed_random_vector(n, seed, f.data()), "ed_random_vector");
+        double s = 0.0;
+        for (double v : f) s += v * v;
+        s = 1.0 / std::sqrt(s);
+        for (double& v : f) v *= s;
+        return f;
+    }
+    // The reference's eigen(): stop test every 10 steps, up to max_steps;
+    // f (host, may be empty for the seeded random start); evec (host) out.
+    double eigen(Hubbard& h, const std::vector<double>& f, std::vector<double>& evec, int max_steps = 1000,
+                 int mode = ED_LANCZOS_REFERENCE, bool reorth = false, uint64_t seed = 0) {
+        ed_lanczos_cfg cfg{};
+        cfg.max_steps = max_steps;
+        cfg.mode = mode;
+        cfg.reorth = reorth ? 1 : 0;
+        cfg.ritz = ED_RITZ_STORED;
+        cfg.start = f.empty() ? ED_START_RANDOM : ED_START_USER;
+        cfg.seed = seed;
+        evec.resize(h.rows());
+        a.assign(max_steps, 0.0);
+        b.assign(max_steps + 1, 0.0);
+        check(ed_lanczos_run(h.handle(), &cfg, f.empty() ? nullptr : f.data(), ED_MEM_HOST, evec.data(), ED_MEM_HOST,
+                             a.data(), b.data(), &result, nullptr),
+              "ed_lanczos_run");
+        a.resize(result.steps);
+        b.resize(result.steps + 1);
+        return result.e0;
+    }
+};
+
+}  // namespace ed

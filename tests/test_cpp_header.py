@@ -1,0 +1,35 @@
+"""The header-only C++ surface (include/ed_hubbard.hpp) compiles against the
+C ABI, links the library, and (on a GPU) reproduces the golden E0."""
+import shutil
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+
+def build_example(tmp_path, edlib):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import _capi
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    libdir = _capi.lib_path().parent
+    exe = tmp_path / "chain8_lanczos"
+    subprocess.run([cxx, "-std=c++17", "-O1", "-I", str(ROOT / "include"), str(ROOT / "tests/cpp/chain8_lanczos.cpp"),
+                    "-o", str(exe), f"-L{libdir}", "-ledgb300", f"-Wl,-rpath,{libdir}"], check=True)
+    return exe
+
+
+def test_cpp_header_builds_and_runs_host_part(tmp_path, edlib):
+    exe = build_example(tmp_path, edlib)
+    out = subprocess.run([str(exe), "--basis-only"], capture_output=True, text=True, check=True).stdout
+    assert "count 70 first 15 last 240" in out
+
+
+@pytest.mark.gpu
+def test_cpp_header_lanczos_on_gpu(tmp_path, edlib, golden_energies):
+    exe = build_example(tmp_path, edlib)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    e0 = float(out.split("E0 ")[1].split()[0])
+    g = golden_energies["chain8_pbc_q44_U4"]["E0"]
+    assert abs(e0 - g) < 1e-10 * abs(g)
