@@ -82,6 +82,7 @@ SIGNATURES = {
     "ed_op_dim_dn": (C.c_int64, [C.c_void_p]),
     "ed_op_is_complex": (C.c_int, [C.c_void_p]),
     "ed_op_perform": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "ed_op_perform_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_lanczos_run": (C.c_int, [C.c_void_p, C.POINTER(ed_lanczos_cfg), C.c_void_p, C.c_int, C.c_void_p,
                                  C.c_int, C.c_void_p, C.c_void_p, C.POINTER(ed_lanczos_result), C.c_void_p]),
     "ed_random_vector": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p]),

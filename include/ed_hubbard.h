@@ -141,6 +141,23 @@ int ed_op_is_complex(const ed_op* op);
  * overwritten; x and y must not overlap. */
 ed_status ed_op_perform(ed_op* op, const double* x, double* y, int mem, void* stream);
 
+/* y = H x on device vectors without any device allocation.  This entry has no
+ * counterpart in the reference.  It is for callers that cannot let a library
+ * allocate GPU memory: code whose device memory belongs to another allocator
+ * (for example a framework's caching pool that has reserved the GPU) and loops
+ * that cannot afford the implicit device synchronisation a cudaMalloc or
+ * cudaFree may cause.  Same result and argument meaning as ed_op_perform with
+ * ED_MEM_DEVICE (x, y device pointers, asynchronous on stream, y
+ * overwritten), but the int64 copy of x lives in a fixed static device array
+ * of 2^21 values (16 MiB, held on every GPU that loads this library until the
+ * process exits): operators with more than 2^21 stored values (rows, or
+ * 2*rows for complex operators) return ED_ERR_RANGE.  The first call on a
+ * device resolves the array's device address (cudaGetSymbolAddress), so make
+ * that first call before any stream capture.  All calls share the one array
+ * and it keeps the last call's contents: calls that overlap on the GPU (other
+ * streams, other threads, other operators on the same device) race. */
+ed_status ed_op_perform_noalloc(ed_op* op, const double* x, double* y, void* stream);
+
 /* ---------------------------------------------------------------- Lanczos -- */
 enum { ED_LANCZOS_REFERENCE = 0,  /* stop test every 10 steps as in
                                        HubMatrix_GPU.cuh:585-597 */
