@@ -204,9 +204,10 @@ def main():
 
     cfg = _capi.ed_lanczos_cfg(max_steps=STEPS, mode=_capi.ED_LANCZOS_FIXED, reorth=0, ritz=_capi.ED_RITZ_STORED,
                                start=_capi.ED_START_RANDOM, profile=0, seed=SEED)
-    # same solve with CUDA events around every matvec / axpy launch (roofline)
+    # same solve with CUDA events around the persistent Lanczos launch and
+    # device timestamps of its phases (roofline)
     cfg_prof = _capi.ed_lanczos_cfg(max_steps=STEPS, mode=_capi.ED_LANCZOS_FIXED, reorth=0,
-                                    ritz=_capi.ED_RITZ_STORED, start=_capi.ED_START_RANDOM, profile=1, seed=SEED)
+                                    ritz=_capi.ED_RITZ_STORED, start=_capi.ED_START_RANDOM, profile=2, seed=SEED)
     evec_dev = torch.empty(D, dtype=torch.float64, device="cuda")
     res = _capi.ed_lanczos_result()
 
@@ -220,7 +221,9 @@ def main():
         solve_device()
     torch.cuda.synchronize()
 
-    e0s, ms, mv_ms, ax_ms, nmv, launches = [], [], 0.0, 0.0, 0, 0
+    e0s, ms, launches = [], [], 0
+    mv_ms = ax_ms = rd_ms = fz_ms = 0.0
+    nmv = 0
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
@@ -238,14 +241,18 @@ def main():
     barrier(world)
     ms_per_step = max_over_ranks(world, sum(ms) / len(ms))
     value = world * STEPS / (ms_per_step / 1000.0)
-    # per-kernel device time: events on the launching stream around each
-    # matvec / axpy of additional solves (not part of `value`)
-    for _ in range(3):
+    # dominant kernel: CUDA events on the launching stream around the
+    # persistent launch of additional solves (not part of `value`), and the
+    # per-step split of its time from device timestamps
+    n_prof = 3
+    for _ in range(n_prof):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         solve_device(cfg_prof)
         mv_ms += res.matvec_ms
         ax_ms += res.axpy_ms
+        rd_ms += res.reduce_ms
+        fz_ms += res.fused_ms
         nmv += res.n_matvec
 
     # e2e: host start vector in, host Ritz vector out, through the C ABI
@@ -276,10 +283,13 @@ def main():
     e2e_s = max_over_ranks(world, sum(e2e_t) / len(e2e_t))
     e2e_value = world * STEPS / e2e_s
 
-    # roofline of the dominant kernel (the matvec): algorithmic bytes per launch
-    avg_mv_ms = mv_ms / max(nmv, 1)
-    alg_bytes = 16.0 * D  # read x once, write H x once (FX int64 = 8 B/element each)
-    achieved = alg_bytes / (avg_mv_ms * 1e-3) / 1e9
+    # roofline of the dominant kernel, the persistent Lanczos launch (one per
+    # solve, STEPS steps): algorithmic bytes per step are the matvec's read of
+    # w_j and write of u (16 B x dim) plus the axpy's reads of u, w_j, w_{j-1}
+    # and write of w_{j+1} (32 B x dim)
+    fused_ms = fz_ms / n_prof
+    alg_bytes = 48.0 * D * STEPS
+    achieved = alg_bytes / (fused_ms * 1e-3) / 1e9
     peaks = {}
     try:
         peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
@@ -287,12 +297,13 @@ def main():
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     traffic = None
-    prof = ROOT / "profiles" / "matvec_kagome12_traffic.json"
+    prof = ROOT / "profiles" / "lz_fused_kagome12_traffic.json"
     if prof.exists():
         try:
             traffic = json.loads(prof.read_text()).get("dram_bytes_per_launch")
         except ValueError:
             traffic = None
+    per_step = lambda t: t / max(nmv, 1) * 1000.0  # noqa: E731  (ms summed over steps -> us per step)
 
     if rank == 0:
         cpu = cpu_baseline(args.cpu_seconds) if world >= 1 else None
@@ -310,10 +321,13 @@ def main():
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_matvec<real,staged,lanczos>",
-                         "note": "achieved = 16 B x dim per launch / mean CUDA-event duration; peak = measured "
-                                 "HBM copy bandwidth; the 13.7 MB working set is L2-resident",
-                         "avg_launch_us": avg_mv_ms * 1000.0, "axpy_avg_us": ax_ms / max(nmv, 1) * 1000.0},
+                         "kernel": "k_lz_fused<real, single class, gather schedule>",
+                         "note": "one launch per solve; achieved = 48 B x dim x steps / mean CUDA-event duration of "
+                                 "the launch; peak = measured HBM copy bandwidth (of measured); the vectors "
+                                 "(6.8 MB each) are L2-resident, HBM sees the Krylov basis write-back",
+                         "avg_launch_us": fused_ms * 1000.0,
+                         "per_step_us": {"matvec_rows": per_step(mv_ms), "axpy": per_step(ax_ms),
+                                         "reductions_barriers": per_step(rd_ms)}},
             "clocks": clk.summary(),
             "cpu_baseline": cpu,
         }

@@ -51,7 +51,9 @@ class ed_lanczos_cfg(C.Structure):
 class ed_lanczos_result(C.Structure):
     _fields_ = [("e0", C.c_double), ("steps", C.c_int32), ("converged", C.c_int32), ("status", C.c_int32),
                 ("min_bits", C.c_int32), ("residual", C.c_double), ("launches", C.c_int64),
-                ("matvec_ms", C.c_double), ("axpy_ms", C.c_double), ("n_matvec", C.c_int32), ("pad_", C.c_int32)]
+                ("matvec_ms", C.c_double), ("axpy_ms", C.c_double), ("n_matvec", C.c_int32), ("pad_", C.c_int32),
+                ("reduce_ms", C.c_double), ("barrier_ms", C.c_double), ("scalar_ms", C.c_double),
+                ("fused_ms", C.c_double)]
 
 
 class ed_kubo_cfg(C.Structure):

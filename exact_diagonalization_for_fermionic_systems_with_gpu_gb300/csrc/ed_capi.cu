@@ -80,12 +80,15 @@ struct OpExtra {
     void* lz_ws = nullptr;
 };
 
+// Device copy of a host table; the allocation is rounded up to 16 bytes and
+// the tail zeroed, so a table can be moved with 16-byte bulk copies.
 template <typename T>
 cudaError_t upload(T** dst, const T* src, size_t n) {
-    const size_t bytes = sizeof(T) * std::max<size_t>(n, 1);
+    const size_t bytes = (sizeof(T) * std::max<size_t>(n, 1) + 15) / 16 * 16;
     cudaError_t e = cudaMalloc(dst, bytes);
     if (e != cudaSuccess) return e;
-    if (n) e = cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice);
+    e = cudaMemset(*dst, 0, bytes);
+    if (e == cudaSuccess && n) e = cudaMemcpy(*dst, src, sizeof(T) * n, cudaMemcpyHostToDevice);
     return e;
 }
 
@@ -317,6 +320,28 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
     a.dnPtr = op->d_dnPtr;
     a.dnEntC = op->d_dnEntC;
     a.dnNnz = (uint32_t)dn_ent.size();
+    // conflict-free gather schedule for the shared-memory kernels (real,
+    // single class); ED_NO_SCHED=1 keeps the CSR gathers
+    a.dnSched = nullptr;
+    a.dnSteps = nullptr;
+    a.schedSteps = 0;
+    a.dimDNp = 0;
+    if (!cplx && td.coef.size() <= 1 && !std::getenv("ED_NO_SCHED")) {
+        ed::GatherSchedule gs;
+        std::string serr;
+        if (ed::build_gather_schedule(td, &gs, &serr)) {
+            if (upload(&op->d_dnSched, gs.ent.data(), gs.ent.size()) != cudaSuccess ||
+                upload(&op->d_dnSteps, gs.steps32.data(), gs.steps32.size()) != cudaSuccess) {
+                ed_op_destroy(op);
+                return ED_ERR_ALLOC;
+            }
+            a.dnSched = op->d_dnSched;
+            a.dnSteps = op->d_dnSteps;
+            a.schedSteps = gs.steps;
+            a.dimDNp = (int)gs.count_pad;
+            a.schedNeg = (int)gs.neg_base;
+        }
+    }
     a.err = op->d_err;
     a.upEnt = op->d_upEnt;
     a.dnEnt = op->d_dnEnt;
@@ -334,7 +359,11 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
     op->grid = ed::matvec_grid(op);
     op->mv_threads = ed::matvec_threads(op->dimDN);
     op->mv_fast = a.nclsUP <= 1 && a.nclsDN <= 1;
-    op->tma_smem = std::getenv("ED_NO_TMA") ? 0 : ed::tma_plan(op, &a);
+    // kernel choice: the row-staged TMA kernel where the down table fits in
+    // shared memory, else the generic kernel; ED_MATVEC=generic forces the
+    // generic kernel (tests compare the two)
+    const char* pick = std::getenv("ED_MATVEC");
+    if (!(pick && std::string(pick) == "generic")) op->tma_smem = ed::tma_plan(op, &a);
     if (op->tma_smem > 0) op->tma_grid = ed::tma_grid(op);
     *out = op;
     return ED_OK;
@@ -348,6 +377,7 @@ ed_status ed_op_destroy(ed_op* op) {
     cudaFree(op->d_upEnt); cudaFree(op->d_dnEnt); cudaFree(op->d_upLen); cudaFree(op->d_dnLen);
     cudaFree(op->d_upNpos); cudaFree(op->d_dnNpos);
     cudaFree(op->d_upPtr); cudaFree(op->d_upEntC); cudaFree(op->d_dnPtr); cudaFree(op->d_dnEntC);
+    cudaFree(op->d_dnSched); cudaFree(op->d_dnSteps);
     cudaFree(op->d_err);
     cudaFree(op->d_dUPq); cudaFree(op->d_dDNq); cudaFree(op->d_stUP); cudaFree(op->d_stDN);
     cudaFree(op->d_xq); cudaFree(op->d_emax); cudaFree(op->d_flag); cudaFree(op->d_io);
@@ -390,10 +420,17 @@ ed_status ed_op_perform(ed_op* op, const double* x, double* y, int mem, void* st
     cudaError_t e = ed::launch_matvec_f64(op, op->d_xq, op->d_emax, dy, s);
     if (e != cudaSuccess) { op->last_error = cudaGetErrorString(e); return ED_ERR_CUDA; }
     if (mem == ED_MEM_HOST) {
-        int flag = 0;
+        int flag = 0, err = 0;
         if (cudaMemcpyAsync(y, dy, sizeof(double) * DW, cudaMemcpyDeviceToHost, s) != cudaSuccess) return ED_ERR_CUDA;
         if (cudaMemcpyAsync(&flag, op->d_flag, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return ED_ERR_CUDA;
+        if (cudaMemcpyAsync(&err, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return ED_ERR_CUDA;
         if (cudaStreamSynchronize(s) != cudaSuccess) return ED_ERR_CUDA;
+        // the bounded-wait flag is sticky: a device-pointer call that gave up
+        // is reported by the next call that synchronises
+        if (err) {
+            cudaMemset(op->d_err, 0, sizeof(int));
+            return ED_ERR_TIMEOUT;
+        }
         if (flag) return ED_ERR_NONFINITE;
     }
     return ED_OK;

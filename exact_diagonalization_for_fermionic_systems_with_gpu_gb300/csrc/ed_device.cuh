@@ -176,6 +176,25 @@ __device__ __forceinline__ i128 block_sum_i128(i128 v, i128* scratch) {
     return r;
 }
 
+// Sum and max in one pass (two barriers); results valid in thread 0.
+__device__ __forceinline__ void block_sum_max(i128& v, uint64_t& m, i128* s128, uint64_t* s64) {
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    v = warp_sum_i128(v);
+    m = warp_max_u64(m);
+    __syncthreads();
+    if (lane == 0) {
+        s128[wid] = v;
+        s64[wid] = m;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < nw ? s128[lane] : (i128)0;
+        m = lane < nw ? s64[lane] : 0ULL;
+        v = warp_sum_i128(v);
+        m = warp_max_u64(m);
+    }
+}
+
 __device__ __forceinline__ uint64_t block_max_u64(uint64_t v, uint64_t* scratch) {
     int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     v = warp_max_u64(v);

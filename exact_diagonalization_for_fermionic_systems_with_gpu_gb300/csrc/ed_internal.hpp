@@ -40,9 +40,18 @@ struct MvArgs {
     const uint32_t* dnPtr;
     const uint32_t* dnEntC;
     uint32_t dnNnz;
+    // conflict-free gather schedule of the down term (real single-class
+    // operators; null otherwise): entries [schedSteps][dimDNp], steps per
+    // 32-column block
+    const uint16_t* dnSched;
+    const uint8_t* dnSteps;
+    int schedSteps;
+    int dimDNp;
+    int schedNeg;         // index of -x[0] in the row buffer; zeros at 2 * schedNeg
     int* err;             // device word set when a bounded wait gives up
     // shared-memory plan of the TMA kernel (byte offsets)
     int sm_row0, sm_row1, sm_dnptr, sm_dnent, sm_dnnpos, sm_ddnq, sm_stdn;
+    int sm_sched, sm_steps;  // schedule layout (instead of dnptr/dnent/dnnpos)
     // output
     double* y;            // FP64 output (perform path)
     const int* p_emax;    // device: max biased exponent of the FP64 input
@@ -73,6 +82,8 @@ struct ed_op {
     uint8_t *d_upLen = nullptr, *d_dnLen = nullptr;
     uint8_t *d_upNpos = nullptr, *d_dnNpos = nullptr;
     uint32_t *d_upPtr = nullptr, *d_upEntC = nullptr, *d_dnPtr = nullptr, *d_dnEntC = nullptr;
+    uint16_t* d_dnSched = nullptr;
+    uint8_t* d_dnSteps = nullptr;
     int* d_err = nullptr;
     int64_t *d_dUPq = nullptr, *d_dDNq = nullptr;
     uint64_t *d_stUP = nullptr, *d_stDN = nullptr;

@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -23,6 +24,7 @@ namespace ed {
 using namespace dev;
 
 size_t tridiag_scratch_bytes(int n);
+cudaError_t launch_lz_fused(const ed_op* op, const LzFusedArgs& f, cudaStream_t s);
 cudaError_t launch_tridiag_lowest(int n, const double* alpha, const double* off, double* out, void* scratch,
                                   cudaStream_t s);
 
@@ -254,6 +256,9 @@ struct Workspace {
     double* ritz_part = nullptr;
     unsigned int* ritz_ctr = nullptr;
     double* inv_norm = nullptr;
+    unsigned int* gbar = nullptr;  // grid-barrier counter of the persistent kernel, then
+                                   // its three reduction sets (kFusedSync bytes)
+    unsigned long long* stamps = nullptr;  // phase timestamps (profile 2), kLzStamps per step
     std::vector<cudaEvent_t> events;  // profiling pool (pairs)
 };
 
@@ -272,13 +277,14 @@ void free_ws(Workspace* w) {
     cudaFree(w->h.part_lo); cudaFree(w->h.part_hi); cudaFree(w->h.part_max); cudaFree(w->h.counter);
     cudaFree(w->emax); cudaFree(w->flag); cudaFree(w->tri_scratch); cudaFree(w->tri_out); cudaFree(w->offd);
     cudaFree(w->dot_lo); cudaFree(w->dot_hi); cudaFree(w->coef_rt); cudaFree(w->coef_rs);
-    cudaFree(w->ritz_part); cudaFree(w->ritz_ctr); cudaFree(w->inv_norm);
+    cudaFree(w->ritz_part); cudaFree(w->ritz_ctr); cudaFree(w->inv_norm); cudaFree(w->gbar);
+    cudaFree(w->stamps);
     for (cudaEvent_t e : w->events) cudaEventDestroy(e);
     *w = Workspace();
 }
 
-constexpr int kMaxPartials = 152 * 16;
 constexpr int kDotChunks = 64;
+constexpr size_t kFusedSync = 128;  // barrier counter at 0, LzRedSet[3] at 32
 
 ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_steps) {
     if (w->basis && w->basis_slots >= slots && w->DW == DW && w->max_steps >= max_steps) return ED_OK;
@@ -298,9 +304,9 @@ ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_s
     LZ_CK(cudaMalloc(&w->h.m, sizeof(uint64_t) * ns));
     LZ_CK(cudaMalloc(&w->h.beta, sizeof(double) * ns));
     LZ_CK(cudaMalloc(&w->h.alpha, sizeof(double) * ns));
-    LZ_CK(cudaMalloc(&w->h.part_lo, sizeof(uint64_t) * kMaxPartials));
-    LZ_CK(cudaMalloc(&w->h.part_hi, sizeof(uint64_t) * kMaxPartials));
-    LZ_CK(cudaMalloc(&w->h.part_max, sizeof(uint64_t) * kMaxPartials));
+    LZ_CK(cudaMalloc(&w->h.part_lo, sizeof(uint64_t) * kLzMaxPartials));
+    LZ_CK(cudaMalloc(&w->h.part_hi, sizeof(uint64_t) * kLzMaxPartials));
+    LZ_CK(cudaMalloc(&w->h.part_max, sizeof(uint64_t) * kLzMaxPartials));
     LZ_CK(cudaMalloc(&w->h.counter, sizeof(unsigned int) * 4));
     LZ_CK(cudaMemset(w->h.counter, 0, sizeof(unsigned int) * 4));
     LZ_CK(cudaMalloc(&w->emax, sizeof(int)));
@@ -312,10 +318,12 @@ ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_s
     LZ_CK(cudaMalloc(&w->dot_hi, sizeof(uint64_t) * ns * kDotChunks));
     LZ_CK(cudaMalloc(&w->coef_rt, sizeof(int64_t) * ns));
     LZ_CK(cudaMalloc(&w->coef_rs, sizeof(int) * ns));
-    LZ_CK(cudaMalloc(&w->ritz_part, sizeof(double) * kMaxPartials));
+    LZ_CK(cudaMalloc(&w->ritz_part, sizeof(double) * kLzMaxPartials));
     LZ_CK(cudaMalloc(&w->ritz_ctr, sizeof(unsigned int)));
     LZ_CK(cudaMemset(w->ritz_ctr, 0, sizeof(unsigned int)));
     LZ_CK(cudaMalloc(&w->inv_norm, sizeof(double)));
+    LZ_CK(cudaMalloc(&w->gbar, kFusedSync));
+    LZ_CK(cudaMalloc(&w->stamps, sizeof(unsigned long long) * kLzStamps * ns));
     LZ_CK(cudaMemcpy(w->lz, &w->h, sizeof(LzState), cudaMemcpyHostToDevice));
     return ED_OK;
 }
@@ -383,8 +391,9 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     LzState* lz = w->lz;
     const LzState& H = w->h;
     int64_t launches = 0;
-    const bool prof = cfg->profile != 0;
-    const size_t need_ev = prof ? (size_t)4 * max_steps : 0;
+    const bool prof = cfg->profile == 1;     // per-step kernels timed with events
+    const bool stamps = cfg->profile == 2;   // persistent kernel with phase timestamps
+    const size_t need_ev = prof ? (size_t)4 * max_steps : (stamps ? (size_t)2 * (max_steps / 10 + 2) : 0);
     while (w->events.size() < need_ev) {
         cudaEvent_t e;
         LZ_CK(cudaEventCreate(&e));
@@ -418,62 +427,95 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     std::vector<double> tri(max_steps + 2);
     int status_dev = 0;
 
+    // Steps run in the persistent kernel (one launch per run of steps, ten at
+    // a time in the reference mode so the stop test keeps its cadence) for
+    // real single-class operators whose down table fits shared memory as a
+    // gather schedule, unless reorthogonalisation or per-step timing asks for
+    // the per-step kernels.  ED_LZ_FUSED=0 never uses it, ED_LZ_FUSED=1 also
+    // for the other operators with a shared-memory plan (complex, several
+    // classes), where the per-step kernels measured faster.
+    const char* fz = std::getenv("ED_LZ_FUSED");
+    const bool force = fz && fz[0] == '1', never = fz && fz[0] == '0';
+    bool fused = op->tma_smem > 0 && !cfg->reorth && !prof && !never && (force || op->mv.dnSched != nullptr);
     int steps_run = 0;
-    for (int j = 0; j < max_steps; ++j) {
-        if (prof) LZ_CK(cudaEventRecord(w->events[4 * j], s));
-        LZ_CK(launch_matvec_lz(op, slot(j), w->u, lz, H.m + j, j, s));
-        if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 1], s));
-        const int64_t* pj = j > 0 ? slot(j - 1) : slot(j);
-        if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 2], s));
-        k_lz_axpy<<<lz_grid(DW), kLzThreads, 0, s>>>(w->u, slot(j), pj, slot(j + 1), DW, lz, j);
-        LZ_CK(cudaGetLastError());
-        if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 3], s));
-        launches += 2;
-        steps_run = j + 1;
-        if (cfg->reorth) {
-            // classical Gram-Schmidt, twice, against v_0..v_j
-            const int nk = j + 1;
-            for (int pass = 0; pass < 2; ++pass) {
-                dim3 g(nk, kDotChunks);
-                k_lz_dots<<<g, kLzThreads, 0, s>>>(w->basis, DW, w->stride, slot(j + 1), w->dot_lo, w->dot_hi);
-                LZ_CK(cudaGetLastError());
-                std::vector<uint64_t> lo((size_t)nk * kDotChunks), hi((size_t)nk * kDotChunks);
-                std::vector<int> ev(nk + 2);
-                std::vector<double> bv(nk + 2);
-                LZ_CK(cudaMemcpyAsync(lo.data(), w->dot_lo, sizeof(uint64_t) * lo.size(), cudaMemcpyDeviceToHost, s));
-                LZ_CK(cudaMemcpyAsync(hi.data(), w->dot_hi, sizeof(uint64_t) * hi.size(), cudaMemcpyDeviceToHost, s));
-                LZ_CK(cudaMemcpyAsync(ev.data(), H.e, sizeof(int) * (nk + 1), cudaMemcpyDeviceToHost, s));
-                LZ_CK(cudaMemcpyAsync(bv.data(), H.beta, sizeof(double) * (nk + 1), cudaMemcpyDeviceToHost, s));
-                LZ_CK(cudaStreamSynchronize(s));
-                const int ew = ev[nk];
-                std::vector<double> r(nk);
-                for (int k = 0; k < nk; ++k) {
-                    __int128 acc = 0;
-                    for (int c = 0; c < kDotChunks; ++c)
-                        acc += (__int128)(((unsigned __int128)hi[(size_t)k * kDotChunks + c] << 64) |
-                                          lo[(size_t)k * kDotChunks + c]);
-                    // <w_k, w> = acc 2^(e_k + e_w + 24); coefficient on q_k in
-                    // units of w's exponent: <w_k,w>/beta_k^2 * 2^(e_k - e_w)
-                    const double dotv = std::ldexp((double)acc, ev[k] + ew + 24);
-                    r[k] = dotv / (bv[k] * bv[k]) * std::ldexp(1.0, ev[k] - ew);
-                }
-                std::vector<int64_t> rt;
-                std::vector<int> rs;
-                int F;
-                fx_coefs(r, &rt, &rs, &F);
-                LZ_CK(cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * nk, cudaMemcpyHostToDevice, s));
-                LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * nk, cudaMemcpyHostToDevice, s));
-                k_lz_reorth<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), w->basis, DW, w->stride, nk, w->coef_rt,
-                                                               w->coef_rs, F);
-                LZ_CK(cudaGetLastError());
-                launches += 2;
+    int n_fused = 0;  // persistent launches
+    int j = 0;
+    while (j < max_steps) {
+        if (fused) {
+            const int j1 = cfg->mode == ED_LANCZOS_REFERENCE ? std::min(max_steps, (j / 10 + 1) * 10) : max_steps;
+            LZ_CK(cudaMemsetAsync(w->gbar, 0, kFusedSync, s));
+            LzRedSet* red = reinterpret_cast<LzRedSet*>(reinterpret_cast<char*>(w->gbar) + 32);
+            LzFusedArgs fa{w->basis, w->stride, stored ? 1 : 0, j, j1, w->u, DW, lz, w->gbar, red,
+                           stamps ? w->stamps : nullptr};
+            if (stamps) LZ_CK(cudaEventRecord(w->events[2 * n_fused], s));
+            const cudaError_t e = launch_lz_fused(op, fa, s);
+            if (e == cudaSuccess && stamps) LZ_CK(cudaEventRecord(w->events[2 * n_fused + 1], s));
+            if (e == cudaErrorNotSupported || e == cudaErrorCooperativeLaunchTooLarge) {
+                cudaGetLastError();
+                fused = false;  // this device cannot hold the grid: per-step kernels
+                continue;
             }
-            k_lz_stats<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), DW, lz, j + 1);
-            LZ_CK(cudaGetLastError());
+            LZ_CK(e);
             ++launches;
+            ++n_fused;
+            j = j1;
+        } else {
+            if (prof) LZ_CK(cudaEventRecord(w->events[4 * j], s));
+            LZ_CK(launch_matvec_lz(op, slot(j), w->u, lz, H.m + j, j, s));
+            if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 1], s));
+            const int64_t* pj = j > 0 ? slot(j - 1) : slot(j);
+            if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 2], s));
+            k_lz_axpy<<<lz_grid(DW), kLzThreads, 0, s>>>(w->u, slot(j), pj, slot(j + 1), DW, lz, j);
+            LZ_CK(cudaGetLastError());
+            if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 3], s));
+            launches += 2;
+            if (cfg->reorth) {
+                // classical Gram-Schmidt, twice, against v_0..v_j
+                const int nk = j + 1;
+                for (int pass = 0; pass < 2; ++pass) {
+                    dim3 g(nk, kDotChunks);
+                    k_lz_dots<<<g, kLzThreads, 0, s>>>(w->basis, DW, w->stride, slot(j + 1), w->dot_lo, w->dot_hi);
+                    LZ_CK(cudaGetLastError());
+                    std::vector<uint64_t> lo((size_t)nk * kDotChunks), hi((size_t)nk * kDotChunks);
+                    std::vector<int> ev(nk + 2);
+                    std::vector<double> bv(nk + 2);
+                    LZ_CK(cudaMemcpyAsync(lo.data(), w->dot_lo, sizeof(uint64_t) * lo.size(), cudaMemcpyDeviceToHost, s));
+                    LZ_CK(cudaMemcpyAsync(hi.data(), w->dot_hi, sizeof(uint64_t) * hi.size(), cudaMemcpyDeviceToHost, s));
+                    LZ_CK(cudaMemcpyAsync(ev.data(), H.e, sizeof(int) * (nk + 1), cudaMemcpyDeviceToHost, s));
+                    LZ_CK(cudaMemcpyAsync(bv.data(), H.beta, sizeof(double) * (nk + 1), cudaMemcpyDeviceToHost, s));
+                    LZ_CK(cudaStreamSynchronize(s));
+                    const int ew = ev[nk];
+                    std::vector<double> r(nk);
+                    for (int k = 0; k < nk; ++k) {
+                        __int128 acc = 0;
+                        for (int c = 0; c < kDotChunks; ++c)
+                            acc += (__int128)(((unsigned __int128)hi[(size_t)k * kDotChunks + c] << 64) |
+                                              lo[(size_t)k * kDotChunks + c]);
+                        // <w_k, w> = acc 2^(e_k + e_w + 24); coefficient on q_k in
+                        // units of w's exponent: <w_k,w>/beta_k^2 * 2^(e_k - e_w)
+                        const double dotv = std::ldexp((double)acc, ev[k] + ew + 24);
+                        r[k] = dotv / (bv[k] * bv[k]) * std::ldexp(1.0, ev[k] - ew);
+                    }
+                    std::vector<int64_t> rt;
+                    std::vector<int> rs;
+                    int F;
+                    fx_coefs(r, &rt, &rs, &F);
+                    LZ_CK(cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * nk, cudaMemcpyHostToDevice, s));
+                    LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * nk, cudaMemcpyHostToDevice, s));
+                    k_lz_reorth<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), w->basis, DW, w->stride, nk,
+                                                                   w->coef_rt, w->coef_rs, F);
+                    LZ_CK(cudaGetLastError());
+                    launches += 2;
+                }
+                k_lz_stats<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), DW, lz, j + 1);
+                LZ_CK(cudaGetLastError());
+                ++launches;
+            }
+            ++j;
         }
-        if (cfg->mode == ED_LANCZOS_REFERENCE && j % 10 == 9) {
-            const int nn = j + 1;
+        steps_run = j;
+        if (cfg->mode == ED_LANCZOS_REFERENCE && j % 10 == 0) {
+            const int nn = j;
             LZ_CK(cudaMemcpyAsync(ha.data(), H.alpha, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
             LZ_CK(cudaMemcpyAsync(hb.data(), H.beta, sizeof(double) * (nn + 1), cudaMemcpyDeviceToHost, s));
             LZ_CK(cudaMemcpyAsync(&status_dev, &lz->status, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -500,7 +542,13 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     LZ_CK(cudaMemcpyAsync(&hs, lz, sizeof(LzState), cudaMemcpyDeviceToHost, s));
     LZ_CK(cudaMemcpyAsync(ha.data(), H.alpha, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
     LZ_CK(cudaMemcpyAsync(hb.data(), H.beta, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost, s));
+    int err_flag = 0;
+    LZ_CK(cudaMemcpyAsync(&err_flag, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
     LZ_CK(cudaStreamSynchronize(s));
+    if (err_flag) {
+        cudaMemset(op->d_err, 0, sizeof(int));
+        return ED_ERR_TIMEOUT;
+    }
     int status = hs.status;
     if (status == 7) {
         // breakdown: T is exact up to the first vanishing beta
@@ -546,7 +594,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     }
     if (alpha_h) std::memcpy(alpha_h, ha.data(), sizeof(double) * n);
     if (beta_h) std::memcpy(beta_h, hb.data(), sizeof(double) * (n + 1));
-    double mv_ms = 0.0, ax_ms = 0.0;
+    double mv_ms = 0.0, ax_ms = 0.0, rd_ms = 0.0, bar_ms = 0.0, sc_ms = 0.0, fz_ms = 0.0;
     if (prof) {
         LZ_CK(cudaStreamSynchronize(s));
         for (int j = 0; j < steps_run; ++j) {
@@ -556,11 +604,33 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             mv_ms += a;
             ax_ms += b;
         }
+    } else if (stamps && n_fused > 0) {
+        LZ_CK(cudaStreamSynchronize(s));
+        for (int k = 0; k < n_fused; ++k) {
+            float a = 0.f;
+            LZ_CK(cudaEventElapsedTime(&a, w->events[2 * k], w->events[2 * k + 1]));
+            fz_ms += a;
+        }
+        std::vector<unsigned long long> t((size_t)kLzStamps * steps_run);
+        LZ_CK(cudaMemcpy(t.data(), w->stamps, sizeof(unsigned long long) * t.size(), cudaMemcpyDeviceToHost));
+        auto ms = [](unsigned long long a, unsigned long long b) { return (double)(b - a) * 1e-6; };
+        for (int j = 0; j < steps_run; ++j) {
+            const unsigned long long* q = t.data() + (size_t)kLzStamps * j;
+            mv_ms += ms(q[0], q[1]);
+            ax_ms += ms(q[4], q[5]);
+            rd_ms += ms(q[1], q[4]) + ms(q[5], q[8]);
+            bar_ms += ms(q[2], q[3]) + ms(q[6], q[7]);
+            sc_ms += ms(q[3], q[4]) + ms(q[7], q[8]);
+        }
     }
     if (res) {
         res->launches = launches;
         res->matvec_ms = mv_ms;
         res->axpy_ms = ax_ms;
+        res->reduce_ms = rd_ms;
+        res->barrier_ms = bar_ms;
+        res->scalar_ms = sc_ms;
+        res->fused_ms = fz_ms;
         res->n_matvec = steps_run;
         res->e0 = e0;
         res->steps = n;

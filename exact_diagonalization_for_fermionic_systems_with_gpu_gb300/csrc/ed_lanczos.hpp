@@ -11,6 +11,9 @@
 
 namespace ed {
 
+constexpr int kLzMaxPartials = 152 * 16;  // entries of each partial-sum array
+constexpr int kLzStamps = 9;              // timestamps per step of the persistent kernel
+
 struct LzState {
     // per Krylov slot j (device arrays of length max_steps + 2)
     int* e;          // exponent: w_j[i] = q_j[i] * 2^e[j]
@@ -33,6 +36,27 @@ struct LzState {
     int status;      // 0 ok, 7 breakdown, 6 non-finite
     int min_bits;    // fewest significant bits of any w_j
     int steps_done;
+};
+
+// Grid-reduction accumulator of the persistent kernel: an exact 128-bit sum
+// as three 42-bit limb sums (l2 holds the signed top limb) and a max.
+struct LzRedSet {
+    unsigned long long l0, l1, l2, mx;
+};
+
+// Arguments of the persistent Lanczos kernel (steps j0 .. j1-1 in one launch).
+struct LzFusedArgs {
+    int64_t* basis;
+    int64_t stride;      // slot stride in elements
+    int stored;          // slot(j) = basis + (stored ? j : j % 3) * stride
+    int j0, j1;
+    int64_t* u;
+    int64_t n;           // stored values (D * W)
+    LzState* lz;
+    unsigned int* gbar;  // grid-barrier arrivals, zero at launch
+    LzRedSet* red;       // three accumulator sets, zero at launch
+    unsigned long long* stamps;  // optional: %globaltimer of block 0 at kLzStamps
+                                 // points of every step (see ed_lanczos_fused.cu)
 };
 
 }  // namespace ed

@@ -17,35 +17,42 @@
 namespace ed {
 namespace dev {
 
-__device__ inline void lz_after_matvec(LzState* lz, int j, i128 alpha_raw, uint64_t m_u, int s_u, int Fc) {
-    const int eX = lz->e[j];
-    const uint64_t mX = lz->m[j];
-    const double bj = lz->beta[j];
-    const int e_u = eX - Fc + s_u;
-    lz->s_u = s_u;
-    lz->e_u = e_u;
-    lz->m_u = m_u;
-    if (!(bj > 0.0) || lz->status != 0) {
+// Scalars of one step after the matvec reduction.
+struct LzCoefs {
+    double alpha;
+    int64_t at[3];
+    int Fa;
+    int e_w;
+};
+
+// alpha_j and the integer axpy coefficients of step j from the exact
+// <w_j, u> (alpha_raw), slot j (eX, mX, bj) and slot j-1 (eP, mP and the
+// reciprocal ibP = 1 / beta_{j-1}).  One division per step: 1 / bj.
+__device__ inline LzCoefs lz_coefs(int j, i128 alpha_raw, int e_u, uint64_t m_u, int eX, uint64_t mX, double bj,
+                                   int eP, uint64_t mP, double ibP, int status) {
+    LzCoefs c;
+    if (!(bj > 0.0) || status != 0) {
         // after a breakdown (or a bad start) the recurrence only carries zeros
-        lz->alpha[j] = 0.0;
-        for (int k = 0; k < 3; ++k) { lz->at[k] = 0; lz->sh[k] = 0; }
-        lz->Fa = 0;
-        lz->e_w = eX;
-        return;
+        c.alpha = 0.0;
+        for (int k = 0; k < 3; ++k) c.at[k] = 0;
+        c.Fa = 0;
+        c.e_w = eX;
+        return c;
     }
+    const double ib = 1.0 / bj;
     const double anum = i128_to_f64(alpha_raw, eX + e_u + 24);
-    const double aj = anum / (bj * bj);
-    lz->alpha[j] = aj;
+    const double aj = (anum * ib) * ib;
+    c.alpha = aj;
 
     double a[3];
     uint64_t mm[3];
-    a[0] = ldexp(1.0, e_u) / bj;
+    a[0] = ldexp(ib, e_u);
     mm[0] = m_u;
-    a[1] = -aj * ldexp(1.0, eX) / bj;
+    a[1] = -aj * ldexp(ib, eX);
     mm[1] = mX;
     if (j > 0) {
-        a[2] = -bj * ldexp(1.0, lz->e[j - 1]) / lz->beta[j - 1];
-        mm[2] = lz->m[j - 1];
+        a[2] = -bj * ldexp(ibP, eP);
+        mm[2] = mP;
     } else {
         a[2] = 0.0;
         mm[2] = 0;
@@ -64,20 +71,41 @@ __device__ inline void lz_after_matvec(LzState* lz, int j, i128 alpha_raw, uint6
     int ka = 0;
     if (amax > 0.0) frexp(amax, &ka);  // amax < 2^ka
     const int Fmin = 62 - ka;
+    for (int k = 0; k < 3; ++k) c.at[k] = (mm[k] != 0 && a[k] != 0.0) ? llrint(ldexp(a[k], Fmin - e_w)) : 0;
+    c.Fa = Fmin;
+    c.e_w = e_w;
+    return c;
+}
+
+// 1 / beta for the w_{j-1} coefficient (beta > 0 on every step that uses it;
+// 0 keeps a breakdown's zeros finite).
+__device__ inline double lz_inv(double b) { return b > 0.0 ? 1.0 / b : 0.0; }
+
+// |w_{j+1}| from the exact sum of (q q) >> 16 at exponent e_w.
+__device__ inline double lz_beta(i128 sumsq, int e_w) { return sqrt(i128_to_f64(sumsq, 2 * e_w + 16)); }
+
+__device__ inline void lz_after_matvec(LzState* lz, int j, i128 alpha_raw, uint64_t m_u, int s_u, int Fc) {
+    const int eX = lz->e[j];
+    const int e_u = eX - Fc + s_u;
+    lz->s_u = s_u;
+    lz->e_u = e_u;
+    lz->m_u = m_u;
+    const LzCoefs c = lz_coefs(j, alpha_raw, e_u, m_u, eX, lz->m[j], lz->beta[j], j > 0 ? lz->e[j - 1] : 0,
+                               j > 0 ? lz->m[j - 1] : 0, j > 0 ? lz_inv(lz->beta[j - 1]) : 0.0, lz->status);
+    lz->alpha[j] = c.alpha;
     for (int k = 0; k < 3; ++k) {
-        lz->at[k] = (mm[k] != 0 && a[k] != 0.0) ? llrint(ldexp(a[k], Fmin - e_w)) : 0;
+        lz->at[k] = c.at[k];
         lz->sh[k] = 0;
     }
-    lz->Fa = Fmin;
-    lz->e_w = e_w;
+    lz->Fa = c.Fa;
+    lz->e_w = c.e_w;
 }
 
 __device__ inline void lz_after_axpy(LzState* lz, int j, i128 sumsq, uint64_t m_w) {
     const int e_w = lz->e_w;
     lz->e[j + 1] = e_w;
     lz->m[j + 1] = m_w;
-    const double b2 = i128_to_f64(sumsq, 2 * e_w + 16);
-    lz->beta[j + 1] = sqrt(b2);
+    lz->beta[j + 1] = lz_beta(sumsq, e_w);
     const int bits = bitlen_u64(m_w);
     if (bits < lz->min_bits) lz->min_bits = bits;
     if (m_w == 0 && lz->status == 0) lz->status = 7;  // breakdown

@@ -1,0 +1,312 @@
+// ed_lanczos_fused.cu — a run of FX Lanczos steps in one persistent
+// cooperative launch (HubMatrix_GPU.cuh:561-590, the recurrence of eigen()).
+//
+// The per-step path costs two launches per step, and the matvec launch
+// re-stages the down-spin tables into every CTA's shared memory each time.
+// Here each CTA (two per SM, all co-resident) stages the tables once and then
+// loops over the steps:
+//   phase M  u = H w_j with the shared-memory row engine (its own rows of u),
+//            then <w_j, u> and max|u|                           -> grid barrier
+//            every CTA derives alpha_j and the axpy coefficients (identical
+//            in every CTA: same integers, same scalar code)
+//   phase A  w_{j+1} = (a0 u + a1 w_j + a2 w_{j-1}) >> Fa on a grid-stride
+//            slice, then |w_{j+1}|^2 and max|w_{j+1}|           -> grid barrier
+//            every CTA derives beta_{j+1}; block 0 stores the scalars
+// Grid reductions: each CTA reduces its values in shared memory and thread 0
+// adds them to a global accumulator set with integer atomics — the 128-bit
+// sum split into three 42-bit limbs, so the total is exact and independent of
+// the order of arrival — and takes the max with atomicMax, before it arrives
+// at the barrier.  After the barrier one read of four words gives every CTA
+// the grid totals.  Three accumulator sets rotate: set r % 3 serves reduction
+// r, and block 0 zeroes the set of reduction r-1 once barrier r has completed
+// (every reader of it has passed barrier r by then; its next user adds only
+// after barrier r+1, which block 0 reaches after the zeroing).
+// The integer totals and the scalar arithmetic are those of the per-step
+// kernels, so the Lanczos coefficients are bit-identical to the per-step path.
+// Vectors written during the launch are read back with L2 (coherent) loads,
+// and before the bulk copies of a row written by another CTA the issuing
+// thread orders them behind the grid barrier with a proxy fence.
+// Grid barriers are bounded (poll count and %globaltimer): a CTA that gives
+// up sets *err and leaves; the host then reports ED_ERR_TIMEOUT.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ed_lanczos.hpp"
+#include "ed_lanczos_dev.cuh"
+#include "ed_matvec_tma.cuh"
+
+namespace ed {
+using namespace dev;
+
+namespace {
+
+constexpr long long kGridSpin = 1LL << 26;
+constexpr unsigned long long kGridWaitNs = 4000000000ULL;  // 4 s
+constexpr uint64_t kLimb = (1ULL << 42) - 1;
+
+__device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void red_release_gpu_add(unsigned int* p, unsigned int v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Thread 0: add a CTA's sum and max to an accumulator set.
+__device__ __forceinline__ void red_push(LzRedSet* r, i128 v, uint64_t m) {
+    const u128 uv = (u128)v;
+    atomicAdd(&r->l0, (unsigned long long)(uv & kLimb));
+    atomicAdd(&r->l1, (unsigned long long)((uv >> 42) & kLimb));
+    atomicAdd(&r->l2, (unsigned long long)(int64_t)(v >> 84));
+    atomicMax(&r->mx, (unsigned long long)m);
+}
+
+// Thread 0, after the barrier: the grid totals.
+__device__ __forceinline__ void red_pull(const LzRedSet* r, i128& v, uint64_t& m) {
+    const unsigned long long l0 = __ldcg(&r->l0), l1 = __ldcg(&r->l1), l2 = __ldcg(&r->l2);
+    m = __ldcg(&r->mx);
+    v = (i128)((u128)l0 + ((u128)l1 << 42) + ((u128)(i128)(int64_t)l2 << 84));
+}
+
+// Grid-wide barrier on a monotone arrival counter: the k-th barrier of the
+// launch completes when k * gridDim.x CTAs have arrived.  Writes and atomics
+// before it (by any thread of any CTA) are visible after it.  False when the
+// wait gave up; *give_up is then set for the whole CTA.
+__device__ __forceinline__ bool grid_sync(unsigned int* gbar, unsigned int& target, int* give_up, int* err) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        target += gridDim.x;
+        // release: this CTA's writes and atomics (ordered before this thread
+        // by the CTA barrier above) before the arrival
+        red_release_gpu_add(gbar, 1u);
+        const unsigned long long t0 = global_ns();
+        long long it = 0;
+        while (ld_relaxed_gpu(gbar) < target) {
+            if (++it > kGridSpin || global_ns() - t0 > kGridWaitNs) {
+                atomicExch(err, 1);
+                *give_up = 1;
+                break;
+            }
+        }
+        fence_acq_rel_gpu();  // acquire: everything released before the last arrival
+    }
+    __syncthreads();
+    return *give_up == 0;
+}
+
+__device__ __forceinline__ unsigned long long* stamps_at(const LzFusedArgs& f, int j) {
+    return f.stamps ? f.stamps + kLzStamps * (size_t)j : nullptr;
+}
+
+// Timestamps (block 0, thread 0) per step: 0 start, 1 rows done, 2 block
+// sums done, 3 barrier passed, 4 coefficients done, 5 axpy done, 6 block sums
+// done, 7 barrier passed, 8 scalars done.
+
+struct SlotScalars {
+    int e;
+    uint64_t m;
+    double beta;
+    double ib;  // 1 / beta (0 when beta is 0)
+};
+
+}  // namespace
+
+template <bool CPLX, bool FAST, bool SCHED>
+__global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, const LzFusedArgs f) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint32_t uoff[kTmaUpStage];
+    __shared__ uint32_t uent[kTmaUpStage];
+    __shared__ int give_up;
+    __shared__ i128 s128[32];
+    __shared__ uint64_t s64[32];
+    __shared__ SlotScalars sX, sP;  // slots j and j-1
+    __shared__ int s_status, s_min_bits;
+    __shared__ LzCoefs s_coef;
+    const TmaSmem S = tma_view(a, sm, uoff, uent, &give_up);
+    LzState* lz = f.lz;
+    const int tid = threadIdx.x;
+    const bool has_row = blockIdx.x < (uint32_t)a.dimUP;
+    const uint32_t G = gridDim.x;
+
+    if (tid == 0) {
+        tma_init(S);
+        tma_issue_tables(a, S);
+        const int j = f.j0;
+        sX = {lz->e[j], lz->m[j], lz->beta[j], lz_inv(lz->beta[j])};
+        if (j > 0) sP = {lz->e[j - 1], lz->m[j - 1], lz->beta[j - 1], lz_inv(lz->beta[j - 1])};
+        else sP = {0, 0, 0.0, 0.0};
+        s_status = lz->status;
+        s_min_bits = lz->min_bits;
+    }
+    if (SCHED) tma_zero_slots(a, S);
+    __syncthreads();
+    if (!tma::mbar_wait(&S.bar[2], 0)) {
+        if (tid == 0) atomicExch(a.err, 1);
+        give_up = 1;
+    }
+    __syncthreads();
+    if (give_up) return;  // no row copy has been issued yet
+
+    auto slot = [&](int j) -> int64_t* {
+        return f.basis + (size_t)(f.stored ? j : j % 3) * (size_t)f.stride;
+    };
+
+    uint32_t rc = 0;          // rows streamed through the row buffers
+    unsigned int target = 0;  // grid-barrier arrivals expected so far
+    int r = 0;                // grid reductions so far
+    for (int j = f.j0; j < f.j1; ++j) {
+        const int64_t* xq = slot(j);
+        const int64_t* pq = j > 0 ? slot(j - 1) : slot(j);
+        int64_t* wq = slot(j + 1);
+        const bool stamp = f.stamps && blockIdx.x == 0 && tid == 0;
+        unsigned long long* st = stamps_at(f, j);
+        if (stamp) st[0] = global_ns();
+
+        // ---- phase M: u = H w_j -------------------------------------------
+        const int b = a.bq_bits + bitlen_u64(sX.m) - 62;
+        const int s_u = b > 0 ? b : 0;
+        if (tid == 0 && has_row) {
+            tma::fence_proxy_async_global();
+            tma::fence_proxy_async_smem();
+            tma_issue_row<CPLX>(a, S, xq, blockIdx.x, rc & 1);
+        }
+        {
+            i128 dot = 0;
+            uint64_t mx = 0;
+            tma_rows<CPLX, 1, FAST, true, SCHED>(a, S, xq, f.u, nullptr, rc, 0, s_u, dot, mx);
+            if (give_up) return;
+            if (stamp) st[1] = global_ns();
+            block_sum_max(dot, mx, s128, s64);
+            if (tid == 0) red_push(&f.red[r % 3], dot, mx);
+            if (stamp) st[2] = global_ns();
+        }
+        if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
+        if (tid == 0) {
+            if (stamp) st[3] = global_ns();
+            i128 s;
+            uint64_t m;
+            red_pull(&f.red[r % 3], s, m);
+            if (blockIdx.x == 0) f.red[(r + 2) % 3] = LzRedSet{0, 0, 0, 0};
+            const int e_u = sX.e - a.Fc + s_u;
+            s_coef = lz_coefs(j, s, e_u, m, sX.e, sX.m, sX.beta, sP.e, sP.m, sP.ib, s_status);
+            if (blockIdx.x == 0) {
+                lz->s_u = s_u;
+                lz->e_u = e_u;
+                lz->m_u = m;
+                lz->alpha[j] = s_coef.alpha;
+                for (int k = 0; k < 3; ++k) {
+                    lz->at[k] = s_coef.at[k];
+                    lz->sh[k] = 0;
+                }
+                lz->Fa = s_coef.Fa;
+                lz->e_w = s_coef.e_w;
+            }
+            if (stamp) st[4] = global_ns();
+        }
+        ++r;
+        __syncthreads();
+
+        // ---- phase A: w_{j+1} = (a0 u + a1 w_j + a2 w_{j-1}) >> Fa ---------
+        {
+            const int64_t a0 = s_coef.at[0], a1 = s_coef.at[1], a2 = s_coef.at[2];
+            const int Fa = s_coef.Fa;
+            i128 ss = 0;
+            uint64_t mw = 0;
+            const int64_t npair = f.n >> 1;
+            const longlong2* u2 = reinterpret_cast<const longlong2*>(f.u);
+            const longlong2* x2 = reinterpret_cast<const longlong2*>(xq);
+            const longlong2* p2 = reinterpret_cast<const longlong2*>(pq);
+            longlong2* w2 = reinterpret_cast<longlong2*>(wq);
+            for (int64_t i = (int64_t)blockIdx.x * blockDim.x + tid; i < npair; i += (int64_t)G * blockDim.x) {
+                const longlong2 uu = __ldcg(u2 + i), xx = __ldcg(x2 + i), pp = __ldcg(p2 + i);
+                longlong2 w;
+                w.x = shr_round_i64(mul_wide(a0, uu.x) + mul_wide(a1, xx.x) + mul_wide(a2, pp.x), Fa);
+                w.y = shr_round_i64(mul_wide(a0, uu.y) + mul_wide(a1, xx.y) + mul_wide(a2, pp.y), Fa);
+                w2[i] = w;
+                ss += (mul_wide(w.x, w.x) >> 16) + (mul_wide(w.y, w.y) >> 16);
+                const uint64_t ax = (uint64_t)(w.x < 0 ? -w.x : w.x), ay = (uint64_t)(w.y < 0 ? -w.y : w.y);
+                mw = ax > mw ? ax : mw;
+                mw = ay > mw ? ay : mw;
+            }
+            if ((f.n & 1) && blockIdx.x == 0 && tid == 0) {
+                const int64_t i = f.n - 1;
+                const int64_t w = shr_round_i64(
+                    mul_wide(a0, __ldcg(f.u + i)) + mul_wide(a1, __ldcg(xq + i)) + mul_wide(a2, __ldcg(pq + i)), Fa);
+                wq[i] = w;
+                ss += mul_wide(w, w) >> 16;
+                const uint64_t aw = (uint64_t)(w < 0 ? -w : w);
+                mw = aw > mw ? aw : mw;
+            }
+            if (stamp) st[5] = global_ns();
+            block_sum_max(ss, mw, s128, s64);
+            if (tid == 0) red_push(&f.red[r % 3], ss, mw);
+            if (stamp) st[6] = global_ns();
+        }
+        if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
+        if (tid == 0) {
+            if (stamp) st[7] = global_ns();
+            i128 s;
+            uint64_t m;
+            red_pull(&f.red[r % 3], s, m);
+            if (blockIdx.x == 0) f.red[(r + 2) % 3] = LzRedSet{0, 0, 0, 0};
+            const int e_w = s_coef.e_w;
+            const double beta = lz_beta(s, e_w);
+            const int bits = bitlen_u64(m);
+            if (bits < s_min_bits) s_min_bits = bits;
+            if (m == 0 && s_status == 0) s_status = 7;  // breakdown
+            if (blockIdx.x == 0) {
+                lz->e[j + 1] = e_w;
+                lz->m[j + 1] = m;
+                lz->beta[j + 1] = beta;
+                lz->min_bits = s_min_bits;
+                lz->status = s_status;
+                lz->steps_done = j + 1;
+            }
+            sP = sX;
+            sX = {e_w, m, beta, lz_inv(beta)};
+            if (stamp) st[8] = global_ns();
+        }
+        ++r;
+        __syncthreads();
+    }
+}
+
+// Cooperative launch of steps j0 .. j1-1; cudaErrorNotSupported when the
+// operator has no shared-memory plan, or the grid cannot be co-resident.
+// f.gbar and the three sets at f.red must be zero.
+cudaError_t launch_lz_fused(const ed_op* op, const LzFusedArgs& f, cudaStream_t s) {
+    if (op->tma_smem <= 0) return cudaErrorNotSupported;
+    const void* fn;
+    if (op->cplx)
+        fn = op->mv_fast ? (const void*)k_lz_fused<true, true, false> : (const void*)k_lz_fused<true, false, false>;
+    else if (!op->mv_fast)
+        fn = (const void*)k_lz_fused<false, false, false>;
+    else
+        fn = op->mv.dnSched ? (const void*)k_lz_fused<false, true, true> : (const void*)k_lz_fused<false, true, false>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, op->tma_smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, sms = 0, coop = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTmaThreads, op->tma_smem)) != cudaSuccess)
+        return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op->device)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, op->device)) != cudaSuccess) return e;
+    if (!coop || per_sm < 1) return cudaErrorNotSupported;
+    const int64_t g = (int64_t)sms * (per_sm < 2 ? per_sm : 2);
+    MvArgs av = op->mv;
+    LzFusedArgs fv = f;
+    void* args[] = {&av, &fv};
+    return cudaLaunchCooperativeKernel(fn, dim3((unsigned)g), dim3(kTmaThreads), args, (size_t)op->tma_smem, s);
+}
+
+}  // namespace ed

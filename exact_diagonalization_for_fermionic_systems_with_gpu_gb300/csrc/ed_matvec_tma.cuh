@@ -1,0 +1,415 @@
+// ed_matvec_tma.cuh — the shared-memory row engine of the matvec, used by the
+// one-launch matvec (ed_matvec_tma.cu) and by the persistent Lanczos kernel
+// (ed_lanczos_fused.cu).
+//
+// A CTA of kTmaThreads threads
+//  * holds the whole down-spin operator (CSR entries, row pointers, npos,
+//    folded diagonal, bitstrings) in shared memory, moved there by TMA bulk
+//    copies (cp.async.bulk global->shared, completion counted on an mbarrier);
+//  * walks the up-rows u = blockIdx.x, + gridDim.x, ... with x[u, :] double
+//    buffered by bulk copies: row u+gridDim.x streams in while row u is
+//    computed;
+//  * computes the down term entirely from shared memory and the up term with
+//    coalesced L2 loads, two output columns per thread so at least eight
+//    up-term loads are in flight per thread.
+// Every mbarrier wait is bounded: after kMaxSpin polls the CTA records an
+// error in *err, waits (bounded) for its copies in flight and stops.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ed_device.cuh"
+#include "ed_internal.hpp"
+#include "ed_matvec_common.cuh"
+
+namespace ed {
+using namespace dev;
+
+constexpr int kTmaThreads = 512;
+constexpr int kTmaUpStage = 256;  // longest up-row held in the static offset arrays
+constexpr long long kMaxSpin = 1LL << 22;
+
+namespace tma {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// generic-proxy accesses of shared memory before async-proxy writes into it
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// generic-proxy writes of global memory (observed by this thread) before
+// async-proxy reads of it
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+__device__ __forceinline__ void expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// dst, src 16-byte aligned; bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false when it gave up.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    const uint32_t addr = smem_u32(bar);
+    for (long long it = 0; it < kMaxSpin; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__host__ __device__ constexpr uint32_t round16(uint32_t b) { return (b + 15u) / 16u * 16u; }
+
+}  // namespace tma
+
+// Shared-memory views: the dynamic area follows the byte offsets in MvArgs
+// (barriers at 0: [0], [1] row buffers, [2] down tables); the up-row offsets
+// and the give-up word are static arrays of the kernel.
+struct TmaSmem {
+    uint64_t* bar;
+    int64_t* row0;
+    int64_t* row1;
+    uint32_t* dptr;
+    uint32_t* dent;
+    uint8_t* dnpos;
+    int64_t* ddq;
+    uint64_t* dst;
+    uint16_t* sched;  // gather schedule (when a.dnSched)
+    uint8_t* steps;
+    uint32_t* uoff;
+    uint32_t* uent;
+    int* give_up;
+};
+
+__device__ __forceinline__ TmaSmem tma_view(const MvArgs& a, unsigned char* sm, uint32_t* uoff, uint32_t* uent,
+                                            int* give_up) {
+    TmaSmem S;
+    S.bar = reinterpret_cast<uint64_t*>(sm);
+    S.row0 = reinterpret_cast<int64_t*>(sm + a.sm_row0);
+    S.row1 = reinterpret_cast<int64_t*>(sm + a.sm_row1);
+    S.dptr = reinterpret_cast<uint32_t*>(sm + a.sm_dnptr);
+    S.dent = reinterpret_cast<uint32_t*>(sm + a.sm_dnent);
+    S.dnpos = sm + a.sm_dnnpos;
+    S.ddq = reinterpret_cast<int64_t*>(sm + a.sm_ddnq);
+    S.dst = reinterpret_cast<uint64_t*>(sm + a.sm_stdn);
+    S.sched = reinterpret_cast<uint16_t*>(sm + a.sm_sched);
+    S.steps = sm + a.sm_steps;
+    S.uoff = uoff;
+    S.uent = uent;
+    S.give_up = give_up;
+    return S;
+}
+
+// Thread 0: initialise the three barriers.
+__device__ __forceinline__ void tma_init(const TmaSmem& S) {
+    for (int k = 0; k < 3; ++k) tma::mbar_init(&S.bar[k], 1);
+    tma::fence_mbar_init();
+    *S.give_up = 0;
+}
+
+// Thread 0: start the copies of the down-spin tables (completion on bar[2]).
+// The device tables are allocated in multiples of 16 bytes and the shared
+// regions in multiples of 128, so every copy is rounded up to 16 bytes.
+__device__ __forceinline__ void tma_issue_tables(const MvArgs& a, const TmaSmem& S) {
+    const uint32_t dimDN = (uint32_t)a.dimDN;
+    if (a.dnSched) {
+        const uint32_t b_sc = tma::round16((uint32_t)a.schedSteps * (uint32_t)a.dimDNp * 2u),
+                       b_stp = tma::round16((uint32_t)a.dimDNp / 32u), b_dq = tma::round16(dimDN * 8u);
+        tma::expect_tx(&S.bar[2], b_sc + b_stp + 2 * b_dq);
+        if (b_sc) tma::bulk_g2s(S.sched, a.dnSched, b_sc, &S.bar[2]);
+        tma::bulk_g2s(S.steps, a.dnSteps, b_stp, &S.bar[2]);
+        tma::bulk_g2s(S.ddq, a.dDNq, b_dq, &S.bar[2]);
+        tma::bulk_g2s(S.dst, a.stDN, b_dq, &S.bar[2]);
+        return;
+    }
+    const uint32_t b_ptr = tma::round16((dimDN + 1) * 4u), b_ent = tma::round16(a.dnNnz * 4u),
+                   b_pos = tma::round16(dimDN), b_dq = tma::round16(dimDN * 8u), b_st = b_dq;
+    tma::expect_tx(&S.bar[2], b_ptr + b_ent + b_pos + b_dq + b_st);
+    tma::bulk_g2s(S.dptr, a.dnPtr, b_ptr, &S.bar[2]);
+    if (b_ent) tma::bulk_g2s(S.dent, a.dnEntC, b_ent, &S.bar[2]);  // no down hops: nothing to copy
+    tma::bulk_g2s(S.dnpos, a.dnNpos, b_pos, &S.bar[2]);
+    tma::bulk_g2s(S.ddq, a.dDNq, b_dq, &S.bar[2]);
+    tma::bulk_g2s(S.dst, a.stDN, b_st, &S.bar[2]);
+}
+
+// The 16 zeros of both row buffers that idle lanes of the gather schedule
+// read (the bulk copies only ever write [0, dimDN)).
+__device__ __forceinline__ void tma_zero_slots(const MvArgs& a, const TmaSmem& S) {
+    if (threadIdx.x < 16) {
+        S.row0[2 * a.schedNeg + threadIdx.x] = 0;
+        S.row1[2 * a.schedNeg + threadIdx.x] = 0;
+    }
+}
+
+// Thread 0: start the copy of row u of x into row buffer `buf`.
+template <bool CPLX>
+__device__ __forceinline__ void tma_issue_row(const MvArgs& a, const TmaSmem& S, const int64_t* xq, uint32_t u,
+                                              int buf) {
+    constexpr int W = CPLX ? 2 : 1;
+    const uint32_t row_bytes = (uint32_t)a.dimDN * W * 8u;
+    tma::expect_tx(&S.bar[buf], row_bytes);
+    tma::bulk_g2s(buf ? S.row1 : S.row0, xq + (size_t)u * a.dimDN * W, row_bytes, &S.bar[buf]);
+}
+
+// Up-term element load: read-only path for a one-launch matvec, L2
+// (coherent) loads when x was written earlier in the same launch.
+template <bool CPLX, bool COH>
+__device__ __forceinline__ void up_load(const int64_t* __restrict__ xq, uint32_t idx, int64_t& r, int64_t& i) {
+    if (CPLX) {
+        const longlong2* p = reinterpret_cast<const longlong2*>(xq) + idx;
+        const longlong2 v = COH ? __ldcg(p) : __ldg(p);
+        r = v.x;
+        i = v.y;
+    } else {
+        r = COH ? __ldcg(xq + idx) : __ldg(xq + idx);
+        i = 0;
+    }
+}
+
+template <bool CPLX, bool COH>
+__device__ __forceinline__ void acc_up(const int64_t* __restrict__ xq, uint32_t idx, int64_t& r, int64_t& i) {
+    int64_t vr, vi;
+    up_load<CPLX, COH>(xq, idx, vr, vi);
+    r += vr;
+    if (CPLX) i += vi;
+}
+
+// The rows of this CTA: u = H x (OUT 0: FP64 y with exponent E_out; OUT 1:
+// FX uq >> s_u with the <x,u> and max|u| partials in dot, mx).
+// On entry thread 0 has issued the copy of row blockIdx.x into buffer rc & 1
+// (when blockIdx.x < dimUP) and the tables are in shared memory; rc counts the
+// rows this CTA has streamed so far (it fixes buffer and barrier phase) and
+// is advanced past the rows done.  On a give-up *S.give_up is set, the copy
+// in flight has been waited for and the function returns early.
+template <bool CPLX, int OUT, bool FAST, bool COH, bool SCHED>
+__device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, const int64_t* __restrict__ xq,
+                                         int64_t* __restrict__ uq, double* __restrict__ y, uint32_t& rc, int E_out,
+                                         int s_u, i128& dot, uint64_t& mx) {
+    constexpr int W = CPLX ? 2 : 1;
+    const uint32_t dimUP = (uint32_t)a.dimUP, dimDN = (uint32_t)a.dimDN;
+    const int tid = threadIdx.x, T = blockDim.x;
+    const bool merge = a.mergeUD != 0;
+    const bool unitU = a.unitUP != 0 && a.nclsUP == 1;
+    const bool unitD = a.unitDN != 0 && a.nclsDN == 1;
+
+    bool issued_next = false;  // thread 0: a copy for row u+gridDim.x is in flight
+    for (uint32_t u = blockIdx.x; u < dimUP; u += gridDim.x, ++rc) {
+        const int buf = rc & 1;
+        const uint32_t parity = (rc >> 1) & 1;
+        // prefetch the next row into the other buffer (its readers finished
+        // at the barrier that closed the previous iteration)
+        const uint32_t un = u + gridDim.x;
+        issued_next = false;
+        if (tid == 0 && un < dimUP) {
+            tma::fence_proxy_async_smem();
+            tma_issue_row<CPLX>(a, S, xq, un, buf ^ 1);
+            issued_next = true;
+        }
+        const uint32_t p0 = __ldg(a.upPtr + u), lenU = __ldg(a.upPtr + u + 1) - p0;
+        const int nposU = FAST ? (int)__ldg(a.upNpos + u) : 0;
+        for (uint32_t k = tid; k < lenU; k += T) {
+            const uint32_t e = __ldg(a.upEntC + p0 + k);
+            S.uoff[k] = (e & kColMask) * dimDN;
+            S.uent[k] = e;
+        }
+        if (!tma::mbar_wait(&S.bar[buf], parity)) {
+            if (tid == 0) atomicExch(a.err, 1);
+            *S.give_up = 1;
+        } else if (SCHED) {
+            // -x beside x, so that a schedule index carries the sign
+            int64_t* xb = buf ? S.row1 : S.row0;
+            for (uint32_t i = tid; i < dimDN; i += T) xb[a.schedNeg + i] = -xb[i];
+        }
+        __syncthreads();
+        if (*S.give_up) {
+            // the copy issued for the next row must land before the CTA
+            // moves on (bounded)
+            if (tid == 0 && issued_next) tma::mbar_wait(&S.bar[buf ^ 1], ((rc + 1) >> 1) & 1);
+            return;
+        }
+        const int64_t* xrow = buf ? S.row1 : S.row0;
+        const uint64_t stu = __ldg(a.stUP + u);
+        const int64_t du = __ldg(a.dUPq + u);
+        const uint32_t ubase = u * dimDN;
+
+        for (uint32_t d0 = tid; d0 < dimDN; d0 += 2 * T) {
+            const uint32_t d1 = d0 + T;
+            const bool v1 = d1 < dimDN;
+            const uint32_t d1c = v1 ? d1 : d0;  // clamp: the second column repeats d0 and is not stored
+            i128 ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;
+            if (FAST) {
+                int64_t upr0 = 0, upi0 = 0, unr0 = 0, uni0 = 0, upr1 = 0, upi1 = 0, unr1 = 0, uni1 = 0;
+                int k = 0;
+                if (v1) {
+#pragma unroll 4
+                    for (; k < nposU; ++k) {
+                        const uint32_t o = S.uoff[k];
+                        acc_up<CPLX, COH>(xq, o + d0, upr0, upi0);
+                        acc_up<CPLX, COH>(xq, o + d1, upr1, upi1);
+                    }
+#pragma unroll 4
+                    for (; k < (int)lenU; ++k) {
+                        const uint32_t o = S.uoff[k];
+                        acc_up<CPLX, COH>(xq, o + d0, unr0, uni0);
+                        acc_up<CPLX, COH>(xq, o + d1, unr1, uni1);
+                    }
+                } else {
+#pragma unroll 4
+                    for (; k < nposU; ++k) acc_up<CPLX, COH>(xq, S.uoff[k] + d0, upr0, upi0);
+#pragma unroll 4
+                    for (; k < (int)lenU; ++k) acc_up<CPLX, COH>(xq, S.uoff[k] + d0, unr0, uni0);
+                }
+                int64_t dr0 = 0, di0 = 0, dr1 = 0, di1 = 0;
+                if (SCHED) {
+                    // conflict-free schedule: in every step the 16 lanes of a
+                    // half warp read 16 different bank pairs of [x | -x | 0]
+                    const uint32_t dp = (uint32_t)a.dimDNp;
+                    const uint16_t* sc0 = S.sched + d0;
+                    const int n0 = S.steps[d0 >> 5];
+#pragma unroll 4
+                    for (int s = 0; s < n0; ++s) dr0 += xrow[sc0[s * dp]];
+                    if (v1) {
+                        const uint16_t* sc1 = S.sched + d1;
+                        const int n1 = S.steps[d1 >> 5];
+#pragma unroll 4
+                        for (int s = 0; s < n1; ++s) dr1 += xrow[sc1[s * dp]];
+                    }
+                } else {
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const uint32_t d = c ? d1c : d0;
+                    const uint32_t q0 = S.dptr[d], q1 = S.dptr[d + 1], qp = q0 + S.dnpos[d];
+                    int64_t pr = 0, pi = 0, nr = 0, ni = 0;
+                    for (uint32_t q = q0; q < qp; ++q) {
+                        const uint32_t col = (S.dent[q] & kColMask) * W;
+                        pr += xrow[col];
+                        if (CPLX) pi += xrow[col + 1];
+                    }
+                    for (uint32_t q = qp; q < q1; ++q) {
+                        const uint32_t col = (S.dent[q] & kColMask) * W;
+                        nr += xrow[col];
+                        if (CPLX) ni += xrow[col + 1];
+                    }
+                    if (c) {
+                        dr1 = pr - nr;
+                        di1 = pi - ni;
+                    } else {
+                        dr0 = pr - nr;
+                        di0 = pi - ni;
+                    }
+                }
+                }
+                if (merge) {
+                    apply_class<CPLX>(ar0, ai0, (upr0 - unr0) + dr0, (upi0 - uni0) + di0, a.coefUP, 0, unitU, a.Fc);
+                    apply_class<CPLX>(ar1, ai1, (upr1 - unr1) + dr1, (upi1 - uni1) + di1, a.coefUP, 0, unitU, a.Fc);
+                } else {
+                    if (lenU) {
+                        apply_class<CPLX>(ar0, ai0, upr0 - unr0, upi0 - uni0, a.coefUP, 0, unitU, a.Fc);
+                        apply_class<CPLX>(ar1, ai1, upr1 - unr1, upi1 - uni1, a.coefUP, 0, unitU, a.Fc);
+                    }
+                    if (a.nclsDN) {
+                        apply_class<CPLX>(ar0, ai0, dr0, di0, a.coefDN, 0, unitD, a.Fc);
+                        apply_class<CPLX>(ar1, ai1, dr1, di1, a.coefDN, 0, unitD, a.Fc);
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const uint32_t d = c ? d1c : d0;
+                    i128& ar = c ? ar1 : ar0;
+                    i128& ai = c ? ai1 : ai0;
+                    {
+                        int cur = -1;
+                        int64_t sr = 0, si = 0;
+                        for (uint32_t k = 0; k < lenU; ++k) {
+                            const uint32_t e = S.uent[k];
+                            const int cl = (int)((e >> kClassShift) & kClassMask);
+                            if (cl != cur) {
+                                if (cur >= 0) apply_class<CPLX>(ar, ai, sr, si, a.coefUP, cur, unitU, a.Fc);
+                                sr = 0;
+                                si = 0;
+                                cur = cl;
+                            }
+                            int64_t r, i;
+                            up_load<CPLX, COH>(xq, S.uoff[k] + d, r, i);
+                            sr += apply_sign(r, e);
+                            if (CPLX) si += apply_sign(i, e);
+                        }
+                        if (cur >= 0) apply_class<CPLX>(ar, ai, sr, si, a.coefUP, cur, unitU, a.Fc);
+                    }
+                    {
+                        int cur = -1;
+                        int64_t sr = 0, si = 0;
+                        for (uint32_t q = S.dptr[d]; q < S.dptr[d + 1]; ++q) {
+                            const uint32_t e = S.dent[q];
+                            const int cl = (int)((e >> kClassShift) & kClassMask);
+                            if (cl != cur) {
+                                if (cur >= 0) apply_class<CPLX>(ar, ai, sr, si, a.coefDN, cur, unitD, a.Fc);
+                                sr = 0;
+                                si = 0;
+                                cur = cl;
+                            }
+                            const uint32_t col = (e & kColMask) * W;
+                            sr += apply_sign(xrow[col], e);
+                            if (CPLX) si += apply_sign(xrow[col + 1], e);
+                        }
+                        if (cur >= 0) apply_class<CPLX>(ar, ai, sr, si, a.coefDN, cur, unitD, a.Fc);
+                    }
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                if (c == 1 && !v1) break;
+                const uint32_t d = c ? d1 : d0;
+                i128& ar = c ? ar1 : ar0;
+                i128& ai = c ? ai1 : ai0;
+                const int64_t xr = xrow[d * W];
+                const int64_t xi = CPLX ? xrow[d * W + 1] : 0;
+                const int64_t dq = du + S.ddq[d] + a.Uq * (int64_t)__popcll(stu & S.dst[d] & a.mask);
+                ar += mul_wide(dq, xr);
+                if (CPLX) ai += mul_wide(dq, xi);
+                const size_t o = (size_t)(ubase + d) * W;
+                if (OUT == 0) {
+                    y[o] = i128_to_f64(ar, E_out);
+                    if (CPLX) y[o + 1] = i128_to_f64(ai, E_out);
+                } else {
+                    const int64_t qr = shr_round_i64(ar, s_u);
+                    uq[o] = qr;
+                    dot += mul_wide(xr, qr) >> 24;
+                    uint64_t aq = (uint64_t)(qr < 0 ? -qr : qr);
+                    mx = aq > mx ? aq : mx;
+                    if (CPLX) {
+                        const int64_t qi = shr_round_i64(ai, s_u);
+                        uq[o + 1] = qi;
+                        dot += mul_wide(xi, qi) >> 24;
+                        aq = (uint64_t)(qi < 0 ? -qi : qi);
+                        mx = aq > mx ? aq : mx;
+                    }
+                }
+            }
+        }
+        __syncthreads();  // row buffer and uoff are free for the next iteration
+    }
+}
+
+}  // namespace ed

@@ -255,4 +255,132 @@ ed_status build_spin(const SpinBasis& basis, const ed_term* terms, int n_terms,
     return ED_OK;
 }
 
+bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* err) {
+    if (t.complex_coef || t.coef.size() > 1) {
+        if (err) *err = "gather schedule: needs a real single-class table";
+        return false;
+    }
+    if (t.count > kSchedMaxCount) {
+        if (err) *err = "gather schedule: too many states";
+        return false;
+    }
+    const int64_t count = t.count;
+    const int64_t cpad = (count + 31) / 32 * 32;
+    const int64_t neg_base = (count + 15) / 16 * 16;
+    const int64_t zero_base = 2 * neg_base;
+    const int64_t ngroups = cpad / 16;
+    constexpr int kL = 16, kB = 16;
+    struct Edge {
+        int lane, bank;
+        uint16_t word;
+    };
+    std::vector<std::vector<uint16_t>> group_steps(ngroups);  // [group] -> words by (step*16 + lane)
+    std::vector<int> group_deg(ngroups, 0);
+    int smax = 0;
+    for (int64_t gi = 0; gi < ngroups; ++gi) {
+        std::vector<Edge> edges;
+        int degL[kL] = {0}, degB[kB] = {0};
+        for (int l = 0; l < kL; ++l) {
+            const int64_t d = gi * 16 + l;
+            if (d >= count) continue;
+            for (int k = 0; k < t.len[d]; ++k) {
+                const uint32_t e = t.ent[(size_t)k * count + d];
+                const uint32_t col = e & kColMask;
+                const int bank = (int)(col % 16);
+                edges.push_back({l, bank, (uint16_t)(col + ((e & kSignBit) ? neg_base : 0))});
+                ++degL[l];
+                ++degB[bank];
+            }
+        }
+        int D = 0;
+        for (int i = 0; i < kL; ++i) D = std::max(D, degL[i]);
+        for (int i = 0; i < kB; ++i) D = std::max(D, degB[i]);
+        std::vector<int> cL((size_t)kL * D, -1), cB((size_t)kB * D, -1), color(edges.size(), -1);
+        auto setc = [&](int e, int c) {
+            color[e] = c;
+            cL[(size_t)edges[e].lane * D + c] = e;
+            cB[(size_t)edges[e].bank * D + c] = e;
+        };
+        for (int e = 0; e < (int)edges.size(); ++e) {
+            const int l = edges[e].lane, b = edges[e].bank;
+            int a = 0, bb = 0;
+            while (cL[(size_t)l * D + a] != -1) ++a;   // free at the lane
+            while (cB[(size_t)b * D + bb] != -1) ++bb; // free at the bank
+            if (cB[(size_t)b * D + a] != -1) {
+                // swap colours a and bb along the alternating path that leaves
+                // bank b on colour a; it cannot reach lane l (no a-edge there)
+                std::vector<int> path;
+                bool at_bank = true;
+                int node = b, c = a;
+                for (;;) {
+                    const int pe = at_bank ? cB[(size_t)node * D + c] : cL[(size_t)node * D + c];
+                    if (pe == -1) break;
+                    path.push_back(pe);
+                    node = at_bank ? edges[pe].lane : edges[pe].bank;
+                    at_bank = !at_bank;
+                    c = (c == a) ? bb : a;
+                }
+                for (int pe : path) {
+                    cL[(size_t)edges[pe].lane * D + color[pe]] = -1;
+                    cB[(size_t)edges[pe].bank * D + color[pe]] = -1;
+                }
+                for (int pe : path) setc(pe, color[pe] == a ? bb : a);
+            }
+            setc(e, a);
+        }
+        // verify: one entry per lane and per bank pair in every step; idle
+        // lanes take the zeros of the bank pairs left free
+        std::vector<uint16_t> words((size_t)D * kL, 0);
+        for (int c = 0; c < D; ++c) {
+            int seen = 0;
+            for (int l = 0; l < kL; ++l) {
+                const int e = cL[(size_t)l * D + c];
+                if (e < 0) continue;
+                const int bit = 1 << edges[e].bank;
+                if (seen & bit || color[e] != c) {
+                    if (err) *err = "gather schedule: colouring check failed";
+                    return false;
+                }
+                seen |= bit;
+                words[(size_t)c * kL + l] = edges[e].word;
+            }
+            int b = 0;
+            for (int l = 0; l < kL; ++l) {
+                if (cL[(size_t)l * D + c] >= 0) continue;
+                while (seen & (1 << b)) ++b;
+                words[(size_t)c * kL + l] = (uint16_t)(zero_base + b);
+                seen |= 1 << b;
+            }
+        }
+        for (int e = 0; e < (int)edges.size(); ++e)
+            if (color[e] < 0) {
+                if (err) *err = "gather schedule: uncoloured entry";
+                return false;
+            }
+        group_steps[gi] = std::move(words);
+        group_deg[gi] = D;
+        smax = std::max(smax, D);
+    }
+    if (smax > 255) {
+        if (err) *err = "gather schedule: more than 255 steps";
+        return false;
+    }
+    g->steps = smax;
+    g->count_pad = cpad;
+    g->neg_base = neg_base;
+    // steps a group does not use read the zero of the lane's own bank pair
+    g->ent.assign((size_t)std::max(smax, 1) * cpad, 0);
+    for (int s2 = 0; s2 < std::max(smax, 1); ++s2)
+        for (int64_t d = 0; d < cpad; ++d) g->ent[(size_t)s2 * cpad + d] = (uint16_t)(zero_base + d % 16);
+    g->steps32.assign(cpad / 32, 0);
+    for (int64_t gi = 0; gi < ngroups; ++gi) {
+        const int D = group_deg[gi];
+        for (int c = 0; c < D; ++c)
+            for (int l = 0; l < kL; ++l) g->ent[(size_t)c * cpad + gi * 16 + l] = group_steps[gi][(size_t)c * kL + l];
+        uint8_t& st = g->steps32[gi / 2];
+        st = (uint8_t)std::max<int>(st, D);
+    }
+    return true;
+}
+
 }  // namespace ed

@@ -75,6 +75,34 @@ struct SpinEll {
     bool overflow = false;
 };
 
+// Bank-conflict-free gather schedule for a real single-class table (the
+// down-spin term of the shared-memory matvec).  The kernel keeps a row of x
+// in shared memory as [x (neg_base words) | -x (neg_base words) | 16 zeros];
+// a schedule entry is an index into that buffer (+x, -x or a zero), so the
+// inner loop is load-index, load-value, add.  Column d is handled by lane
+// d % 32 of a warp; the 16 lanes of a half warp load 8-byte words, and the
+// word at index i sits in bank pair i % 16 (neg_base is a multiple of 16).
+// Step s gives every column at most one of its entries, chosen so that the
+// 16 columns of a half warp touch 16 different bank pairs: a proper edge
+// colouring of the bipartite multigraph (columns x bank pairs, one edge per
+// entry), which needs exactly as many colours as its largest degree
+// (Koenig's theorem) and is found with alternating-path recolouring.  Lanes
+// without an entry in a step read the zero of a bank pair no other lane of
+// the half warp uses in that step.
+constexpr int kSchedMaxCount = 32752;  // 2 * neg_base + 16 indices fit 16 bits
+
+struct GatherSchedule {
+    int steps = 0;                 // schedule length (max over the 32-column blocks)
+    int64_t count_pad = 0;         // count rounded up to 32 (row stride of ent)
+    int64_t neg_base = 0;          // count rounded up to 16: index of -x[0]
+    std::vector<uint16_t> ent;     // ent[s * count_pad + d]: buffer index
+    std::vector<uint8_t> steps32;  // steps the warp of 32-column block k runs
+};
+
+// False (with *err) when the table is not eligible: complex or several
+// classes, more than kSchedMaxCount states, or more than 255 steps.
+bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* err);
+
 // Build both layouts for one spin from a term list.  Returns ED_OK or an
 // error (bad site, table overflow, complex term in a real operator when
 // allow_complex is false).

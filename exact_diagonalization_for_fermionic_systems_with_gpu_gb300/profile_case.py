@@ -3,7 +3,9 @@
     python -m exact_diagonalization_for_fermionic_systems_with_gpu_gb300.profile_case \
         --case kagome12 --what lanczos --steps 20
 
---what lanczos : one fixed-step Lanczos solve (matvec + axpy kernels)
+--what lanczos : one fixed-step Lanczos solve, per-step kernels timed with events
+--what fused   : one fixed-step Lanczos solve in the persistent kernel, phases
+                 timed with device timestamps
 --what perform : --steps operator applies through the FP64 C-ABI path
 Cases: kagome12 (6+6, dim 853,776, L2-resident vectors), chain14 (7+7 open
 chain with disorder, dim 11,778,624, vectors larger than L2), lieb18
@@ -42,21 +44,30 @@ def build_case(name: str):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="kagome12")
-    ap.add_argument("--what", default="lanczos", choices=["lanczos", "perform"])
+    ap.add_argument("--what", default="lanczos", choices=["lanczos", "fused", "perform"])
     ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--ritz", default="none", choices=["none", "stored"],
+                    help="stored: keep the Krylov basis and form the Ritz vector, as the bench does")
     args = ap.parse_args()
     import torch
     op = build_case(args.case)
     lib = _capi.load()
     t0 = time.perf_counter()
-    if args.what == "lanczos":
+    if args.what in ("lanczos", "fused"):
+        ritz = _capi.ED_RITZ_STORED if args.ritz == "stored" else _capi.ED_RITZ_NONE
         cfg = _capi.ed_lanczos_cfg(max_steps=args.steps, mode=_capi.ED_LANCZOS_FIXED, reorth=0,
-                                   ritz=_capi.ED_RITZ_NONE, start=_capi.ED_START_RANDOM, profile=1, seed=0)
+                                   ritz=ritz, start=_capi.ED_START_RANDOM,
+                                   profile=1 if args.what == "lanczos" else 2, seed=0)
         res = _capi.ed_lanczos_result()
-        _capi.check(lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0, None, 0, None, None, C.byref(res), None),
-                    "ed_lanczos_run")
-        print(f"E0 {res.e0:.12f} steps {res.steps} matvec {res.matvec_ms / res.n_matvec * 1e3:.1f} us "
-              f"axpy {res.axpy_ms / res.n_matvec * 1e3:.1f} us")
+        evec = np.empty(op.rows() * (2 if op.is_complex else 1))
+        _capi.check(lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0,
+                                       C.c_void_p(evec.ctypes.data) if args.ritz == "stored" else None, 0,
+                                       None, None, C.byref(res), None), "ed_lanczos_run")
+        n = max(res.n_matvec, 1)
+        print(f"E0 {res.e0:.12f} steps {res.steps} matvec {res.matvec_ms / n * 1e3:.1f} us "
+              f"axpy {res.axpy_ms / n * 1e3:.1f} us reduce {res.reduce_ms / n * 1e3:.1f} us "
+              f"(barrier wait {res.barrier_ms / n * 1e3:.1f}, scalars {res.scalar_ms / n * 1e3:.1f}) "
+              f"launches {res.launches}" + (f" persistent launch {res.fused_ms:.3f} ms" if res.fused_ms else ""))
     else:
         dt = torch.complex128 if op.is_complex else torch.float64
         x = torch.empty(op.rows(), dtype=torch.float64 if not op.is_complex else torch.float64,

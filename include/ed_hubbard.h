@@ -174,9 +174,11 @@ typedef struct {
     int32_t ritz;          /* ED_RITZ_* */
     int32_t start;         /* ED_START_RANDOM (counter-based, seed below) |
                               ED_START_USER (start vector given) */
-    int32_t profile;       /* 1 = time every matvec / axpy launch with CUDA
-                              events on the launching stream (result fields
-                              matvec_ms, axpy_ms) */
+    int32_t profile;       /* 1 = per-step kernels, every matvec / axpy launch
+                              timed with CUDA events on the launching stream
+                              (result fields matvec_ms, axpy_ms);
+                              2 = persistent kernel with device timestamps
+                              of its phases (matvec_ms, axpy_ms, reduce_ms) */
     uint64_t seed;         /* seed of the uniform(-1,1) start vector */
 } ed_lanczos_cfg;
 
@@ -188,10 +190,17 @@ typedef struct {
     int32_t min_bits;      /* fewest significant bits any Lanczos vector kept */
     double residual;       /* |beta_{n} z_{n-1}| of the lowest Ritz pair */
     int64_t launches;      /* kernels this call launched */
-    double matvec_ms;      /* profile: summed device time of the matvec launches */
-    double axpy_ms;        /* profile: summed device time of the axpy launches */
-    int32_t n_matvec;      /* matvec launches */
+    double matvec_ms;      /* profile: summed device time of the matvecs */
+    double axpy_ms;        /* profile: summed device time of the axpys */
+    int32_t n_matvec;      /* matvecs (Lanczos steps run) */
     int32_t pad_;
+    double reduce_ms;      /* profile 2: time between the phases (block sums,
+                              grid barriers, scalar updates) ... */
+    double barrier_ms;     /* ... of which waiting at the grid barriers */
+    double scalar_ms;      /* ... of which reading the grid totals and updating
+                              the Lanczos scalars */
+    double fused_ms;       /* profile 2: CUDA-event time of the persistent
+                              kernel launches */
 } ed_lanczos_result;
 
 /* Run Lanczos on op.  start: ED_START_USER start vector (rows doubles, mem

@@ -245,10 +245,23 @@ void orc_matvec_z(const orc_tbq* up, const orc_tbq* dn, double U, uint64_t mask,
 
 /* ------------------------------------------------------- vector algebra -- */
 
+/* Fixed chunks summed in order: the same result for any thread count (an
+ * OpenMP reduction combines per-thread sums in an unspecified order, which
+ * moves the last bits of a 200-step Lanczos from run to run). */
 static double dot(const double* a, const double* b, int64_t n) {
+    enum { kChunks = 256 };
+    double part[kChunks];
+    const int64_t chunk = (n + kChunks - 1) / kChunks;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < kChunks; ++k) {
+        const int64_t lo = (int64_t)k * chunk;
+        const int64_t hi = lo + chunk < n ? lo + chunk : n;
+        double s = 0.0;
+        for (int64_t i = lo; i < hi; ++i) s += a[i] * b[i];
+        part[k] = s;
+    }
     double s = 0.0;
-#pragma omp parallel for reduction(+ : s) schedule(static)
-    for (int64_t i = 0; i < n; ++i) s += a[i] * b[i];
+    for (int k = 0; k < kChunks; ++k) s += part[k];
     return s;
 }
 

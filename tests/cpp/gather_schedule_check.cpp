@@ -1,0 +1,118 @@
+// Host-only check of the down-term gather schedule (build_gather_schedule):
+// for spin tables of several lattices, every entry of every row appears in
+// the schedule exactly once (as an index of +x or -x, the rest of the steps
+// reading zeros), no step of a 16-column group touches a bank pair twice, and
+// the per-block step counts cover the entries.  Prints one line
+// per case: "<name> count <n> max_len <L> steps <S> ok".
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "ed_tables.hpp"
+
+using namespace ed;
+
+static int check(const char* name, int n, int q, const std::vector<ed_term>& terms) {
+    SpinBasis b;
+    b.build(n, q);
+    SpinTable t;
+    std::string err;
+    if (build_spin(b, terms.data(), (int)terms.size(), false, &t, nullptr, &err) != ED_OK) {
+        std::printf("%s build_spin failed: %s\n", name, err.c_str());
+        return 1;
+    }
+    GatherSchedule g;
+    if (!build_gather_schedule(t, &g, &err)) {
+        std::printf("%s schedule failed: %s\n", name, err.c_str());
+        return 1;
+    }
+    const int64_t cnt = t.count, cp = g.count_pad, nb = g.neg_base, zb = 2 * g.neg_base;
+    if (cp % 32 != 0 || cp < cnt || nb % 16 != 0 || nb < cnt || (int64_t)g.steps32.size() != cp / 32) {
+        std::printf("%s bad padding\n", name);
+        return 1;
+    }
+    for (int64_t d = 0; d < cp; ++d) {
+        std::map<int64_t, int> want, got;  // +-(col + 1)
+        if (d < cnt)
+            for (int k = 0; k < t.len[d]; ++k) {
+                const uint32_t e = t.ent[(size_t)k * cnt + d];
+                const int64_t c = (int64_t)(e & kColMask) + 1;
+                ++want[(e & kSignBit) ? -c : c];
+            }
+        const int nst = g.steps32[d / 32];
+        for (int s = 0; s < nst; ++s) {
+            const int64_t w = g.ent[(size_t)s * cp + d];
+            if (w >= zb + 16 || (w >= cnt && w < nb) || (w >= nb + cnt && w < zb)) {
+                std::printf("%s index out of the buffer (d %lld s %d)\n", name, (long long)d, s);
+                return 1;
+            }
+            if (w >= zb) continue;
+            ++got[w < nb ? w + 1 : -(w - nb + 1)];
+        }
+        if (want != got) {
+            std::printf("%s row %lld: schedule entries differ from the table\n", name, (long long)d);
+            return 1;
+        }
+    }
+    for (int64_t g0 = 0; g0 < cp; g0 += 16) {
+        const int nst = g.steps32[g0 / 32];
+        for (int s = 0; s < nst; ++s) {
+            int seen = 0;
+            for (int l = 0; l < 16; ++l) {
+                const int bit = 1 << (g.ent[(size_t)s * cp + g0 + l] % 16);
+                if (seen & bit) {
+                    std::printf("%s bank conflict at group %lld step %d\n", name, (long long)g0, s);
+                    return 1;
+                }
+                seen |= bit;
+            }
+        }
+    }
+    std::printf("%s count %lld max_len %d steps %d ok\n", name, (long long)cnt, t.max_len, g.steps);
+    return 0;
+}
+
+static std::vector<ed_term> bonds(const std::vector<std::pair<int, int>>& bs, double t) {
+    std::vector<ed_term> v;
+    for (auto& p : bs) v.push_back({ED_TERM_HOP, p.first, p.second, 0, t, 0.0});
+    return v;
+}
+
+int main() {
+    int fails = 0;
+    {
+        std::vector<std::pair<int, int>> bs;
+        for (int i = 0; i < 14; ++i) bs.push_back({i, (i + 1) % 14});
+        fails += check("chain14_q7", 14, 7, bonds(bs, -1.0));
+    }
+    {
+        // 12 sites, every site on four bonds (ring plus second neighbours)
+        std::vector<std::pair<int, int>> bs;
+        for (int i = 0; i < 12; ++i) {
+            bs.push_back({i, (i + 1) % 12});
+            bs.push_back({i, (i + 2) % 12});
+        }
+        fails += check("ring12_nnn_q6", 12, 6, bonds(bs, -1.0));
+        fails += check("ring12_nnn_q5", 12, 5, bonds(bs, 1.0));
+    }
+    {
+        // 16 sites, random bonds (fixed LCG), 6 particles
+        std::vector<std::pair<int, int>> bs;
+        uint64_t x = 12345;
+        for (int k = 0; k < 40; ++k) {
+            x = x * 6364136223846793005ULL + 1442695040888963407ULL;
+            const int i = (int)((x >> 33) % 16);
+            x = x * 6364136223846793005ULL + 1442695040888963407ULL;
+            const int j = (int)((x >> 33) % 16);
+            if (i != j) bs.push_back({i, j});
+        }
+        fails += check("random16_q6", 16, 6, bonds(bs, 0.5));
+    }
+    {
+        std::vector<std::pair<int, int>> bs = {{0, 1}};
+        fails += check("dimer_q1", 2, 1, bonds(bs, -1.0));
+    }
+    return fails ? 1 : 0;
+}

@@ -33,3 +33,20 @@ def test_cpp_header_lanczos_on_gpu(tmp_path, edlib, golden_energies):
     e0 = float(out.split("E0 ")[1].split()[0])
     g = golden_energies["chain8_pbc_q44_U4"]["E0"]
     assert abs(e0 - g) < 1e-10 * abs(g)
+
+
+def test_gather_schedule_host_check(tmp_path):
+    """The down-term gather schedule (host code, no GPU): every table entry
+    scheduled exactly once, no bank pair used twice by one half warp in one
+    step, step counts covering the entries."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    csrc = ROOT / "exact_diagonalization_for_fermionic_systems_with_gpu_gb300/csrc"
+    exe = tmp_path / "gather_schedule_check"
+    subprocess.run([cxx, "-std=c++17", "-O2", "-I", str(csrc), str(ROOT / "tests/cpp/gather_schedule_check.cpp"),
+                    str(csrc / "ed_tables.cpp"), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stdout + out.stderr
+    lines = out.stdout.strip().splitlines()
+    assert len(lines) == 5 and all(l.endswith(" ok") for l in lines)

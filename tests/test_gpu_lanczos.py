@@ -162,3 +162,57 @@ def test_lanczos_profile_and_launch_count(ed):
                               C.byref(res), None) == 0
     assert res.n_matvec == 50 and res.matvec_ms > 0 and res.axpy_ms > 0
     assert res.launches == 3 + 2 * 50 + 12 + 2
+
+
+def fused_cases():
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    eps12 = list(philox_uniform(100, 12, 6.0))
+    return [
+        ("kagome12_66_U8_fixed300_ritz", 12, 6, 6, L.kagome12(), L.kagome12(), 8.0, "fixed", 300, "stored"),
+        ("kagome12_66_U8_reference", 12, 6, 6, L.kagome12(), L.kagome12(), 8.0, "reference", 1000, "stored"),
+        ("kagome12_54_flux_complex", 12, 5, 4, L.kagome12(flux=0.3), L.kagome12(flux=0.3), 4.0, "fixed", 80,
+         "stored"),
+        ("kagome12_55_Kx_2classes", 12, 5, 5, L.kagome12_kinetic_x(), L.kagome12_kinetic_x(), 1.0, "fixed", 60,
+         "none"),
+        ("chain12_open_W6_66_three_slots", 12, 6, 6, L.chain(12, periodic=False, eps=eps12),
+         L.chain(12, periodic=False, eps=eps12), 1.0, "fixed", 120, "none"),
+        ("chain2_11_breakdown", 2, 1, 1, L.chain(2, periodic=False), L.chain(2, periodic=False), 3.0, "fixed", 12,
+         "stored"),
+    ]
+
+
+@pytest.mark.parametrize("case", fused_cases(), ids=lambda c: c[0])
+def test_persistent_kernel_matches_per_step_kernels(ed, monkeypatch, case):
+    """The persistent Lanczos kernel (all steps in one cooperative launch)
+    and the per-step kernels (a matvec and an axpy launch per step) perform
+    the same exact integer reductions and the same scalar arithmetic: alpha,
+    beta, E0 and the Ritz vector agree bit for bit, also past a breakdown and
+    with the three-slot (no stored basis) recurrence."""
+    name, N, qu, qd, tu, td, U, mode, steps, ritz = case
+    op = op_for(ed, N, qu, qd, tu, td, U)
+    runs = {}
+    for fused in ("1", "0"):
+        monkeypatch.setenv("ED_LZ_FUSED", fused)
+        lz = ed.Lanczos()
+        e0, v = lz.eigen(op, max_steps=steps, mode=mode, ritz=ritz, seed=3)
+        runs[fused] = (lz.a, lz.b, e0, v, lz.result.steps, lz.result.launches)
+    monkeypatch.delenv("ED_LZ_FUSED")
+    f, p = runs["1"], runs["0"]
+    assert f[0] == p[0] and f[1] == p[1] and f[2] == p[2] and f[4] == p[4]
+    if ritz != "none":
+        assert np.array_equal(f[3], p[3])
+    assert f[5] < p[5]  # the persistent path launched fewer kernels
+
+
+def test_persistent_kernel_launch_count(ed):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, _capi
+    import ctypes as C
+    op = op_for(ed, 12, 6, 6, L.kagome12(), L.kagome12(), 8.0)
+    lib = _capi.load()
+    cfg = _capi.ed_lanczos_cfg(max_steps=50, mode=1, reorth=0, ritz=1, start=0, profile=0, seed=0)
+    res = _capi.ed_lanczos_result()
+    v = np.empty(op.rows())
+    assert lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0, C.c_void_p(v.ctypes.data), 0, None, None,
+                              C.byref(res), None) == 0
+    # random, emax, start; one persistent launch; tridiagonal solve; Ritz
+    assert res.launches == 3 + 1 + 12 + 2

@@ -32,9 +32,9 @@ def real_cases():
         ("kagome12_66_U8", 12, 6, 6, L.kagome12(), L.kagome12(), 8.0, None),
         ("kagome12_54_Kx", 12, 5, 4, L.kagome12_kinetic_x(), L.kagome12_kinetic_x(), 0.0, None),
         ("kagome12_54_Jx", 12, 5, 4, L.kagome12_current_x(), L.kagome12_current_x(), 0.0, None),
-        ("chain12_open_W6_66", 12, 6, 6, L.chain(12, False, eps=eps12), L.chain(12, False, eps=eps12), 1.0, None),
-        ("chain12_open_W6_75", 12, 7, 5, L.chain(12, False, eps=eps12), L.chain(12, False, eps=eps12), 1.0, None),
-        ("chain12_open_W6_84", 12, 8, 4, L.chain(12, False, eps=eps12), L.chain(12, False, eps=eps12), 1.0, None),
+        ("chain12_open_W6_66", 12, 6, 6, L.chain(12, periodic=False, eps=eps12), L.chain(12, periodic=False, eps=eps12), 1.0, None),
+        ("chain12_open_W6_75", 12, 7, 5, L.chain(12, periodic=False, eps=eps12), L.chain(12, periodic=False, eps=eps12), 1.0, None),
+        ("chain12_open_W6_84", 12, 8, 4, L.chain(12, periodic=False, eps=eps12), L.chain(12, periodic=False, eps=eps12), 1.0, None),
         ("lieb12_66_U4", 12, 6, 6, L.lieb12(), L.lieb12(), 4.0, None),
         ("square3x4_43_U3", 12, 4, 3, L.squared_3by4(), L.squared_3by4(), 3.0, None),
         ("atomic8_32_U3", 8, 3, 2, [("N", i, 0, eps8[i], 0.0) for i in range(8)],
@@ -158,32 +158,44 @@ def test_device_random_vector_matches_host(ed, edlib):
     assert np.array_equal(t.cpu().numpy(), philox_uniform(42, n))
 
 
-def tma_cases():
+def kernel_cases():
     from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
     eps12 = list(philox_uniform(100, 12, 6.0))
     return [
         ("kagome12_66_U8", 12, 6, 6, L.kagome12(), L.kagome12(), 8.0),
+        ("kagome12_66_U0", 12, 6, 6, L.kagome12(), L.kagome12(), 0.0),
         ("kagome12_54_flux", 12, 5, 4, L.kagome12(flux=0.3), L.kagome12(flux=0.3), 4.0),
         ("kagome12_55_Kx_2classes", 12, 5, 5, L.kagome12_kinetic_x(), L.kagome12_kinetic_x(), 1.0),
-        ("chain12_open_W6_75", 12, 7, 5, L.chain(12, False, eps=eps12), L.chain(12, False, eps=eps12), 1.0),
+        ("chain12_open_W6_75", 12, 7, 5, L.chain(12, periodic=False, eps=eps12), L.chain(12, periodic=False, eps=eps12), 1.0),
         ("chain8_35", 8, 3, 5, L.chain(8), L.chain(8), 2.0),
+        ("chain8_04_no_up_hops", 8, 0, 4, L.chain(8), L.chain(8), 2.0),
+        ("chain2_11", 2, 1, 1, L.chain(2, periodic=False), L.chain(2, periodic=False), 3.0),
+        ("chain14_75", 14, 7, 5, L.chain(14), L.chain(14), 4.0),
     ]
 
 
-@pytest.mark.parametrize("case", tma_cases(), ids=lambda c: c[0])
-def test_shared_memory_kernel_matches_generic_kernel(ed, monkeypatch, case):
-    """The TMA/shared-memory matvec and the generic kernel compute the same
-    exact integer sums: their outputs and Lanczos coefficients agree bit for bit."""
+@pytest.mark.parametrize("case", kernel_cases(), ids=lambda c: c[0])
+def test_matvec_kernels_agree_bit_for_bit(ed, monkeypatch, case):
+    """The row-staged TMA kernel and the generic kernel compute the same exact
+    integer sums: their outputs and Lanczos coefficients agree bit for bit
+    (operators whose down table does not fit shared memory take the generic
+    kernel either way)."""
     name, N, qu, qd, ut, dt, U = case
-    op_tma = make_op(ed, N, qu, qd, ut, dt, U)
-    monkeypatch.setenv("ED_NO_TMA", "1")
-    op_gen = make_op(ed, N, qu, qd, ut, dt, U)
-    monkeypatch.delenv("ED_NO_TMA")
+    ops = {}
+    for kind in ("", "generic"):
+        if kind:
+            monkeypatch.setenv("ED_MATVEC", kind)
+        ops[kind or "auto"] = make_op(ed, N, qu, qd, ut, dt, U)
+        monkeypatch.delenv("ED_MATVEC", raising=False)
     rng = np.random.default_rng(11)
-    n = op_tma.rows()
-    x = rng.standard_normal(n) + (1j * rng.standard_normal(n) if op_tma.is_complex else 0)
-    assert np.array_equal(op_tma.matvec(x), op_gen.matvec(x))
-    l1, l2 = ed.Lanczos(), ed.Lanczos()
-    e1, _ = l1.eigen(op_tma, max_steps=30, mode="fixed", ritz="none", seed=4)
-    e2, _ = l2.eigen(op_gen, max_steps=30, mode="fixed", ritz="none", seed=4)
-    assert l1.a == l2.a and l1.b == l2.b and e1 == e2
+    n = ops["auto"].rows()
+    cplx = ops["auto"].is_complex
+    x = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
+    ys = {k: op.matvec(x) for k, op in ops.items()}
+    assert np.array_equal(ys["auto"], ys["generic"])
+    runs = {}
+    for k, op in ops.items():
+        lz = ed.Lanczos()
+        e, _ = lz.eigen(op, max_steps=min(30, n), mode="fixed", ritz="none", seed=4)
+        runs[k] = (lz.a, lz.b, e)
+    assert runs["auto"] == runs["generic"]

@@ -107,11 +107,15 @@ def test_drude_kubo_matches_oracle(ed, orc):
     assert abs(kin - kinetic) < 1e-12 * abs(kinetic)
     assert abs(vert - vertex) < 1e-8 * abs(vertex)
     assert abs(D - Dref) < 1e-8 * max(abs(Dref), 1e-3)
-    # pointwise sigma(w) near its 1/delta-high peaks follows the exact pole
+    # sigma(w) itself near its 1/delta-high peaks follows the exact pole
     # positions of a 200-step Lanczos without reorthogonalisation, which
-    # (ghost copies included) depend on rounding; the integrated weight above
-    # is the quantity held to 1e-8
-    assert np.max(np.abs(sigma - sig)) < 1e-3 * np.max(np.abs(sig))
+    # (ghost copies included) move with last-bit rounding, and its running
+    # integral (the spectral weight below w) moves by the weight of a pole
+    # times its shift over delta near such a pole; held to 2e-3 of the total
+    # weight at every w (observed: up to 3e-4 near the sharpest poles), while
+    # the total (the Drude weight above) is held to 1e-8
+    run = np.cumsum(sigma - sig) * 0.004
+    assert np.max(np.abs(run)) < 2e-3 * np.sum(np.abs(sig)) * 0.004
 
 
 @pytest.mark.parametrize("flux", [0.3, 1.1])
