@@ -11,6 +11,7 @@
 
 #include "../../include/ed_hubbard.h"
 #include "ed_device.cuh"
+#include "ed_tridiag.hpp"
 #include "ed_internal.hpp"
 
 namespace ed {
@@ -19,9 +20,6 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
                       cudaStream_t s);
 void lanczos_free_ws(void* p);
 cudaError_t launch_random(double* f, int64_t n, uint64_t seed, cudaStream_t s);
-size_t tridiag_scratch_bytes(int n);
-cudaError_t launch_tridiag_lowest(int n, const double* alpha, const double* off, double* out, void* scratch,
-                                  cudaStream_t s);
 
 // ------------------------------------------------------- device rank/unrank --
 __global__ void k_unrank(const int64_t* __restrict__ ranks, int64_t count, uint64_t* __restrict__ words, int n_sites,
@@ -466,28 +464,8 @@ ed_status ed_random_vector_device(int64_t n, uint64_t seed, double* out_device, 
 
 ed_status ed_tridiag_lowest(int n, const double* alpha, const double* offdiag, double* e0, double* z) {
     if (n < 1 || !alpha || (n > 1 && !offdiag) || !e0) return ED_ERR_ARG;
-    double *d_a = nullptr, *d_o = nullptr, *d_out = nullptr;
-    void* scratch = nullptr;
-    ed_status st = ED_OK;
-    std::vector<double> out(n + 1);
-    if (cudaMalloc(&d_a, sizeof(double) * n) != cudaSuccess || cudaMalloc(&d_o, sizeof(double) * n) != cudaSuccess ||
-        cudaMalloc(&d_out, sizeof(double) * (n + 1)) != cudaSuccess ||
-        cudaMalloc(&scratch, ed::tridiag_scratch_bytes(n)) != cudaSuccess) {
-        st = ED_ERR_ALLOC;
-    } else {
-        cudaMemcpy(d_a, alpha, sizeof(double) * n, cudaMemcpyHostToDevice);
-        cudaMemset(d_o, 0, sizeof(double) * n);
-        if (n > 1) cudaMemcpy(d_o, offdiag, sizeof(double) * (n - 1), cudaMemcpyHostToDevice);
-        if (ed::launch_tridiag_lowest(n, d_a, d_o, d_out, scratch, 0) != cudaSuccess ||
-            cudaMemcpy(out.data(), d_out, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost) != cudaSuccess)
-            st = ED_ERR_CUDA;
-    }
-    cudaFree(d_a); cudaFree(d_o); cudaFree(d_out); cudaFree(scratch);
-    if (st == ED_OK) {
-        *e0 = out[0];
-        if (z) std::memcpy(z, out.data() + 1, sizeof(double) * n);
-    }
-    return st;
+    *e0 = ed::tridiag_lowest_host(n, alpha, offdiag, z);
+    return ED_OK;
 }
 
 }  // extern "C"

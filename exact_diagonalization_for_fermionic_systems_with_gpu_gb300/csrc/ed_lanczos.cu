@@ -19,14 +19,12 @@
 #include "ed_internal.hpp"
 #include "ed_lanczos.hpp"
 #include "ed_lanczos_dev.cuh"
+#include "ed_tridiag.hpp"
 
 namespace ed {
 using namespace dev;
 
-size_t tridiag_scratch_bytes(int n);
 cudaError_t launch_lz_fused(const ed_op* op, const LzFusedArgs& f, cudaStream_t s);
-cudaError_t launch_tridiag_lowest(int n, const double* alpha, const double* off, double* out, void* scratch,
-                                  cudaStream_t s);
 
 constexpr int kLzThreads = 256;
 
@@ -189,13 +187,46 @@ __global__ void __launch_bounds__(kLzThreads) k_lz_reorth(int64_t* __restrict__ 
 }
 
 // evec = sum_k (rt_k q_k >> rs_k) * 2^-F as FP64, plus |evec|^2 partials.
+// A thread forms two adjacent elements from 16-byte loads of every slot
+// (slots are 256-byte aligned), four slots per iteration so that eight loads
+// are in flight; the basis is read once, at HBM rate.
 __global__ void __launch_bounds__(kLzThreads) k_ritz(const int64_t* __restrict__ basis, int64_t n, int64_t stride,
                                                      int nk, const int64_t* __restrict__ rt,
                                                      const int* __restrict__ rs, int F, double* __restrict__ out,
                                                      double* __restrict__ part, unsigned int* counter,
                                                      double* inv_norm) {
     double ss = 0.0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t npair = n >> 1;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < npair; i += (int64_t)gridDim.x * blockDim.x) {
+        const longlong2* q = reinterpret_cast<const longlong2*>(basis) + i;
+        const int64_t s2 = stride >> 1;
+        i128 a0 = 0, a1 = 0;
+        int k = 0;
+        for (; k + 4 <= nk; k += 4) {
+            const longlong2 v0 = __ldg(q + (k + 0) * s2), v1 = __ldg(q + (k + 1) * s2);
+            const longlong2 v2 = __ldg(q + (k + 2) * s2), v3 = __ldg(q + (k + 3) * s2);
+            const int64_t c0 = __ldg(rt + k), c1 = __ldg(rt + k + 1), c2 = __ldg(rt + k + 2), c3 = __ldg(rt + k + 3);
+            const int r0 = __ldg(rs + k), r1 = __ldg(rs + k + 1), r2 = __ldg(rs + k + 2), r3 = __ldg(rs + k + 3);
+            a0 += (mul_wide(c0, v0.x) >> r0) + (mul_wide(c1, v1.x) >> r1) + (mul_wide(c2, v2.x) >> r2) +
+                  (mul_wide(c3, v3.x) >> r3);
+            a1 += (mul_wide(c0, v0.y) >> r0) + (mul_wide(c1, v1.y) >> r1) + (mul_wide(c2, v2.y) >> r2) +
+                  (mul_wide(c3, v3.y) >> r3);
+        }
+        for (; k < nk; ++k) {
+            const longlong2 v = __ldg(q + k * s2);
+            const int64_t c = __ldg(rt + k);
+            const int r = __ldg(rs + k);
+            a0 += mul_wide(c, v.x) >> r;
+            a1 += mul_wide(c, v.y) >> r;
+        }
+        const double x0 = i128_to_f64(a0, -F), x1 = i128_to_f64(a1, -F);
+        out[2 * i] = x0;
+        out[2 * i + 1] = x1;
+        ss = fma(x0, x0, ss);
+        ss = fma(x1, x1, ss);
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const int64_t i = n - 1;
         i128 acc = 0;
         for (int k = 0; k < nk; ++k) acc += mul_wide(rt[k], basis[(int64_t)k * stride + i]) >> rs[k];
         const double v = i128_to_f64(acc, -F);
@@ -246,9 +277,6 @@ struct Workspace {
     LzState h;              // host mirror (pointers)
     int* emax = nullptr;
     int* flag = nullptr;
-    void* tri_scratch = nullptr;
-    double* tri_out = nullptr;
-    double* offd = nullptr;
     uint64_t* dot_lo = nullptr;
     uint64_t* dot_hi = nullptr;
     int64_t* coef_rt = nullptr;
@@ -275,7 +303,7 @@ void free_ws(Workspace* w) {
     cudaFree(w->basis); cudaFree(w->u); cudaFree(w->fbuf); cudaFree(w->lz);
     cudaFree(w->h.e); cudaFree(w->h.m); cudaFree(w->h.beta); cudaFree(w->h.alpha);
     cudaFree(w->h.part_lo); cudaFree(w->h.part_hi); cudaFree(w->h.part_max); cudaFree(w->h.counter);
-    cudaFree(w->emax); cudaFree(w->flag); cudaFree(w->tri_scratch); cudaFree(w->tri_out); cudaFree(w->offd);
+    cudaFree(w->emax); cudaFree(w->flag); 
     cudaFree(w->dot_lo); cudaFree(w->dot_hi); cudaFree(w->coef_rt); cudaFree(w->coef_rs);
     cudaFree(w->ritz_part); cudaFree(w->ritz_ctr); cudaFree(w->inv_norm); cudaFree(w->gbar);
     cudaFree(w->stamps);
@@ -311,9 +339,6 @@ ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_s
     LZ_CK(cudaMemset(w->h.counter, 0, sizeof(unsigned int) * 4));
     LZ_CK(cudaMalloc(&w->emax, sizeof(int)));
     LZ_CK(cudaMalloc(&w->flag, sizeof(int)));
-    LZ_CK(cudaMalloc(&w->tri_scratch, tridiag_scratch_bytes((int)ns)));
-    LZ_CK(cudaMalloc(&w->tri_out, sizeof(double) * (ns + 1)));
-    LZ_CK(cudaMalloc(&w->offd, sizeof(double) * ns));
     LZ_CK(cudaMalloc(&w->dot_lo, sizeof(uint64_t) * ns * kDotChunks));
     LZ_CK(cudaMalloc(&w->dot_hi, sizeof(uint64_t) * ns * kDotChunks));
     LZ_CK(cudaMalloc(&w->coef_rt, sizeof(int64_t) * ns));
@@ -523,11 +548,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             if (status_dev != 0) { n = nn; break; }
             double anorm = std::fabs(ha[0] + hb[1]);
             for (int k = 1; k < nn; ++k) anorm = std::max(anorm, hb[k] + std::fabs(ha[k] + hb[k + 1]));
-            LZ_CK(cudaMemcpyAsync(w->offd, H.beta + 1, sizeof(double) * nn, cudaMemcpyDeviceToDevice, s));
-            LZ_CK(launch_tridiag_lowest(nn, H.alpha, w->offd, w->tri_out, w->tri_scratch, s));
-            launches += 12;
-            LZ_CK(cudaMemcpyAsync(tri.data(), w->tri_out, sizeof(double) * (nn + 1), cudaMemcpyDeviceToHost, s));
-            LZ_CK(cudaStreamSynchronize(s));
+            tri[0] = tridiag_lowest_host(nn, ha.data(), hb.data() + 1, tri.data() + 1);
             e0 = tri[0];
             if (std::fabs(hb[nn] * tri[nn]) < tolconv * anorm && std::fabs(tri[1]) > tolconv * anorm) {
                 converged = true;
@@ -559,11 +580,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     } else if (status != 0) {
         return ED_ERR_NONFINITE;
     }
-    LZ_CK(cudaMemcpyAsync(w->offd, H.beta + 1, sizeof(double) * n, cudaMemcpyDeviceToDevice, s));
-    LZ_CK(launch_tridiag_lowest(n, H.alpha, w->offd, w->tri_out, w->tri_scratch, s));
-    launches += 12;
-    LZ_CK(cudaMemcpyAsync(tri.data(), w->tri_out, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost, s));
-    LZ_CK(cudaStreamSynchronize(s));
+    tri[0] = tridiag_lowest_host(n, ha.data(), hb.data() + 1, tri.data() + 1);
     e0 = tri[0];
     resid = std::fabs(hb[n] * tri[n]);
 
@@ -582,7 +599,10 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
         double* out = evec_mem == ED_MEM_DEVICE ? evec : w->fbuf;
         const int g = lz_grid(DW);
-        k_ritz<<<g, kLzThreads, 0, s>>>(w->basis, DW, w->stride, n, w->coef_rt, w->coef_rs, F, out, w->ritz_part,
+        // one pair of elements per thread where the grid allows
+        int64_t gr = (DW / 2 + kLzThreads - 1) / kLzThreads;
+        gr = std::max<int64_t>(1, std::min<int64_t>(gr, kLzMaxPartials));
+        k_ritz<<<(int)gr, kLzThreads, 0, s>>>(w->basis, DW, w->stride, n, w->coef_rt, w->coef_rs, F, out, w->ritz_part,
                                         w->ritz_ctr, w->inv_norm);
         LZ_CK(cudaGetLastError());
         k_scale<<<g, kLzThreads, 0, s>>>(out, DW, w->inv_norm);

@@ -57,7 +57,8 @@ def random_vector(n: int, seed: int = 0) -> np.ndarray:
 
 
 def tridiag_lowest(alpha: Sequence[float], offdiag: Sequence[float]):
-    """Lowest eigenpair of a symmetric tridiagonal matrix, solved on the device."""
+    """Lowest eigenpair of a symmetric tridiagonal matrix (host solver of the
+    Lanczos T: Sturm bisection and inverse iteration)."""
     a = np.ascontiguousarray(alpha, dtype=np.float64)
     o = np.ascontiguousarray(offdiag, dtype=np.float64)
     n = a.size

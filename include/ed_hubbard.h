@@ -223,8 +223,10 @@ ed_status ed_random_vector_device(int64_t n, uint64_t seed, double* out_device, 
 ed_status ed_random_vector(int64_t n, uint64_t seed, double* out_host);
 
 /* Lowest eigenpair of the symmetric tridiagonal (alpha[0..n-1], off-diagonal
- * beta[0..n-2]) computed by the device solver: eigenvalue e0 and eigenvector
- * z (n doubles).  Host in/out; replaces LAPACKf77::dsted for the Lanczos T. */
+ * beta[0..n-2]): eigenvalue e0 (Sturm bisection to adjacent doubles) and unit
+ * eigenvector z (n doubles, inverse iteration, largest component positive;
+ * may be NULL).  Host in/out, computed on the host (T is a few hundred rows);
+ * replaces LAPACKf77::dsted for the Lanczos T. */
 ed_status ed_tridiag_lowest(int n, const double* alpha, const double* offdiag,
                             double* e0, double* z);
 

@@ -147,3 +147,20 @@ def test_lattice_tables():
     for i, j in zip(L.LIEB18_FIRST, L.LIEB18_SECOND):
         deg[i] += 1; deg[j] += 1
     assert sorted(set(deg)) == [2, 4]
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 17, 100, 301, 1000])
+def test_tridiagonal_lowest_vs_scipy(edlib, n):
+    """ed_tridiag_lowest (host bisection + inverse iteration, the Lanczos T
+    eigensolve) against scipy's LAPACK tridiagonal solver."""
+    import numpy as np
+    from scipy.linalg import eigh_tridiagonal
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300.hubbard import tridiag_lowest
+    rng = np.random.default_rng(n)
+    a = rng.normal(size=n) * 3
+    b = np.abs(rng.normal(size=max(n - 1, 0))) + 1e-3
+    lam, z = tridiag_lowest(a, b)
+    w, V = eigh_tridiagonal(a, b) if n > 1 else (a, np.ones((1, 1)))
+    assert abs(lam - w[0]) < 1e-12 * max(1.0, np.max(np.abs(w)))
+    assert abs(abs(z @ V[:, 0]) - 1.0) < 1e-9
+    assert np.max(np.abs(z)) == np.max(z)  # largest component positive

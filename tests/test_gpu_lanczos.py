@@ -128,18 +128,6 @@ def test_complex_peierls_lanczos(ed, orc):
     assert np.linalg.norm(H @ v - e0 * v) < 1e-6
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 17, 100, 301, 1000])
-def test_device_tridiagonal_vs_scipy(ed, n):
-    from scipy.linalg import eigh_tridiagonal
-    rng = np.random.default_rng(n)
-    a = rng.normal(size=n) * 3
-    b = np.abs(rng.normal(size=max(n - 1, 0))) + 1e-3
-    lam, z = ed.tridiag_lowest(a, b)
-    w, V = eigh_tridiagonal(a, b) if n > 1 else (a, np.ones((1, 1)))
-    assert abs(lam - w[0]) < 1e-12 * max(1.0, np.max(np.abs(w)))
-    assert abs(abs(z @ V[:, 0]) - 1.0) < 1e-9
-
-
 def test_start_vector_user_vs_random_same(ed):
     """ED_START_RANDOM(seed) is exactly the Philox vector a caller would pass."""
     from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
@@ -161,7 +149,7 @@ def test_lanczos_profile_and_launch_count(ed):
     assert lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0, C.c_void_p(v.ctypes.data), 0, None, None,
                               C.byref(res), None) == 0
     assert res.n_matvec == 50 and res.matvec_ms > 0 and res.axpy_ms > 0
-    assert res.launches == 3 + 2 * 50 + 12 + 2
+    assert res.launches == 3 + 2 * 50 + 2
 
 
 def fused_cases():
@@ -214,5 +202,6 @@ def test_persistent_kernel_launch_count(ed):
     v = np.empty(op.rows())
     assert lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0, C.c_void_p(v.ctypes.data), 0, None, None,
                               C.byref(res), None) == 0
-    # random, emax, start; one persistent launch; tridiagonal solve; Ritz
-    assert res.launches == 3 + 1 + 12 + 2
+    # random, emax, start; one persistent launch; Ritz sum and scale (the
+    # tridiagonal eigensolve runs on the host)
+    assert res.launches == 3 + 1 + 2
