@@ -53,7 +53,7 @@ class ed_lanczos_result(C.Structure):
                 ("min_bits", C.c_int32), ("residual", C.c_double), ("launches", C.c_int64),
                 ("matvec_ms", C.c_double), ("axpy_ms", C.c_double), ("n_matvec", C.c_int32), ("pad_", C.c_int32),
                 ("reduce_ms", C.c_double), ("barrier_ms", C.c_double), ("scalar_ms", C.c_double),
-                ("fused_ms", C.c_double)]
+                ("fused_ms", C.c_double), ("rows_spread_ms", C.c_double), ("axpy_spread_ms", C.c_double)]
 
 
 class ed_kubo_cfg(C.Structure):

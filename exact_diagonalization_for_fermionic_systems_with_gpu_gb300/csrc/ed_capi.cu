@@ -362,7 +362,20 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
     // generic kernel (tests compare the two)
     const char* pick = std::getenv("ED_MATVEC");
     if (!(pick && std::string(pick) == "generic")) op->tma_smem = ed::tma_plan(op, &a);
-    if (op->tma_smem > 0) op->tma_grid = ed::tma_grid(op);
+    if (op->tma_smem > 0) {
+        op->tma_grid = ed::tma_grid(op);
+        std::vector<uint32_t> rs, rl, rq;
+        ed::row_plan(op->tup, op->tma_grid, &rs, &rl, &rq);
+        if (upload(&op->d_rowStart, rs.data(), rs.size()) != cudaSuccess ||
+            upload(&op->d_rowList, rl.data(), rl.size()) != cudaSuccess ||
+            upload(&op->d_rowQueue, rq.data(), rq.size()) != cudaSuccess) {
+            ed_op_destroy(op);
+            return ED_ERR_ALLOC;
+        }
+        op->mv.rowStart = op->d_rowStart;
+        op->mv.rowList = op->d_rowList;
+        op->mv.rowQueue = op->d_rowQueue;
+    }
     *out = op;
     return ED_OK;
 }
@@ -375,7 +388,7 @@ ed_status ed_op_destroy(ed_op* op) {
     cudaFree(op->d_upEnt); cudaFree(op->d_dnEnt); cudaFree(op->d_upLen); cudaFree(op->d_dnLen);
     cudaFree(op->d_upNpos); cudaFree(op->d_dnNpos);
     cudaFree(op->d_upPtr); cudaFree(op->d_upEntC); cudaFree(op->d_dnPtr); cudaFree(op->d_dnEntC);
-    cudaFree(op->d_dnSched); cudaFree(op->d_dnSteps);
+    cudaFree(op->d_dnSched); cudaFree(op->d_dnSteps); cudaFree(op->d_rowStart); cudaFree(op->d_rowList); cudaFree(op->d_rowQueue);
     cudaFree(op->d_err);
     cudaFree(op->d_dUPq); cudaFree(op->d_dDNq); cudaFree(op->d_stUP); cudaFree(op->d_stDN);
     cudaFree(op->d_xq); cudaFree(op->d_emax); cudaFree(op->d_flag); cudaFree(op->d_io);

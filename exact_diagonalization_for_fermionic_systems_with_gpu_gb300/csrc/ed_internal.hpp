@@ -48,6 +48,11 @@ struct MvArgs {
     int schedSteps;
     int dimDNp;
     int schedNeg;         // index of -x[0] in the row buffer; zeros at 2 * schedNeg
+    // rows of each CTA of the shared-memory kernels (balanced on the host):
+    // CTA b computes rows rowList[rowStart[b] .. rowStart[b+1])
+    const uint32_t* rowStart;
+    const uint32_t* rowList;
+    const uint32_t* rowQueue;  // all rows in decreasing order of cost (dynamic distribution)
     int* err;             // device word set when a bounded wait gives up
     // shared-memory plan of the TMA kernel (byte offsets)
     int sm_row0, sm_row1, sm_dnptr, sm_dnent, sm_dnnpos, sm_ddnq, sm_stdn;
@@ -84,6 +89,7 @@ struct ed_op {
     uint32_t *d_upPtr = nullptr, *d_upEntC = nullptr, *d_dnPtr = nullptr, *d_dnEntC = nullptr;
     uint16_t* d_dnSched = nullptr;
     uint8_t* d_dnSteps = nullptr;
+    uint32_t *d_rowStart = nullptr, *d_rowList = nullptr, *d_rowQueue = nullptr;
     int* d_err = nullptr;
     int64_t *d_dUPq = nullptr, *d_dDNq = nullptr;
     uint64_t *d_stUP = nullptr, *d_stDN = nullptr;
@@ -120,6 +126,11 @@ int matvec_grid(const ed_op* op);
 int matvec_threads(int64_t dimDN);
 int tma_plan(const ed_op* op, MvArgs* a);
 int tma_grid(const ed_op* op);
+// Rows of each of the G CTAs: longest-processing-time-first under the cost
+// model 1 + w * len_up(u) / mean len_up (w from ED_ROW_COST_UP, default kRowCostUp).
+// queue: all rows in decreasing order of that cost.
+void row_plan(const SpinTable& up, int G, std::vector<uint32_t>* start, std::vector<uint32_t>* list,
+              std::vector<uint32_t>* queue);
 cudaError_t launch_matvec_tma(const ed_op* op, const MvArgs& a, int out, cudaStream_t s);
 
 }  // namespace ed

@@ -287,6 +287,9 @@ struct Workspace {
     unsigned int* gbar = nullptr;  // grid-barrier counter of the persistent kernel, then
                                    // its three reduction sets (kFusedSync bytes)
     unsigned long long* stamps = nullptr;  // phase timestamps (profile 2), kLzStamps per step
+    uint64_t* fxbound = nullptr;           // 2^kFxBits - 1: the bound every Lanczos vector meets
+    unsigned long long* cta_stamps = nullptr;  // per-CTA phase ends (profile 2)
+    size_t cta_stamps_n = 0;
     std::vector<cudaEvent_t> events;  // profiling pool (pairs)
 };
 
@@ -306,13 +309,13 @@ void free_ws(Workspace* w) {
     cudaFree(w->emax); cudaFree(w->flag); 
     cudaFree(w->dot_lo); cudaFree(w->dot_hi); cudaFree(w->coef_rt); cudaFree(w->coef_rs);
     cudaFree(w->ritz_part); cudaFree(w->ritz_ctr); cudaFree(w->inv_norm); cudaFree(w->gbar);
-    cudaFree(w->stamps);
+    cudaFree(w->stamps); cudaFree(w->fxbound); cudaFree(w->cta_stamps);
     for (cudaEvent_t e : w->events) cudaEventDestroy(e);
     *w = Workspace();
 }
 
 constexpr int kDotChunks = 64;
-constexpr size_t kFusedSync = 128;  // barrier counter at 0, LzRedSet[3] at 32
+constexpr size_t kFusedSync = 192;  // barrier counter at 0, LzRedSet[4] at 32, row-queue counters at 160
 
 ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_steps) {
     if (w->basis && w->basis_slots >= slots && w->DW == DW && w->max_steps >= max_steps) return ED_OK;
@@ -348,6 +351,11 @@ ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_s
     LZ_CK(cudaMemset(w->ritz_ctr, 0, sizeof(unsigned int)));
     LZ_CK(cudaMalloc(&w->inv_norm, sizeof(double)));
     LZ_CK(cudaMalloc(&w->gbar, kFusedSync));
+    {
+        const uint64_t bound = (1ULL << kFxBits) - 1;
+        LZ_CK(cudaMalloc(&w->fxbound, sizeof(uint64_t)));
+        LZ_CK(cudaMemcpy(w->fxbound, &bound, sizeof(uint64_t), cudaMemcpyHostToDevice));
+    }
     LZ_CK(cudaMalloc(&w->stamps, sizeof(unsigned long long) * kLzStamps * ns));
     LZ_CK(cudaMemcpy(w->lz, &w->h, sizeof(LzState), cudaMemcpyHostToDevice));
     return ED_OK;
@@ -470,8 +478,19 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             const int j1 = cfg->mode == ED_LANCZOS_REFERENCE ? std::min(max_steps, (j / 10 + 1) * 10) : max_steps;
             LZ_CK(cudaMemsetAsync(w->gbar, 0, kFusedSync, s));
             LzRedSet* red = reinterpret_cast<LzRedSet*>(reinterpret_cast<char*>(w->gbar) + 32);
-            LzFusedArgs fa{w->basis, w->stride, stored ? 1 : 0, j, j1, w->u, DW, lz, w->gbar, red,
-                           stamps ? w->stamps : nullptr};
+            if (stamps) {
+                const size_t need = (size_t)2 * max_steps * op->tma_grid;
+                if (w->cta_stamps_n < need) {
+                    cudaFree(w->cta_stamps);
+                    w->cta_stamps = nullptr;
+                    w->cta_stamps_n = 0;
+                    LZ_CK(cudaMalloc(&w->cta_stamps, sizeof(unsigned long long) * need));
+                    w->cta_stamps_n = need;
+                }
+            }
+            unsigned int* taken = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(w->gbar) + 160);
+            LzFusedArgs fa{w->basis, w->stride, stored ? 1 : 0, j, j1, w->u, DW, lz, w->gbar, red, taken,
+                           stamps ? w->stamps : nullptr, stamps ? w->cta_stamps : nullptr};
             if (stamps) LZ_CK(cudaEventRecord(w->events[2 * n_fused], s));
             const cudaError_t e = launch_lz_fused(op, fa, s);
             if (e == cudaSuccess && stamps) LZ_CK(cudaEventRecord(w->events[2 * n_fused + 1], s));
@@ -486,7 +505,10 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             j = j1;
         } else {
             if (prof) LZ_CK(cudaEventRecord(w->events[4 * j], s));
-            LZ_CK(launch_matvec_lz(op, slot(j), w->u, lz, H.m + j, j, s));
+            // output shift from the |q| < 2^54 bound (as the persistent kernel
+            // does), or from the exact max when reorthogonalisation may have
+            // changed the vector
+            LZ_CK(launch_matvec_lz(op, slot(j), w->u, lz, cfg->reorth ? H.m + j : w->fxbound, j, s));
             if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 1], s));
             const int64_t* pj = j > 0 ? slot(j - 1) : slot(j);
             if (prof) LZ_CK(cudaEventRecord(w->events[4 * j + 2], s));
@@ -614,7 +636,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     }
     if (alpha_h) std::memcpy(alpha_h, ha.data(), sizeof(double) * n);
     if (beta_h) std::memcpy(beta_h, hb.data(), sizeof(double) * (n + 1));
-    double mv_ms = 0.0, ax_ms = 0.0, rd_ms = 0.0, bar_ms = 0.0, sc_ms = 0.0, fz_ms = 0.0;
+    double mv_ms = 0.0, ax_ms = 0.0, rd_ms = 0.0, bar_ms = 0.0, sc_ms = 0.0, fz_ms = 0.0, rws_ms = 0.0, axs_ms = 0.0;
     if (prof) {
         LZ_CK(cudaStreamSynchronize(s));
         for (int j = 0; j < steps_run; ++j) {
@@ -642,6 +664,15 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             bar_ms += ms(q[2], q[3]) + ms(q[6], q[7]);
             sc_ms += ms(q[3], q[4]) + ms(q[7], q[8]);
         }
+        const int G = op->tma_grid;
+        std::vector<unsigned long long> c((size_t)2 * steps_run * G);
+        LZ_CK(cudaMemcpy(c.data(), w->cta_stamps, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost));
+        for (int j2 = 0; j2 < steps_run; ++j2)
+            for (int ph = 0; ph < 2; ++ph) {
+                const unsigned long long* q = c.data() + ((size_t)j2 * 2 + ph) * G;
+                const auto mm = std::minmax_element(q, q + G);
+                (ph ? axs_ms : rws_ms) += ms(*mm.first, *mm.second);
+            }
     }
     if (res) {
         res->launches = launches;
@@ -651,6 +682,8 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         res->barrier_ms = bar_ms;
         res->scalar_ms = sc_ms;
         res->fused_ms = fz_ms;
+        res->rows_spread_ms = rws_ms;
+        res->axpy_spread_ms = axs_ms;
         res->n_matvec = steps_run;
         res->e0 = e0;
         res->steps = n;

@@ -13,6 +13,7 @@ namespace ed {
 
 constexpr int kLzMaxPartials = 152 * 16;  // entries of each partial-sum array
 constexpr int kLzStamps = 9;              // timestamps per step of the persistent kernel
+constexpr int kFxBits = 54;               // every FX Lanczos vector has |q| < 2^kFxBits
 
 struct LzState {
     // per Krylov slot j (device arrays of length max_steps + 2)
@@ -54,9 +55,12 @@ struct LzFusedArgs {
     int64_t n;           // stored values (D * W)
     LzState* lz;
     unsigned int* gbar;  // grid-barrier arrivals, zero at launch
-    LzRedSet* red;       // three accumulator sets, zero at launch
+    LzRedSet* red;       // four accumulator sets, zero at launch
+    unsigned int* taken; // two row-queue counters (step parity), zero at launch
     unsigned long long* stamps;  // optional: %globaltimer of block 0 at kLzStamps
                                  // points of every step (see ed_lanczos_fused.cu)
+    unsigned long long* cta_stamps;  // optional: every CTA's rows-done and axpy-done
+                                     // times, [step][2][gridDim.x]
 };
 
 }  // namespace ed

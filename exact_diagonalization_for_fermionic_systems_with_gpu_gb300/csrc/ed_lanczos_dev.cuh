@@ -17,6 +17,26 @@
 namespace ed {
 namespace dev {
 
+// x * 2^k, exact: an add to the exponent field when x and the result are
+// normal numbers, ldexp otherwise.
+__device__ __forceinline__ double scale2(double x, int k) {
+    const long long b = __double_as_longlong(x);
+    const int ex = (int)((b >> 52) & 0x7FF);
+    if (ex == 0 || ex + k <= 0 || ex + k >= 0x7FF) return ldexp(x, k);
+    return __longlong_as_double(b + ((long long)k << 52));
+}
+
+// The exponent frexp returns for x != 0 (|x| in [2^(e-1), 2^e)).
+__device__ __forceinline__ int frexp_exp(double x) {
+    const int ex = (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+    if (ex == 0 || ex == 0x7FF) {
+        int e = 0;
+        frexp(x, &e);
+        return e;
+    }
+    return ex - 1022;
+}
+
 // Scalars of one step after the matvec reduction.
 struct LzCoefs {
     double alpha;
@@ -46,12 +66,12 @@ __device__ inline LzCoefs lz_coefs(int j, i128 alpha_raw, int e_u, uint64_t m_u,
 
     double a[3];
     uint64_t mm[3];
-    a[0] = ldexp(ib, e_u);
+    a[0] = scale2(ib, e_u);
     mm[0] = m_u;
-    a[1] = -aj * ldexp(ib, eX);
+    a[1] = -aj * scale2(ib, eX);
     mm[1] = mX;
     if (j > 0) {
-        a[2] = -bj * ldexp(ibP, eP);
+        a[2] = -bj * scale2(ibP, eP);
         mm[2] = mP;
     } else {
         a[2] = 0.0;
@@ -60,18 +80,22 @@ __device__ inline LzCoefs lz_coefs(int j, i128 alpha_raw, int e_u, uint64_t m_u,
     double B = 0.0;
     for (int k = 0; k < 3; ++k) B += fabs(a[k]) * (double)mm[k];
     B *= (1.0 + 1e-9);
-    int kB = 0;
-    if (B > 0.0) frexp(B, &kB);  // B < 2^kB
+    const int kB = B > 0.0 ? frexp_exp(B) : 0;  // B < 2^kB
     const int e_w = kB - 54;
     // One common number of fractional bits for the three integer
-    // coefficients: the largest |a_k| 2^-e_w sets it so every |at_k| < 2^62.
-    double amax = 0.0;
-    for (int k = 0; k < 3; ++k)
-        if (mm[k] != 0) amax = fmax(amax, fabs(a[k]) * ldexp(1.0, -e_w));
+    // coefficients: the largest |a_k| 2^-e_w sets it so every |at_k| < 2^62
+    // (scaling by 2^-e_w is exact, so its frexp exponent is the largest
+    // exponent of the a_k minus e_w).
     int ka = 0;
-    if (amax > 0.0) frexp(amax, &ka);  // amax < 2^ka
+    bool any = false;
+    for (int k = 0; k < 3; ++k)
+        if (mm[k] != 0 && a[k] != 0.0) {
+            const int ek = frexp_exp(a[k]) - e_w;
+            ka = any ? max(ka, ek) : ek;
+            any = true;
+        }
     const int Fmin = 62 - ka;
-    for (int k = 0; k < 3; ++k) c.at[k] = (mm[k] != 0 && a[k] != 0.0) ? llrint(ldexp(a[k], Fmin - e_w)) : 0;
+    for (int k = 0; k < 3; ++k) c.at[k] = (mm[k] != 0 && a[k] != 0.0) ? llrint(scale2(a[k], Fmin - e_w)) : 0;
     c.Fa = Fmin;
     c.e_w = e_w;
     return c;

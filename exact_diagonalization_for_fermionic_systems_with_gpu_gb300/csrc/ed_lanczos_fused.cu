@@ -5,22 +5,28 @@
 // re-stages the down-spin tables into every CTA's shared memory each time.
 // Here each CTA (two per SM, all co-resident) stages the tables once and then
 // loops over the steps:
-//   phase M  u = H w_j with the shared-memory row engine (its own rows of u),
+//   phase M  u = H w_j with the shared-memory row engine, rows handed out
+//            through a queue (heaviest first, taken with an atomic counter),
 //            then <w_j, u> and max|u|                           -> grid barrier
 //            every CTA derives alpha_j and the axpy coefficients (identical
 //            in every CTA: same integers, same scalar code)
 //   phase A  w_{j+1} = (a0 u + a1 w_j + a2 w_{j-1}) >> Fa on a grid-stride
 //            slice, then |w_{j+1}|^2 and max|w_{j+1}|           -> grid barrier
-//            every CTA derives beta_{j+1}; block 0 stores the scalars
+//            (a data barrier: beta_{j+1} is read with the next step's sums)
+// The matvec's output shift uses the bound |q| < 2^54 that every Lanczos
+// vector meets by construction, so no step waits for a norm before its
+// matvec; the per-step kernels use the same bound when they run without
+// reorthogonalisation.
 // Grid reductions: each CTA reduces its values in shared memory and thread 0
 // adds them to a global accumulator set with integer atomics — the 128-bit
 // sum split into three 42-bit limbs, so the total is exact and independent of
 // the order of arrival — and takes the max with atomicMax, before it arrives
 // at the barrier.  After the barrier one read of four words gives every CTA
-// the grid totals.  Three accumulator sets rotate: set r % 3 serves reduction
-// r, and block 0 zeroes the set of reduction r-1 once barrier r has completed
-// (every reader of it has passed barrier r by then; its next user adds only
-// after barrier r+1, which block 0 reaches after the zeroing).
+// the grid totals.  Four accumulator sets rotate: set r % 4 serves reduction
+// r (two per step), which is read after barrier r or r+1; block 0 zeroes the
+// set of reduction r-2 once barrier r has completed (all its readers have
+// passed barrier r), and its next user adds only after barrier r+1, which
+// block 0 reaches after the zeroing.
 // The integer totals and the scalar arithmetic are those of the per-step
 // kernels, so the Lanczos coefficients are bit-identical to the per-step path.
 // Vectors written during the launch are read back with L2 (coherent) loads,
@@ -120,6 +126,27 @@ struct SlotScalars {
     double ib;  // 1 / beta (0 when beta is 0)
 };
 
+// Thread 0: slot k (= w_k) is complete with exponent e, exact sum of
+// (q q) >> 16 and max |q|: beta_k, breakdown and precision bookkeeping
+// (lz_after_axpy's), shift the slot scalars, block 0 stores them.
+__device__ __forceinline__ void slot_done(LzState* lz, int k, int e, i128 ss, uint64_t m, SlotScalars& sX,
+                                          SlotScalars& sP, int& status, int& min_bits, bool store) {
+    const double beta = lz_beta(ss, e);
+    const int bits = bitlen_u64(m);
+    if (bits < min_bits) min_bits = bits;
+    if (m == 0 && status == 0) status = 7;  // breakdown
+    if (store) {
+        lz->e[k] = e;
+        lz->m[k] = m;
+        lz->beta[k] = beta;
+        lz->min_bits = min_bits;
+        lz->status = status;
+        lz->steps_done = k;
+    }
+    sP = sX;
+    sX = {e, m, beta, lz_inv(beta)};
+}
+
 }  // namespace
 
 template <bool CPLX, bool FAST, bool SCHED>
@@ -136,7 +163,9 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
     const TmaSmem S = tma_view(a, sm, uoff, uent, &give_up);
     LzState* lz = f.lz;
     const int tid = threadIdx.x;
-    const bool has_row = blockIdx.x < (uint32_t)a.dimUP;
+    __shared__ uint32_t s_next;  // row-queue index taken by thread 0
+    uint32_t u0 = 0;
+    const bool has_row = tma_first_row_dyn(a, &u0);
     const uint32_t G = gridDim.x;
 
     if (tid == 0) {
@@ -164,7 +193,11 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
 
     uint32_t rc = 0;          // rows streamed through the row buffers
     unsigned int target = 0;  // grid-barrier arrivals expected so far
-    int r = 0;                // grid reductions so far
+    // every Lanczos vector has |q| < 2^54 (start vector by its FX exponent,
+    // later ones by the axpy bound), so the matvec shift needs no reduction
+    const int sb = a.bq_bits + kFxBits - 62;
+    const int s_u = sb > 0 ? sb : 0;
+    int e_w_prev = 0;         // exponent of w_j chosen at step j-1
     for (int j = f.j0; j < f.j1; ++j) {
         const int64_t* xq = slot(j);
         const int64_t* pq = j > 0 ? slot(j - 1) : slot(j);
@@ -172,23 +205,24 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
         const bool stamp = f.stamps && blockIdx.x == 0 && tid == 0;
         unsigned long long* st = stamps_at(f, j);
         if (stamp) st[0] = global_ns();
+        const int rM = 2 * (j - f.j0), rA = rM + 1;  // reductions (and barriers) of this step
 
         // ---- phase M: u = H w_j -------------------------------------------
-        const int b = a.bq_bits + bitlen_u64(sX.m) - 62;
-        const int s_u = b > 0 ? b : 0;
         if (tid == 0 && has_row) {
             tma::fence_proxy_async_global();
             tma::fence_proxy_async_smem();
-            tma_issue_row<CPLX>(a, S, xq, blockIdx.x, rc & 1);
+            tma_issue_row<CPLX>(a, S, xq, u0, rc & 1);
         }
         {
             i128 dot = 0;
             uint64_t mx = 0;
-            tma_rows<CPLX, 1, FAST, true, SCHED>(a, S, xq, f.u, nullptr, rc, 0, s_u, dot, mx);
+            tma_rows<CPLX, 1, FAST, true, SCHED, true>(a, S, xq, f.u, nullptr, rc, 0, s_u, dot, mx,
+                                                       f.taken + (j & 1), &s_next);
             if (give_up) return;
             if (stamp) st[1] = global_ns();
+            if (f.cta_stamps && tid == 0) f.cta_stamps[(size_t)j * 2 * G + blockIdx.x] = global_ns();
             block_sum_max(dot, mx, s128, s64);
-            if (tid == 0) red_push(&f.red[r % 3], dot, mx);
+            if (tid == 0) red_push(&f.red[rM % 4], dot, mx);
             if (stamp) st[2] = global_ns();
         }
         if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
@@ -196,10 +230,23 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
             if (stamp) st[3] = global_ns();
             i128 s;
             uint64_t m;
-            red_pull(&f.red[r % 3], s, m);
-            if (blockIdx.x == 0) f.red[(r + 2) % 3] = LzRedSet{0, 0, 0, 0};
+            red_pull(&f.red[rM % 4], s, m);
+            if (j > f.j0) {
+                // slot j from the previous step's axpy reduction
+                i128 ss;
+                uint64_t mw;
+                red_pull(&f.red[(rM - 1) % 4], ss, mw);
+                slot_done(lz, j, e_w_prev, ss, mw, sX, sP, s_status, s_min_bits, blockIdx.x == 0);
+            }
+            if (blockIdx.x == 0) {
+                if (rM >= 2) f.red[(rM - 2) % 4] = LzRedSet{0, 0, 0, 0};
+                // the other queue counter was last taken from in step j-1 and
+                // is next taken from in step j+1, after the next barrier
+                f.taken[(j + 1) & 1] = 0;
+            }
             const int e_u = sX.e - a.Fc + s_u;
             s_coef = lz_coefs(j, s, e_u, m, sX.e, sX.m, sX.beta, sP.e, sP.m, sP.ib, s_status);
+            e_w_prev = s_coef.e_w;
             if (blockIdx.x == 0) {
                 lz->s_u = s_u;
                 lz->e_u = e_u;
@@ -214,7 +261,6 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
             }
             if (stamp) st[4] = global_ns();
         }
-        ++r;
         __syncthreads();
 
         // ---- phase A: w_{j+1} = (a0 u + a1 w_j + a2 w_{j-1}) >> Fa ---------
@@ -249,42 +295,35 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
                 mw = aw > mw ? aw : mw;
             }
             if (stamp) st[5] = global_ns();
+            if (f.cta_stamps) {
+                __syncthreads();
+                if (tid == 0) f.cta_stamps[((size_t)j * 2 + 1) * G + blockIdx.x] = global_ns();
+            }
             block_sum_max(ss, mw, s128, s64);
-            if (tid == 0) red_push(&f.red[r % 3], ss, mw);
+            if (tid == 0) red_push(&f.red[rA % 4], ss, mw);
             if (stamp) st[6] = global_ns();
         }
+        // a data barrier: the next matvec gathers w_{j+1} from every CTA; the
+        // norm and max of w_{j+1} are read at the next step's reduction
         if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
         if (tid == 0) {
-            if (stamp) st[7] = global_ns();
-            i128 s;
-            uint64_t m;
-            red_pull(&f.red[r % 3], s, m);
-            if (blockIdx.x == 0) f.red[(r + 2) % 3] = LzRedSet{0, 0, 0, 0};
-            const int e_w = s_coef.e_w;
-            const double beta = lz_beta(s, e_w);
-            const int bits = bitlen_u64(m);
-            if (bits < s_min_bits) s_min_bits = bits;
-            if (m == 0 && s_status == 0) s_status = 7;  // breakdown
-            if (blockIdx.x == 0) {
-                lz->e[j + 1] = e_w;
-                lz->m[j + 1] = m;
-                lz->beta[j + 1] = beta;
-                lz->min_bits = s_min_bits;
-                lz->status = s_status;
-                lz->steps_done = j + 1;
+            if (blockIdx.x == 0 && rA >= 2) f.red[(rA - 2) % 4] = LzRedSet{0, 0, 0, 0};
+            if (stamp) st[7] = st[8] = global_ns();
+            if (j + 1 == f.j1 && blockIdx.x == 0) {
+                // the last slot of this launch: block 0 stores its scalars
+                i128 ss;
+                uint64_t mw;
+                red_pull(&f.red[rA % 4], ss, mw);
+                slot_done(lz, j + 1, s_coef.e_w, ss, mw, sX, sP, s_status, s_min_bits, true);
             }
-            sP = sX;
-            sX = {e_w, m, beta, lz_inv(beta)};
-            if (stamp) st[8] = global_ns();
         }
-        ++r;
         __syncthreads();
     }
 }
 
 // Cooperative launch of steps j0 .. j1-1; cudaErrorNotSupported when the
 // operator has no shared-memory plan, or the grid cannot be co-resident.
-// f.gbar and the three sets at f.red must be zero.
+// f.gbar and the four sets at f.red must be zero.
 cudaError_t launch_lz_fused(const ed_op* op, const LzFusedArgs& f, cudaStream_t s) {
     if (op->tma_smem <= 0) return cudaErrorNotSupported;
     const void* fn;
@@ -301,8 +340,9 @@ cudaError_t launch_lz_fused(const ed_op* op, const LzFusedArgs& f, cudaStream_t 
         return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op->device)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, op->device)) != cudaSuccess) return e;
-    if (!coop || per_sm < 1) return cudaErrorNotSupported;
-    const int64_t g = (int64_t)sms * (per_sm < 2 ? per_sm : 2);
+    // the row plan is made for op->tma_grid CTAs, all of which must be resident
+    if (!coop || (int64_t)per_sm * sms < op->tma_grid) return cudaErrorNotSupported;
+    const int64_t g = op->tma_grid;
     MvArgs av = op->mv;
     LzFusedArgs fv = f;
     void* args[] = {&av, &fv};

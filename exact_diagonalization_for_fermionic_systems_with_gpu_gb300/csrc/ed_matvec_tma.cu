@@ -5,12 +5,19 @@
 // plan and the launchers.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <cstdlib>
+#include <functional>
+#include <queue>
+#include <vector>
 
 #include "ed_matvec_tma.cuh"
 
 namespace ed {
 using namespace dev;
+
+constexpr double kRowCostUp = 0.8;  // up-term share of a row's cost at the mean up-row length
 
 template <bool CPLX, int OUT, bool FAST, bool SCHED>
 __global__ void __launch_bounds__(kTmaThreads, 2) k_matvec_tma(const MvArgs a) {
@@ -19,11 +26,12 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_matvec_tma(const MvArgs a) {
     __shared__ uint32_t uent[kTmaUpStage];
     __shared__ int give_up;
     const TmaSmem S = tma_view(a, sm, uoff, uent, &give_up);
-    const bool has_row = blockIdx.x < (uint32_t)a.dimUP;
+    uint32_t u0 = 0;
+    const bool has_row = tma_first_row(a, &u0);
     if (threadIdx.x == 0) {
         tma_init(S);
         tma_issue_tables(a, S);
-        if (has_row) tma_issue_row<CPLX>(a, S, a.xq, blockIdx.x, 0);
+        if (has_row) tma_issue_row<CPLX>(a, S, a.xq, u0, 0);
     }
     if (SCHED) tma_zero_slots(a, S);
     __syncthreads();
@@ -44,7 +52,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_matvec_tma(const MvArgs a) {
     uint64_t mx = 0;
     uint32_t rc = 0;
     if (!give_up) {
-        tma_rows<CPLX, OUT, FAST, false, SCHED>(a, S, a.xq, a.uq, a.y, rc, E_out, s_u, dot, mx);
+        tma_rows<CPLX, OUT, FAST, false, SCHED, false>(a, S, a.xq, a.uq, a.y, rc, E_out, s_u, dot, mx);
     } else if (threadIdx.x == 0 && has_row) {
         tma::mbar_wait(&S.bar[0], 0);  // the first row copy must land before the CTA exits
     }
@@ -127,11 +135,49 @@ int tma_grid(const ed_op* op) {
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, kTmaThreads, op->tma_smem) != cudaSuccess ||
         per_sm < 1)
         per_sm = 1;
+    if (per_sm > 2) per_sm = 2;
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op->device);
-    int64_t g = (int64_t)sms * per_sm;
-    if (g > op->dimUP) g = op->dimUP;
-    return (int)(g < 1 ? 1 : g);
+    // every CTA is resident at once (the persistent Lanczos kernel relies on
+    // it); rows are spread over them by row_plan, some CTAs may have none
+    return sms * per_sm;
+}
+
+void row_plan(const SpinTable& up, int G, std::vector<uint32_t>* start, std::vector<uint32_t>* list,
+              std::vector<uint32_t>* queue) {
+    const int64_t n = up.count;
+    double w = kRowCostUp;
+    if (const char* e = std::getenv("ED_ROW_COST_UP")) w = std::atof(e);
+    double mean = 0.0;
+    for (int64_t u = 0; u < n; ++u) mean += up.len[u];
+    mean = n ? mean / (double)n : 0.0;
+    std::vector<double> cost(n);
+    for (int64_t u = 0; u < n; ++u) cost[u] = 1.0 + (mean > 0.0 ? w * up.len[u] / mean : 0.0);
+    std::vector<uint32_t> order(n);
+    for (int64_t u = 0; u < n; ++u) order[u] = (uint32_t)u;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return cost[x] > cost[y]; });
+    *queue = order;
+    // least-loaded CTA first; ties to the lowest index
+    using Slot = std::pair<double, int>;
+    std::priority_queue<Slot, std::vector<Slot>, std::greater<Slot>> heap;
+    for (int b = 0; b < G; ++b) heap.push({0.0, b});
+    std::vector<std::vector<uint32_t>> rows(G);
+    for (uint32_t u : order) {
+        Slot sl = heap.top();
+        heap.pop();
+        rows[sl.second].push_back(u);
+        sl.first += cost[u];
+        heap.push(sl);
+    }
+    start->assign(G + 1, 0);
+    list->clear();
+    list->reserve(n);
+    for (int b = 0; b < G; ++b) {
+        std::sort(rows[b].begin(), rows[b].end());
+        (*start)[b] = (uint32_t)list->size();
+        list->insert(list->end(), rows[b].begin(), rows[b].end());
+    }
+    (*start)[G] = (uint32_t)list->size();
 }
 
 }  // namespace ed

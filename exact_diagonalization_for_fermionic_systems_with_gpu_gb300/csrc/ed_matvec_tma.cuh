@@ -194,36 +194,66 @@ __device__ __forceinline__ void acc_up(const int64_t* __restrict__ xq, uint32_t 
     if (CPLX) i += vi;
 }
 
+// First row of this CTA (rowList[rowStart[b]]); false when it has none.
+__device__ __forceinline__ bool tma_first_row(const MvArgs& a, uint32_t* u) {
+    const uint32_t r0 = __ldg(a.rowStart + blockIdx.x);
+    if (r0 >= __ldg(a.rowStart + blockIdx.x + 1)) return false;
+    *u = __ldg(a.rowList + r0);
+    return true;
+}
+
 // The rows of this CTA: u = H x (OUT 0: FP64 y with exponent E_out; OUT 1:
 // FX uq >> s_u with the <x,u> and max|u| partials in dot, mx).
-// On entry thread 0 has issued the copy of row blockIdx.x into buffer rc & 1
-// (when blockIdx.x < dimUP) and the tables are in shared memory; rc counts the
-// rows this CTA has streamed so far (it fixes buffer and barrier phase) and
-// is advanced past the rows done.  On a give-up *S.give_up is set, the copy
-// in flight has been waited for and the function returns early.
-template <bool CPLX, int OUT, bool FAST, bool COH, bool SCHED>
+// On entry thread 0 has issued the copy of the CTA's first row into buffer
+// rc & 1 (when it has rows) and the tables are in shared memory; rc counts
+// the rows this CTA has streamed so far (it fixes buffer and barrier phase)
+// and is advanced past the rows done.  On a give-up *S.give_up is set, the
+// copy in flight has been waited for and the function returns early.
+// Rows of the CTA.  Static: the host plan rowList[rowStart[b] ..).  Dynamic
+// (taken != null): CTA b starts at rowQueue[b] and takes each further row as
+// rowQueue[gridDim.x + atomicAdd(taken, 1)] while it computes the current
+// one, so CTAs that finish early take more rows (the queue is in decreasing
+// order of cost).  *snext is a shared word for the index taken.
+__device__ __forceinline__ bool tma_first_row_dyn(const MvArgs& a, uint32_t* u) {
+    if (blockIdx.x >= (uint32_t)a.dimUP) return false;
+    *u = __ldg(a.rowQueue + blockIdx.x);
+    return true;
+}
+
+template <bool CPLX, int OUT, bool FAST, bool COH, bool SCHED, bool DYN>
 __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, const int64_t* __restrict__ xq,
                                          int64_t* __restrict__ uq, double* __restrict__ y, uint32_t& rc, int E_out,
-                                         int s_u, i128& dot, uint64_t& mx) {
+                                         int s_u, i128& dot, uint64_t& mx, unsigned int* taken = nullptr,
+                                         uint32_t* snext = nullptr) {
     constexpr int W = CPLX ? 2 : 1;
-    const uint32_t dimUP = (uint32_t)a.dimUP, dimDN = (uint32_t)a.dimDN;
+    const uint32_t dimDN = (uint32_t)a.dimDN;
     const int tid = threadIdx.x, T = blockDim.x;
     const bool merge = a.mergeUD != 0;
     const bool unitU = a.unitUP != 0 && a.nclsUP == 1;
     const bool unitD = a.unitDN != 0 && a.nclsDN == 1;
+    const uint32_t nq = (uint32_t)a.dimUP;
 
-    bool issued_next = false;  // thread 0: a copy for row u+gridDim.x is in flight
-    for (uint32_t u = blockIdx.x; u < dimUP; u += gridDim.x, ++rc) {
+    bool issued_next = false;  // thread 0: a copy for the next row is in flight
+    const uint32_t r1 = DYN ? nq : __ldg(a.rowStart + blockIdx.x + 1);
+    for (uint32_t r = DYN ? blockIdx.x : __ldg(a.rowStart + blockIdx.x); r < r1; ++rc) {
+        const uint32_t u = DYN ? __ldg(a.rowQueue + r) : __ldg(a.rowList + r);
         const int buf = rc & 1;
         const uint32_t parity = (rc >> 1) & 1;
         // prefetch the next row into the other buffer (its readers finished
         // at the barrier that closed the previous iteration)
-        const uint32_t un = u + gridDim.x;
         issued_next = false;
-        if (tid == 0 && un < dimUP) {
-            tma::fence_proxy_async_smem();
-            tma_issue_row<CPLX>(a, S, xq, un, buf ^ 1);
-            issued_next = true;
+        if (tid == 0) {
+            uint32_t rn = r + 1;
+            if (DYN) {
+                rn = gridDim.x + atomicAdd(taken, 1u);
+                *snext = rn;
+            }
+            if (rn < r1) {
+                const uint32_t un = DYN ? __ldg(a.rowQueue + rn) : __ldg(a.rowList + rn);
+                tma::fence_proxy_async_smem();
+                tma_issue_row<CPLX>(a, S, xq, un, buf ^ 1);
+                issued_next = true;
+            }
         }
         const uint32_t p0 = __ldg(a.upPtr + u), lenU = __ldg(a.upPtr + u + 1) - p0;
         const int nposU = FAST ? (int)__ldg(a.upNpos + u) : 0;
@@ -247,6 +277,7 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
             if (tid == 0 && issued_next) tma::mbar_wait(&S.bar[buf ^ 1], ((rc + 1) >> 1) & 1);
             return;
         }
+        const uint32_t r_next = DYN ? *snext : r + 1;  // written by thread 0 before the barrier above
         const int64_t* xrow = buf ? S.row1 : S.row0;
         const uint64_t stu = __ldg(a.stUP + u);
         const int64_t du = __ldg(a.dUPq + u);
@@ -409,6 +440,7 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
             }
         }
         __syncthreads();  // row buffer and uoff are free for the next iteration
+        r = r_next;
     }
 }
 

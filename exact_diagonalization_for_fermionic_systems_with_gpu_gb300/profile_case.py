@@ -67,7 +67,9 @@ def main():
         print(f"E0 {res.e0:.12f} steps {res.steps} matvec {res.matvec_ms / n * 1e3:.1f} us "
               f"axpy {res.axpy_ms / n * 1e3:.1f} us reduce {res.reduce_ms / n * 1e3:.1f} us "
               f"(barrier wait {res.barrier_ms / n * 1e3:.1f}, scalars {res.scalar_ms / n * 1e3:.1f}) "
-              f"launches {res.launches}" + (f" persistent launch {res.fused_ms:.3f} ms" if res.fused_ms else ""))
+              f"launches {res.launches}" + (f" persistent launch {res.fused_ms:.3f} ms, CTA finish spread: rows "
+                                            f"{res.rows_spread_ms / n * 1e3:.1f} us axpy {res.axpy_spread_ms / n * 1e3:.1f} us"
+                                            if res.fused_ms else ""))
     else:
         dt = torch.complex128 if op.is_complex else torch.float64
         x = torch.empty(op.rows(), dtype=torch.float64 if not op.is_complex else torch.float64,

@@ -201,6 +201,9 @@ typedef struct {
                               the Lanczos scalars */
     double fused_ms;       /* profile 2: CUDA-event time of the persistent
                               kernel launches */
+    double rows_spread_ms; /* profile 2: summed over steps, last minus first
+                              CTA to finish its matvec rows */
+    double axpy_spread_ms; /* profile 2: the same for the axpy slices */
 } ed_lanczos_result;
 
 /* Run Lanczos on op.  start: ED_START_USER start vector (rows doubles, mem
