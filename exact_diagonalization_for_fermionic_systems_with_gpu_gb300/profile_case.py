@@ -6,6 +6,7 @@
 --what lanczos : one fixed-step Lanczos solve, per-step kernels timed with events
 --what fused   : one fixed-step Lanczos solve in the persistent kernel, phases
                  timed with device timestamps
+--what solve   : the same solve without timing hooks (what bench.py runs)
 --what perform : --steps operator applies through the FP64 C-ABI path
 Cases: kagome12 (6+6, dim 853,776, L2-resident vectors), chain14 (7+7 open
 chain with disorder, dim 11,778,624, vectors larger than L2), lieb18
@@ -44,7 +45,7 @@ def build_case(name: str):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="kagome12")
-    ap.add_argument("--what", default="lanczos", choices=["lanczos", "fused", "perform"])
+    ap.add_argument("--what", default="lanczos", choices=["lanczos", "fused", "solve", "perform"])
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--ritz", default="none", choices=["none", "stored"],
                     help="stored: keep the Krylov basis and form the Ritz vector, as the bench does")
@@ -53,11 +54,11 @@ def main():
     op = build_case(args.case)
     lib = _capi.load()
     t0 = time.perf_counter()
-    if args.what in ("lanczos", "fused"):
+    if args.what in ("lanczos", "fused", "solve"):
         ritz = _capi.ED_RITZ_STORED if args.ritz == "stored" else _capi.ED_RITZ_NONE
         cfg = _capi.ed_lanczos_cfg(max_steps=args.steps, mode=_capi.ED_LANCZOS_FIXED, reorth=0,
                                    ritz=ritz, start=_capi.ED_START_RANDOM,
-                                   profile=1 if args.what == "lanczos" else 2, seed=0)
+                                   profile={"lanczos": 1, "fused": 2, "solve": 0}[args.what], seed=0)
         res = _capi.ed_lanczos_result()
         evec = np.empty(op.rows() * (2 if op.is_complex else 1))
         _capi.check(lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0,
