@@ -1,12 +1,14 @@
 // ed_lanczos.cu — device-resident FX Lanczos (HubMatrix_GPU.cuh:477-613).
 //
-// One step = two launches:
+// A run is either one persistent launch (ed_lanczos_fused.cu) or two
+// launches per step:
 //   k_matvec<OUT=1>  u = H w_j (exact), alpha_j, axpy coefficients
 //   k_lz_axpy        w_{j+1} = a0 u + a1 w_j + a2 w_{j-1}, beta_{j+1}
-// Scalars never leave the device during the recurrence.  The Krylov vectors
-// are kept (ED_RITZ_STORED: one int64 vector per step, memory is plentiful
-// on this GPU) so the Ritz vector is a single weighted sum instead of the
-// reference's second Lanczos pass.
+// Scalars never leave the device during the recurrence.  The Ritz vector is
+// a single weighted sum of the stored Krylov vectors (ED_RITZ_STORED: one
+// int64 vector per step), or, when the basis does not fit, the reference's
+// second Lanczos pass (ED_RITZ_RECOMPUTE), which regenerates the same
+// vectors bit for bit and accumulates the sum as it goes.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -246,6 +248,39 @@ __global__ void __launch_bounds__(kLzThreads) k_ritz(const int64_t* __restrict__
     }
 }
 
+// Second-pass Ritz sum: acc (+)= (rt_k q_k >> rs_k) * 2^-F for the Lanczos
+// vector q_k just produced (first: acc is overwritten).
+__global__ void __launch_bounds__(kLzThreads) k_ritz_acc(double* __restrict__ acc, const int64_t* __restrict__ q,
+                                                         int64_t n, const int64_t* __restrict__ rt,
+                                                         const int* __restrict__ rs, int F, int k, int first) {
+    const int64_t c = rt[k];
+    const int r = rs[k];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double t = i128_to_f64(mul_wide(c, q[i]) >> r, -F);
+        acc[i] = first ? t : acc[i] + t;
+    }
+}
+
+// *inv_norm = 1 / |v| (0 for a zero vector); block partials, last block sums.
+__global__ void __launch_bounds__(kLzThreads) k_inv_norm(const double* __restrict__ v, int64_t n,
+                                                         double* __restrict__ part, unsigned int* counter,
+                                                         double* inv_norm) {
+    double ss = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        ss = fma(v[i], v[i], ss);
+    __shared__ double sd[32];
+    const double bs = block_sum_f64(ss, sd);
+    if (threadIdx.x == 0) part[blockIdx.x] = bs;
+    if (elect_last_block(counter)) {
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int i = 0; i < (int)gridDim.x; ++i) t += __ldcg(part + i);
+            *inv_norm = t > 0.0 ? 1.0 / sqrt(t) : 0.0;
+            *counter = 0;
+        }
+    }
+}
+
 __global__ void k_scale(double* __restrict__ v, int64_t n, const double* __restrict__ s) {
     const double f = *s;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -414,8 +449,10 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     const int W = op->cplx ? 2 : 1;
     const int64_t DW = op->D * W;
     const int max_steps = cfg->max_steps;
+    // with reorthogonalisation the basis is stored anyway, and its Ritz sum
+    // replaces the second pass
     const bool stored = cfg->ritz == ED_RITZ_STORED || cfg->reorth;
-    if (cfg->ritz == ED_RITZ_RECOMPUTE) return ED_ERR_NOT_BUILT;
+    const int ritz = (cfg->ritz == ED_RITZ_RECOMPUTE && cfg->reorth) ? ED_RITZ_STORED : cfg->ritz;
     const size_t slots = stored ? (size_t)max_steps + 1 : 3;
     if (!*ws_slot) *ws_slot = new WsHolder();
     Workspace* w = &reinterpret_cast<WsHolder*>(*ws_slot)->ws;
@@ -606,7 +643,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     e0 = tri[0];
     resid = std::fabs(hb[n] * tri[n]);
 
-    if (evec && cfg->ritz == ED_RITZ_STORED) {
+    if (evec && ritz == ED_RITZ_STORED) {
         std::vector<int> ev(n);
         std::vector<uint64_t> mv(n);
         LZ_CK(cudaMemcpyAsync(ev.data(), H.e, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
@@ -633,6 +670,56 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         if (evec_mem != ED_MEM_DEVICE)
             LZ_CK(cudaMemcpyAsync(evec, out, sizeof(double) * DW, cudaMemcpyDeviceToHost, s));
         LZ_CK(cudaStreamSynchronize(s));
+    }
+    if (evec && ritz == ED_RITZ_RECOMPUTE) {
+        // The reference's second pass (HubMatrix_GPU.cuh:600-612): the same
+        // start vector and the same deterministic recurrence regenerate
+        // w_0 .. w_{n-1} bit for bit; each is added to the Ritz sum with
+        // weight z_k / beta_k as soon as it exists.
+        std::vector<int> ev(n);
+        LZ_CK(cudaMemcpyAsync(ev.data(), H.e, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+        LZ_CK(cudaStreamSynchronize(s));
+        std::vector<double> r(n);
+        for (int k = 0; k < n; ++k) r[k] = tri[1 + k] / hb[k] * std::ldexp(1.0, ev[k]);
+        std::vector<int64_t> rt;
+        std::vector<int> rs;
+        int F;
+        fx_coefs(r, &rt, &rs, &F);
+        LZ_CK(cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
+        LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+        LZ_CK(cudaMemsetAsync(H.counter, 0, sizeof(unsigned int) * 4, s));
+        LZ_CK(launch_emax(w->fbuf, DW, w->emax, w->flag, s));
+        k_lz_start<<<lz_grid(DW), kLzThreads, 0, s>>>(w->fbuf, DW, w->emax, w->flag, slot(0), lz);
+        LZ_CK(cudaGetLastError());
+        // the start vector in fbuf is consumed: fbuf can hold the sum
+        double* out = evec_mem == ED_MEM_DEVICE ? evec : w->fbuf;
+        const int g = lz_grid(DW);
+        k_ritz_acc<<<g, kLzThreads, 0, s>>>(out, slot(0), DW, w->coef_rt, w->coef_rs, F, 0, 1);
+        LZ_CK(cudaGetLastError());
+        launches += 3;
+        for (int k = 0; k + 1 < n; ++k) {
+            LZ_CK(launch_matvec_lz(op, slot(k), w->u, lz, w->fxbound, k, s));
+            const int64_t* pk = k > 0 ? slot(k - 1) : slot(k);
+            k_lz_axpy<<<g, kLzThreads, 0, s>>>(w->u, slot(k), pk, slot(k + 1), DW, lz, k);
+            LZ_CK(cudaGetLastError());
+            k_ritz_acc<<<g, kLzThreads, 0, s>>>(out, slot(k + 1), DW, w->coef_rt, w->coef_rs, F, k + 1, 0);
+            LZ_CK(cudaGetLastError());
+            launches += 3;
+        }
+        k_inv_norm<<<g, kLzThreads, 0, s>>>(out, DW, w->ritz_part, w->ritz_ctr, w->inv_norm);
+        LZ_CK(cudaGetLastError());
+        k_scale<<<g, kLzThreads, 0, s>>>(out, DW, w->inv_norm);
+        LZ_CK(cudaGetLastError());
+        launches += 2;
+        if (evec_mem != ED_MEM_DEVICE)
+            LZ_CK(cudaMemcpyAsync(evec, out, sizeof(double) * DW, cudaMemcpyDeviceToHost, s));
+        int err2 = 0;
+        LZ_CK(cudaMemcpyAsync(&err2, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+        LZ_CK(cudaStreamSynchronize(s));
+        if (err2) {
+            cudaMemset(op->d_err, 0, sizeof(int));
+            return ED_ERR_TIMEOUT;
+        }
     }
     if (alpha_h) std::memcpy(alpha_h, ha.data(), sizeof(double) * n);
     if (beta_h) std::memcpy(beta_h, hb.data(), sizeof(double) * (n + 1));

@@ -3,8 +3,9 @@
 // The Lanczos vectors are kept unnormalised (w_j, |w_j| = beta_j) in FX
 // format, one exponent per vector; v_j = w_j / beta_j is never formed.  All
 // scalar bookkeeping (alpha_j, beta_j, exponents, the integer coefficients
-// of the next axpy) happens on the device in the last block of each
-// reduction, so a step is two kernel launches with no host round trip.
+// of the next axpy) happens on the device: in the last block of each
+// reduction of the per-step kernels (two launches per step), or in every
+// CTA of the persistent kernel after its grid barriers (one launch per run).
 #pragma once
 
 #include <cstdint>

@@ -60,7 +60,7 @@ def main():
                                    ritz=ritz, start=_capi.ED_START_RANDOM,
                                    profile={"lanczos": 1, "fused": 2, "solve": 0}[args.what], seed=0)
         res = _capi.ed_lanczos_result()
-        evec = np.empty(op.rows() * (2 if op.is_complex else 1))
+        evec = np.empty(op.rows() * (2 if op.is_complex else 1)) if args.ritz == "stored" else None
         _capi.check(lib.ed_lanczos_run(op.handle, C.byref(cfg), None, 0,
                                        C.c_void_p(evec.ctypes.data) if args.ritz == "stored" else None, 0,
                                        None, None, C.byref(res), None), "ed_lanczos_run")
@@ -80,10 +80,17 @@ def main():
         _capi.check(lib.ed_random_vector_device(n, 1, C.c_void_p(x.data_ptr()), None), "random")
         x = x.view(dt) if op.is_complex else x
         y = torch.empty_like(x)
+        op.Hubbard_mv(x, y)  # warm
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
         for _ in range(args.steps):
             op.Hubbard_mv(x, y)
+        e1.record()
         torch.cuda.synchronize()
-        print(f"{args.steps} applies, |y| = {float(torch.linalg.vector_norm(y)):.6e}")
+        ms = e0.elapsed_time(e1) / max(args.steps, 1)
+        gbs = 16.0 * op.rows() * (2 if op.is_complex else 1) / (ms * 1e-3) / 1e9
+        print(f"{args.steps} applies, {ms:.3f} ms each ({gbs:.0f} GB/s of 16 B x stored values), "
+              f"|y| = {float(torch.linalg.vector_norm(y)):.6e}")
     print(f"wall {time.perf_counter() - t0:.2f} s")
     op.close()
 

@@ -331,3 +331,25 @@ def ref_tables(N: int, Q: int, terms: Sequence[tuple]):
 
 def num_threads() -> int:
     return int(load().orc_num_threads())
+
+
+def sampled_rows(up: Tables, dn: Tables, U: float, idx: np.ndarray, fetch, mask: int | None = None):
+    """Hubbard_mv_ (HubMatrix_GPU.cuh:114-161) restated for selected output
+    elements only, for vectors too large for the host: y[i] for the flat
+    indices i = u * dim_dn + d in idx, with x read through fetch(flat indices)
+    -> float64 values.  Returns (y, scale) where scale[i] = sum of |terms|,
+    the size the rounding of y[i] is measured against."""
+    mask = mask_all(up.N) if mask is None else mask
+    idx = np.asarray(idx, dtype=np.int64)
+    nd = dn.count
+    u, d = idx // nd, idx % nd
+    axu, aju = up.Ax[:, u], up.Aj[:, u]          # (slots, n)
+    axd, ajd = dn.Ax[:, d], dn.Aj[:, d]
+    xu = fetch((aju * nd + d[None, :]).ravel()).reshape(axu.shape)
+    xd = fetch((u[None, :] * nd + ajd).ravel()).reshape(axd.shape)
+    x0 = fetch(idx)
+    occ = np.array([bin(int(a) & int(b) & mask).count("1") for a, b in zip(up.state[u], dn.state[d])], dtype=np.float64)
+    tu, td, t0 = axu * xu, axd * xd, U * occ * x0
+    y = tu.sum(0) + td.sum(0) + t0
+    scale = np.abs(tu).sum(0) + np.abs(td).sum(0) + np.abs(t0)
+    return y, scale

@@ -205,3 +205,27 @@ def test_persistent_kernel_launch_count(ed):
     # random, emax, start; one persistent launch; Ritz sum and scale (the
     # tridiagonal eigensolve runs on the host)
     assert res.launches == 3 + 1 + 2
+
+
+@pytest.mark.parametrize("case", ["kagome12_fixed", "chain8_reference", "chain12_fixed_per_step"])
+def test_ritz_recompute_matches_stored(ed, monkeypatch, case):
+    """ED_RITZ_RECOMPUTE (the reference's second Lanczos pass, three working
+    vectors) regenerates the same Lanczos vectors bit for bit, so its Ritz
+    vector equals the stored-basis sum up to the FP64 accumulation of the
+    second pass (1e-12 normwise), with identical T and E0."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    if case == "kagome12_fixed":
+        op, steps, mode = op_for(ed, 12, 6, 6, L.kagome12(), L.kagome12(), 8.0), 300, "fixed"
+    elif case == "chain8_reference":
+        op, steps, mode = op_for(ed, 8, 4, 4, L.chain(8), L.chain(8), 4.0), 1000, "reference"
+    else:
+        eps = list(philox_uniform(100, 12, 6.0))
+        t = L.chain(12, periodic=False, eps=eps)
+        op, steps, mode = op_for(ed, 12, 6, 6, t, t, 1.0), 200, "fixed"
+        monkeypatch.setenv("ED_LZ_FUSED", "0")
+    l1, l2 = ed.Lanczos(), ed.Lanczos()
+    e1, v1 = l1.eigen(op, max_steps=steps, mode=mode, ritz="stored", seed=2)
+    e2, v2 = l2.eigen(op, max_steps=steps, mode=mode, ritz="recompute", seed=2)
+    assert e1 == e2 and l1.a == l2.a and l1.b == l2.b
+    assert np.linalg.norm(v1 - v2) < 1e-12
+    assert abs(np.linalg.norm(v2) - 1.0) < 1e-13

@@ -199,3 +199,36 @@ def test_matvec_kernels_agree_bit_for_bit(ed, monkeypatch, case):
         e, _ = lz.eigen(op, max_steps=min(30, n), mode="fixed", ritz="none", seed=4)
         runs[k] = (lz.a, lz.b, e)
     assert runs["auto"] == runs["generic"]
+
+
+def test_lieb18_full_size_sampled_rows(ed, orc):
+    """Lieb18 9+9 (D = 2,363,904,400; 18.9 GB per FP64 vector), which the
+    reference's int-indexed kernel cannot run: y = H x on the device for a
+    uniform(-1,1) x, and 20,000 output elements (plus the first and last)
+    recomputed on the host from the oracle's tables, each to 1e-13 of the sum
+    of its terms' magnitudes."""
+    import torch
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    t = L.lieb18()
+    H = make_op(ed, 18, 9, 9, t, t, 4.0)
+    D = H.rows()
+    assert D == 48620 * 48620
+    free, _ = torch.cuda.mem_get_info()
+    if free < 64e9:
+        pytest.skip("needs ~57 GB of free device memory")
+    g = torch.Generator(device="cuda").manual_seed(18)
+    x = torch.empty(D, dtype=torch.float64, device="cuda").uniform_(-1.0, 1.0, generator=g)
+    y = torch.empty_like(x)
+    H.Hubbard_mv(x, y)
+    torch.cuda.synchronize()
+    rng = np.random.default_rng(18)
+    idx = np.concatenate([[0, D - 1], rng.integers(0, D, 20000)])
+    up = orc.Tables(18, 9, t)
+
+    def fetch(i):
+        return x[torch.from_numpy(np.ascontiguousarray(i)).to("cuda")].cpu().numpy()
+
+    ys, scale = orc.sampled_rows(up, up, 4.0, idx, fetch)
+    yg = y[torch.from_numpy(idx).to("cuda")].cpu().numpy()
+    assert np.all(np.abs(yg - ys) <= 1e-13 * scale + 1e-300)
+    H.close()

@@ -10,9 +10,9 @@ import math
 import numpy as np
 import pytest
 
-from conftest import rel_err
+from conftest import philox_uniform, rel_err
 
-SURVEY_E0_CHAIN8 = -4.603526299989137  # dense eigvalsh on the reference tables, L=8 PBC 4+4 U=4
+DENSE_E0_CHAIN8 = -4.603526299989137  # dense eigvalsh on the reference tables, L=8 PBC 4+4 U=4
 
 
 def _digest(state, ax, aj):
@@ -67,7 +67,7 @@ def test_oracle_live_against_reference_build(orc):
 def test_dense_e0_chain8(orc, golden_energies):
     from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
     g = golden_energies["chain8_pbc_q44_U4"]
-    assert abs(g["E0"] - SURVEY_E0_CHAIN8) < 1e-12 * abs(SURVEY_E0_CHAIN8)
+    assert abs(g["E0"] - DENSE_E0_CHAIN8) < 1e-12 * abs(DENSE_E0_CHAIN8)
     t = orc.Tables(8, 4, L.chain(8))
     H = t.sparse()
     import scipy.sparse as sp
@@ -156,3 +156,16 @@ def test_continued_fraction_vs_resolvent(orc):
     g = orc.continued_fraction(a, b, norm2, E, w)
     direct = np.array([phi @ np.linalg.solve((wk + E) * np.eye(H.shape[0]) - H, phi) for wk in w])
     assert np.max(np.abs(g - direct)) < 1e-9 * np.max(np.abs(direct))
+
+
+def test_sampled_rows_match_full_matvec(orc):
+    """oracle.sampled_rows (the check for vectors too large for the host)
+    equals the full restated matvec on the rows it samples."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    eps = list(philox_uniform(11, 8, 2.0))
+    up, dn = orc.Tables(8, 3, L.chain(8)), orc.Tables(8, 5, L.chain(8, eps=eps))
+    x = philox_uniform(5, up.count * dn.count)
+    y = orc.matvec(up, dn, 2.5, x, mask=0b10110111)
+    idx = np.random.default_rng(0).choice(x.size, 300, replace=False)
+    ys, scale = orc.sampled_rows(up, dn, 2.5, idx, lambda i: x[i], mask=0b10110111)
+    assert np.all(np.abs(ys - y[idx]) <= 1e-14 * (scale + 1e-300))
