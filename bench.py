@@ -64,7 +64,8 @@ def max_over_ranks(world, value: float) -> float:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -84,7 +85,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except FileNotFoundError:
             self.proc = None
         return self
@@ -162,7 +163,7 @@ def run_reference(args, world, rank):
     t0 = time.perf_counter()
     orc.lanczos(t, t, U, f, 2, mode="fixed", want_evec=False)
     per = (time.perf_counter() - t0) / 2
-    n = max(2, min(STEPS, int(8.0 / max(per, 1e-6))))
+    n = max(2, min(STEPS, int(min(8.0, args.cpu_seconds) / max(per, 1e-6))))
     for _ in range(args.warmup):
         orc.lanczos(t, t, U, f, 2, mode="fixed", want_evec=False)
     times = []
