@@ -57,6 +57,62 @@ __global__ void k_dot_final(const double* part, int nb, double* out) {
     }
 }
 
+// ------------------------------------------------------------------ S^2 --
+// y = S_xy x with S_xy = (S+S- + S-S+)/2 on the (N_up, N_dn) product basis
+// (TotalSpin/include/HubMatrix_TotalSpin.cuh:20-66):
+//   S_xy = 1/2 sum_i [n_i,up (1 - n_i,dn) + n_i,dn (1 - n_i,up)]
+//          - sum_{i<j} (c+_j,up c_i,up c+_i,dn c_j,dn + h.c.)
+// A spin exchange moves an up particle and a down particle between two
+// singly occupied sites of opposite spin; its fermion sign is (-1)^(number of
+// up and down particles strictly between the two sites), and the term enters
+// as -x for an even count, +x for an odd one.  One thread per element: the
+// exchange partners come from bit operations on the two words and their
+// ranks from the CNS binomial tables (bt[p * kdim + k] = C(p, k)).
+__device__ __forceinline__ int64_t cns_rank_dev(uint64_t w, const int64_t* __restrict__ bt, int kdim) {
+    int64_t r = 0;
+    int k = 0;
+    while (w) {
+        const int p = __ffsll((long long)w) - 1;
+        r += bt[p * kdim + k + 1];
+        ++k;
+        w &= w - 1;
+    }
+    return r;
+}
+
+__global__ void k_sxy(const double* __restrict__ x, double* __restrict__ y, int64_t dimUP, int64_t dimDN, int W,
+                      const uint64_t* __restrict__ stUP, const uint64_t* __restrict__ stDN,
+                      const int64_t* __restrict__ btU, int kdU, const int64_t* __restrict__ btD, int kdD) {
+    const int64_t D = dimUP * dimDN;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < D; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = k / dimDN, d = k - u * dimDN;
+        const uint64_t up = stUP[u], dn = stDN[d];
+        const uint64_t single = up ^ dn;
+        const double half = 0.5 * (double)__popcll(single);
+        double sr = half * x[k * W], si = W == 2 ? half * x[k * W + 1] : 0.0;
+        for (uint64_t a = single & up; a; a &= a - 1) {
+            const int p = __ffsll((long long)a) - 1;
+            for (uint64_t b = single & dn; b; b &= b - 1) {
+                const int q = __ffsll((long long)b) - 1;
+                const uint64_t ex = (1ULL << p) | (1ULL << q);
+                const uint64_t up2 = up ^ ex, dn2 = dn ^ ex;
+                const int i = p < q ? p : q, j = p < q ? q : p;
+                const uint64_t between = ((1ULL << j) - 1ULL) & ~((2ULL << i) - 1ULL);
+                const int nsign = __popcll(up2 & between) + __popcll(dn2 & between);
+                const int64_t kk = cns_rank_dev(up2, btU, kdU) * dimDN + cns_rank_dev(dn2, btD, kdD);
+                const double vr = x[kk * W];
+                sr += (nsign & 1) ? vr : -vr;
+                if (W == 2) {
+                    const double vi = x[kk * W + 1];
+                    si += (nsign & 1) ? vi : -vi;
+                }
+            }
+        }
+        y[k * W] = sr;
+        if (W == 2) y[k * W + 1] = si;
+    }
+}
+
 // y = x - c * p (complex pairs when cplx), c = (cr, ci)
 __global__ void k_project(const double* __restrict__ x, const double* __restrict__ p, const double* __restrict__ c,
                           int64_t n, int cplx, double* __restrict__ y) {
@@ -277,6 +333,77 @@ ed_status ed_vec_zdot(int64_t n, const double* x, const double* y, int mem, doub
         return ED_OK;
     }
     return dev_dot(x, y, n, true, out, reinterpret_cast<cudaStream_t>(stream));
+}
+
+namespace {
+
+// y = S_xy x, both on the device
+ed_status sxy_device(const ed_op* op, const double* x, double* y, cudaStream_t s) {
+    auto table = [](int n, int q, std::vector<int64_t>* bt) {
+        const int kdim = q + 2;
+        bt->assign((size_t)(n + 1) * kdim, 0);
+        for (int p = 0; p <= n; ++p)
+            for (int k = 0; k < kdim; ++k) (*bt)[(size_t)p * kdim + k] = ed::binom(p, k);
+        return kdim;
+    };
+    std::vector<int64_t> tu, td;
+    const int kdU = table(op->n_sites, op->n_up, &tu), kdD = table(op->n_sites, op->n_dn, &td);
+    int64_t* d_bt = nullptr;
+    if (cudaMallocAsync(&d_bt, sizeof(int64_t) * (tu.size() + td.size()), s) != cudaSuccess) return ED_ERR_ALLOC;
+    cudaMemcpyAsync(d_bt, tu.data(), sizeof(int64_t) * tu.size(), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_bt + tu.size(), td.data(), sizeof(int64_t) * td.size(), cudaMemcpyHostToDevice, s);
+    int64_t blocks = (op->D + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    ed::k_sxy<<<(int)std::max<int64_t>(blocks, 1), 256, 0, s>>>(x, y, op->dimUP, op->dimDN, op->cplx ? 2 : 1,
+                                                               op->d_stUP, op->d_stDN, d_bt, kdU,
+                                                               d_bt + tu.size(), kdD);
+    const cudaError_t e = cudaGetLastError();
+    cudaFreeAsync(d_bt, s);
+    return e == cudaSuccess ? ED_OK : ED_ERR_CUDA;
+}
+
+}  // namespace
+
+ed_status ed_s2_apply(ed_op* op, const double* x, double* y, int mem, void* stream) {
+    if (!op || !x || !y || (mem != ED_MEM_HOST && mem != ED_MEM_DEVICE)) return ED_ERR_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int64_t nd = op->D * (op->cplx ? 2 : 1);
+    if (mem == ED_MEM_DEVICE) return sxy_device(op, x, y, s);
+    const double* dx;
+    double* owned;
+    ed_status st = to_device(x, nd, mem, &dx, &owned, s);
+    double* dy = nullptr;
+    if (st == ED_OK && cudaMallocAsync(&dy, sizeof(double) * nd, s) != cudaSuccess) st = ED_ERR_ALLOC;
+    if (st == ED_OK) st = sxy_device(op, dx, dy, s);
+    if (st == ED_OK && cudaMemcpyAsync(y, dy, sizeof(double) * nd, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+        st = ED_ERR_CUDA;
+    if (dy) cudaFreeAsync(dy, s);
+    if (owned) cudaFreeAsync(owned, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess && st == ED_OK) st = ED_ERR_CUDA;
+    return st;
+}
+
+ed_status ed_s2_expect(ed_op* op, const double* psi, int mem, double* out, void* stream) {
+    if (!op || !psi || !out || (mem != ED_MEM_HOST && mem != ED_MEM_DEVICE)) return ED_ERR_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const int64_t nd = op->D * (op->cplx ? 2 : 1);
+    const double* dpsi;
+    double* owned;
+    ed_status st = to_device(psi, nd, mem, &dpsi, &owned, s);
+    double* spsi = nullptr;
+    if (st == ED_OK && cudaMallocAsync(&spsi, sizeof(double) * nd, s) != cudaSuccess) st = ED_ERR_ALLOC;
+    if (st == ED_OK) st = sxy_device(op, dpsi, spsi, s);
+    double r[2] = {0.0, 0.0};
+    if (st == ED_OK) st = dev_dot(dpsi, spsi, op->D, op->cplx, r, s);
+    if (spsi) cudaFreeAsync(spsi, s);
+    if (owned) cudaFreeAsync(owned, s);
+    cudaStreamSynchronize(s);
+    if (st == ED_OK) {
+        const double sz = 0.5 * (op->n_up - op->n_dn);
+        out[0] = r[0];
+        out[1] = sz * sz + r[0];
+    }
+    return st;
 }
 
 ed_status ed_op_expect(ed_op* op, const double* psi, int mem, double* out, void* stream) {

@@ -107,3 +107,27 @@ def entanglement_entropy(op: Hubbard, psi, a_sites: Sequence[int]):
     check(_capi.load().ed_entanglement_entropy(op.handle, p, mem, mask, C.byref(svn), C.byref(sref), None),
           "ed_entanglement_entropy")
     return svn.value, sref.value
+
+
+def s2_apply(op: Hubbard, x):
+    """y = S_xy x, S_xy = (S+S- + S-S+)/2 (TotalSpin::Hubbard::Hubbard_mv):
+    a numpy array in gives a numpy array out, a CUDA tensor a CUDA tensor
+    (on the current stream's device, synchronised)."""
+    p, mem, keep = _mem(x)
+    if mem == _capi.ED_MEM_HOST:
+        y = np.empty(keep.size, dtype=np.float64)
+        check(_capi.load().ed_s2_apply(op.handle, p, C.c_void_p(y.ctypes.data), mem, None), "ed_s2_apply")
+        return y.view(np.complex128) if op.is_complex else y
+    import torch
+    y = torch.empty_like(x)
+    check(_capi.load().ed_s2_apply(op.handle, p, C.c_void_p(y.data_ptr()), mem, None), "ed_s2_apply")
+    torch.cuda.synchronize(y.device)
+    return y
+
+
+def s2_expect(op: Hubbard, psi):
+    """(<S_xy>, S^2) of a normalised psi (S^2 = (N_up - N_dn)^2 / 4 + <S_xy>)."""
+    p, mem, keep = _mem(psi)
+    out = np.zeros(2)
+    check(_capi.load().ed_s2_expect(op.handle, p, mem, C.c_void_p(out.ctypes.data), None), "ed_s2_expect")
+    return float(out[0]), float(out[1])

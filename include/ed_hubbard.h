@@ -225,6 +225,18 @@ ed_status ed_random_vector_device(int64_t n, uint64_t seed, double* out_device, 
  * normalised.  Host output. */
 ed_status ed_random_vector(int64_t n, uint64_t seed, double* out_host);
 
+/* y = S_xy x, S_xy = (S+S- + S-S+)/2, the transverse part of the total spin
+ * on the operator's (N, N_up, N_dn) product basis (TotalSpin::Hubbard::
+ * Hubbard_mv, TotalSpin/include/HubMatrix_TotalSpin.cuh:20-66,120-175).
+ * x, y: rows values (2*rows, interleaved re,im, for complex operators) at
+ * mem; synchronous for host memory, asynchronous on stream otherwise. */
+ed_status ed_s2_apply(ed_op* op, const double* x, double* y, int mem, void* stream);
+
+/* For a normalised psi: out[0] = <psi|S_xy|psi>, out[1] = S^2 =
+ * (N_up - N_dn)^2 / 4 + <S_xy> (ConservedTotalSpin_Kagome_randomHop.cu:
+ * 113-116).  Synchronous. */
+ed_status ed_s2_expect(ed_op* op, const double* psi, int mem, double* out, void* stream);
+
 /* Lowest eigenpair of the symmetric tridiagonal (alpha[0..n-1], off-diagonal
  * beta[0..n-2]): eigenvalue e0 (Sturm bisection to adjacent doubles) and unit
  * eigenvector z (n doubles, inverse iteration, largest component positive;

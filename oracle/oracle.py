@@ -353,3 +353,44 @@ def sampled_rows(up: Tables, dn: Tables, U: float, idx: np.ndarray, fetch, mask:
     y = tu.sum(0) + td.sum(0) + t0
     scale = np.abs(tu).sum(0) + np.abs(td).sum(0) + np.abs(t0)
     return y, scale
+
+
+def sxy_matvec(up: Tables, dn: Tables, x: np.ndarray) -> np.ndarray:
+    """S_xy = (S+S- + S-S+)/2 on the product basis, restated from
+    TotalSpin/include/HubMatrix_TotalSpin.cuh:20-66 (loop over site pairs
+    i < j, vectorised over the basis): for a pair of singly occupied sites of
+    opposite spin the exchanged state contributes -x (even number of
+    particles strictly between i and j in the exchanged words) or +x; the
+    diagonal is popcount(up ^ dn) / 2."""
+    N = up.N
+    su, sd = up.state.astype(np.uint64), dn.state.astype(np.uint64)
+    nu, nd = su.size, sd.size
+    U = np.repeat(su, nd)
+    Dn = np.tile(sd, nu)
+    xv = np.asarray(x).reshape(-1)
+    one = np.uint64(1)
+
+    def bit(w, i):
+        return (w >> np.uint64(i)) & one
+
+    def popc(w):
+        c = np.zeros(w.shape, dtype=np.int64)
+        for b in range(N):
+            c += bit(w, b).astype(np.int64)
+        return c
+
+    y = 0.5 * popc(U ^ Dn) * xv
+    for i in range(N):
+        for j in range(i + 1, N):
+            iup, idn, jup, jdn = bit(U, i), bit(Dn, i), bit(U, j), bit(Dn, j)
+            sel = (iup != idn) & (iup == jdn) & (idn == jup)
+            if not np.any(sel):
+                continue
+            ex = np.uint64((1 << i) | (1 << j))
+            u2, d2 = U[sel] ^ ex, Dn[sel] ^ ex
+            between = np.uint64(((1 << j) - 1) & ~((1 << (i + 1)) - 1))
+            sgn = popc(u2 & between) + popc(d2 & between)
+            k = np.searchsorted(su, u2) * nd + np.searchsorted(sd, d2)
+            v = xv[k]
+            y[np.nonzero(sel)[0]] += np.where(sgn % 2 == 0, -v, v)
+    return y

@@ -147,3 +147,38 @@ def test_flux_response_vs_dense_sum_over_states(ed, orc, flux):
     em = ground(ed, N, q, q, L.kagome12(flux=flux - h), U)[1]
     assert abs((ep - em) / (2 * h) - first) < 1e-6
     assert abs((ep - 2 * e0 + em) / h ** 2 - second) < 1e-4 * max(1.0, abs(second))
+
+
+@pytest.mark.parametrize("case", ["chain8_35", "kagome12_54", "kagome12_22_flux"])
+def test_s2_apply_matches_oracle(ed, orc, case):
+    """ed_s2_apply (TotalSpin::Hubbard::Hubbard_mv) against the restated
+    S_xy on random vectors, real and complex (Peierls) operators, 1e-14 of
+    the vector norms."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    N, qu, qd, t = {"chain8_35": (8, 3, 5, L.chain(8)), "kagome12_54": (12, 5, 4, L.kagome12()),
+                    "kagome12_22_flux": (12, 2, 2, L.kagome12(flux=0.4))}[case]
+    op = ed.Hubbard(ed.H_TBq(N, qu).extend(t), ed.H_TBq(N, qd).extend(t), 2.0)
+    up, dn = orc.Tables(N, qu), orc.Tables(N, qd)
+    rng = np.random.default_rng(7)
+    n = op.rows()
+    x = rng.standard_normal(n) + (1j * rng.standard_normal(n) if op.is_complex else 0)
+    y = ob.s2_apply(op, x)
+    ref = orc.sxy_matvec(up, dn, x.real) + (1j * orc.sxy_matvec(up, dn, x.imag) if op.is_complex else 0)
+    assert np.linalg.norm(y - ref) < 1e-14 * np.linalg.norm(x) * 4
+
+
+def test_s2_of_ground_states(ed):
+    """Total spin of Lanczos ground states (ConservedTotalSpin_Kagome_
+    randomHop.cu:113-116): the half-filled L=8 Hubbard ring is a singlet;
+    Kagome12 5+4 has S^2 = S(S+1) with S half-integer >= 1/2."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    op = ed.Hubbard(ed.H_TBq(8, 4).extend(L.chain(8)), ed.H_TBq(8, 4).extend(L.chain(8)), 4.0)
+    e0, v = ed.Lanczos().eigen(op, max_steps=100, mode="fixed", reorth=True, seed=0)
+    sxy, s2 = ob.s2_expect(op, v)
+    assert abs(s2) < 1e-9 and abs(sxy - s2) < 1e-15
+    op2 = ed.Hubbard(ed.H_TBq(12, 5).extend(L.kagome12()), ed.H_TBq(12, 4).extend(L.kagome12()), 4.0)
+    e0, v = ed.Lanczos().eigen(op2, max_steps=300, mode="fixed", reorth=True, seed=0)
+    sxy, s2 = ob.s2_expect(op2, v)
+    S = (-1 + math.sqrt(1 + 4 * s2)) / 2
+    assert abs(s2 - (0.25 + sxy)) < 1e-14
+    assert abs(2 * S - round(2 * S)) < 1e-6 and round(2 * S) % 2 == 1

@@ -169,3 +169,28 @@ def test_sampled_rows_match_full_matvec(orc):
     idx = np.random.default_rng(0).choice(x.size, 300, replace=False)
     ys, scale = orc.sampled_rows(up, dn, 2.5, idx, lambda i: x[i], mask=0b10110111)
     assert np.all(np.abs(ys - y[idx]) <= 1e-14 * (scale + 1e-300))
+
+
+def test_sxy_oracle_total_spin_multiplets(orc):
+    """The restated S_xy gives S^2 = S(S+1) on exact eigenstates: two sites
+    with one up and one down fermion split into a singlet (S^2 = 0) and the
+    Sz = 0 member of the triplet (S^2 = 2); the half-filled Hubbard chain of
+    4 sites has a singlet ground state; S^2 commutes with H."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    up, dn = orc.Tables(2, 1), orc.Tables(2, 1)
+    S = np.column_stack([orc.sxy_matvec(up, dn, e) for e in np.eye(4)])
+    w = np.linalg.eigvalsh(S)
+    # two doublon singlets, the singlet and the Sz = 0 triplet member of the
+    # singly occupied pair
+    assert np.allclose(w, [0.0, 0.0, 0.0, 2.0])
+    t = L.chain(4)
+    Hu, Hd = orc.Tables(4, 2, t), orc.Tables(4, 2, t)
+    H = orc.hamiltonian(4, 2, 2, t, t, 4.0).toarray()
+    S = np.column_stack([orc.sxy_matvec(Hu, Hd, e) for e in np.eye(H.shape[0])])
+    assert np.max(np.abs(H @ S - S @ H)) < 1e-12
+    ev, V = np.linalg.eigh(H)
+    assert abs(V[:, 0] @ S @ V[:, 0]) < 1e-10
+    # every eigenvalue of S_xy (Sz = 0) is S(S+1)
+    ws = np.linalg.eigvalsh(S)
+    ss = (-1 + np.sqrt(1 + 4 * np.clip(ws, 0, None))) / 2
+    assert np.max(np.abs(ss - np.round(ss))) < 1e-10
