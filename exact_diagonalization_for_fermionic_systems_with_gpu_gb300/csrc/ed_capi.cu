@@ -92,6 +92,47 @@ cudaError_t upload(T** dst, const T* src, size_t n) {
 
 }  // namespace
 
+// Plans and uploads the two-pass matvec when the down index's bandwidth
+// leaves a useful window in shared memory; leaves op->striped false otherwise.
+static ed_status plan_striped(ed_op* op, bool forced) {
+    std::vector<uint32_t> perm, inv;
+    int64_t bw = 0;
+    ed::rcm_order(op->tdn, &perm, &inv, &bw);
+    // window of chunk + 2 bw columns (+ alignment) in at most ~220 KB
+    const int64_t max_win = 220 * 1024 / 8;
+    int64_t chunk = (max_win - 2 * bw - 64) / 1024 * 1024;
+    if (chunk > 16384) chunk = 16384;
+    const int64_t dn_pad = (op->dimDN + 1023) / 1024 * 1024;
+    if (chunk > dn_pad) chunk = dn_pad;
+    if (chunk < 1024) return ED_OK;  // too wide: the generic kernel stays
+    if (!forced && op->dimDN * 8 <= 160 * 1024) return ED_OK;
+    ed::GatherSchedule32 g;
+    std::string err;
+    if (!ed::build_gather_schedule32(op->tdn, perm, inv, &g, &err)) return ED_OK;
+    const int Fc = op->mv.Fc;
+    std::vector<int64_t> dq((size_t)op->dimDN);
+    std::vector<uint64_t> st((size_t)op->dimDN);
+    for (int64_t c = 0; c < op->dimDN; ++c) {
+        dq[c] = (int64_t)std::llrint(std::ldexp(op->tdn.diag_re[perm[c]], Fc));
+        st[c] = op->bdn.state[perm[c]];
+    }
+    if (upload(&op->d_permDN, perm.data(), perm.size()) != cudaSuccess ||
+        upload(&op->d_sched32, g.ent.data(), g.ent.size()) != cudaSuccess ||
+        upload(&op->d_steps32, g.steps32.data(), g.steps32.size()) != cudaSuccess ||
+        upload(&op->d_dDNqP, dq.data(), dq.size()) != cudaSuccess ||
+        upload(&op->d_stDNp, st.data(), st.size()) != cudaSuccess)
+        return ED_ERR_ALLOC;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op->device);
+    op->striped = true;
+    op->st_grid = sms;
+    op->st_bw = bw;
+    op->st_chunk = (int)chunk;
+    op->st_win = (int)(chunk + 2 * bw + 32);
+    op->st_cpad = g.count_pad;
+    return ED_OK;
+}
+
 // The Lanczos workspace pointer rides on the op (opaque to the header).
 struct ed_op_ext : ed_op {
     OpExtra extra;
@@ -361,7 +402,18 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
     // shared memory, else the generic kernel; ED_MATVEC=generic forces the
     // generic kernel (tests compare the two)
     const char* pick = std::getenv("ED_MATVEC");
-    if (!(pick && std::string(pick) == "generic")) op->tma_smem = ed::tma_plan(op, &a);
+    const std::string want = pick ? pick : "";
+    if (want != "generic" && want != "striped") op->tma_smem = ed::tma_plan(op, &a);
+    // sectors whose down rows exceed shared memory: the two-pass matvec over
+    // a bandwidth-reducing order of the down index (ED_MATVEC=striped forces
+    // it where it applies)
+    if (op->tma_smem == 0 && want != "generic" && !cplx && op->mv_fast && op->dimDN % 2 == 0) {
+        const ed_status sst = plan_striped(op, want == "striped");
+        if (sst != ED_OK) {
+            ed_op_destroy(op);
+            return sst;
+        }
+    }
     if (op->tma_smem > 0) {
         op->tma_grid = ed::tma_grid(op);
         std::vector<uint32_t> rs, rl, rq;
@@ -389,6 +441,8 @@ ed_status ed_op_destroy(ed_op* op) {
     cudaFree(op->d_upNpos); cudaFree(op->d_dnNpos);
     cudaFree(op->d_upPtr); cudaFree(op->d_upEntC); cudaFree(op->d_dnPtr); cudaFree(op->d_dnEntC);
     cudaFree(op->d_dnSched); cudaFree(op->d_dnSteps); cudaFree(op->d_rowStart); cudaFree(op->d_rowList); cudaFree(op->d_rowQueue);
+    cudaFree(op->d_permDN); cudaFree(op->d_sched32); cudaFree(op->d_steps32); cudaFree(op->d_dDNqP);
+    cudaFree(op->d_stDNp); cudaFree(op->d_sdn);
     cudaFree(op->d_err);
     cudaFree(op->d_dUPq); cudaFree(op->d_dDNq); cudaFree(op->d_stUP); cudaFree(op->d_stDN);
     cudaFree(op->d_xq); cudaFree(op->d_emax); cudaFree(op->d_flag); cudaFree(op->d_io);

@@ -70,6 +70,22 @@ struct MvArgs {
     int64_t coefDN[2 * kMaxCls];
 };
 
+// Two-pass (striped) matvec for sectors whose down rows exceed shared memory
+// (ed_matvec_striped.cu); the down index is in the op's permuted order.
+struct StripedArgs {
+    const int64_t* xq;        // FX input, permuted order
+    int64_t* sdn;             // int64 down sums (pass D out, pass U in / FP64 out)
+    int64_t dimUP, dimDN;
+    const uint32_t* sched32;  // [steps][cpad] permuted column | sign, kSched32None idle
+    const uint8_t* steps32;
+    int64_t cpad;
+    int64_t bw;               // bandwidth of the permuted down index
+    int chunk;                // columns per pass-D item
+    const int64_t* dDNq;      // folded down diagonal, permuted
+    const uint64_t* stDN;     // down bitstrings, permuted
+    int* err;
+};
+
 }  // namespace ed
 
 struct ed_op {
@@ -107,6 +123,16 @@ struct ed_op {
     bool mv_fast = false;       // at most one coefficient class per spin
     int tma_smem = 0;           // >0: the shared-memory/TMA matvec is used
     int tma_grid = 0;
+    // two-pass matvec (striped): down index permuted by perm (new -> old)
+    bool striped = false;
+    int st_grid = 0, st_win = 0, st_chunk = 0;
+    int64_t st_bw = 0, st_cpad = 0;
+    uint32_t* d_permDN = nullptr;
+    uint32_t* d_sched32 = nullptr;
+    uint8_t* d_steps32 = nullptr;
+    int64_t* d_dDNqP = nullptr;
+    uint64_t* d_stDNp = nullptr;
+    int64_t* d_sdn = nullptr;   // D down sums, allocated on first use
     std::string last_error;
 };
 
@@ -132,5 +158,12 @@ int tma_grid(const ed_op* op);
 void row_plan(const SpinTable& up, int G, std::vector<uint32_t>* start, std::vector<uint32_t>* list,
               std::vector<uint32_t>* queue);
 cudaError_t launch_matvec_tma(const ed_op* op, const MvArgs& a, int out, cudaStream_t s);
+cudaError_t launch_striped_down(const ed_op* op, const StripedArgs& g, cudaStream_t s);
+cudaError_t launch_striped_up(const ed_op* op, const MvArgs& a, const StripedArgs& g, int out, cudaStream_t s);
+cudaError_t launch_permute_f64(const ed_op* op, const double* in, double* out, int forward, cudaStream_t s);
+cudaError_t launch_permute_i64(const ed_op* op, const int64_t* in, int64_t* out, int forward, cudaStream_t s);
+cudaError_t launch_to_fx_perm(const ed_op* op, const double* x, const int* d_emax, int64_t* xq, cudaStream_t s);
+// the striped path's scratch (D int64) and its arguments for input xq
+cudaError_t striped_args(ed_op* op, const int64_t* xq, StripedArgs* g);
 
 }  // namespace ed

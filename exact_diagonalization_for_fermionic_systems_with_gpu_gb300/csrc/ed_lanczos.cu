@@ -483,8 +483,16 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         LZ_CK(launch_random(w->fbuf, DW, cfg->seed, s));
         ++launches;
     }
-    LZ_CK(launch_emax(w->fbuf, DW, w->emax, w->flag, s));
-    k_lz_start<<<lz_grid(DW), kLzThreads, 0, s>>>(w->fbuf, DW, w->emax, w->flag, slot(0), lz);
+    // the two-pass matvec works in its permuted down order: the start vector
+    // is permuted into the u buffer (free until the first matvec)
+    const double* start_vec = w->fbuf;
+    if (op->striped) {
+        LZ_CK(launch_permute_f64(op, w->fbuf, reinterpret_cast<double*>(w->u), 1, s));
+        start_vec = reinterpret_cast<const double*>(w->u);
+        ++launches;
+    }
+    LZ_CK(launch_emax(start_vec, DW, w->emax, w->flag, s));
+    k_lz_start<<<lz_grid(DW), kLzThreads, 0, s>>>(start_vec, DW, w->emax, w->flag, slot(0), lz);
     LZ_CK(cudaGetLastError());
     launches += 2;
 
@@ -661,12 +669,18 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         // one pair of elements per thread where the grid allows
         int64_t gr = (DW / 2 + kLzThreads - 1) / kLzThreads;
         gr = std::max<int64_t>(1, std::min<int64_t>(gr, kLzMaxPartials));
-        k_ritz<<<(int)gr, kLzThreads, 0, s>>>(w->basis, DW, w->stride, n, w->coef_rt, w->coef_rs, F, out, w->ritz_part,
+        // in the two-pass matvec's permuted order the sum goes through u
+        double* rv = op->striped ? reinterpret_cast<double*>(w->u) : out;
+        k_ritz<<<(int)gr, kLzThreads, 0, s>>>(w->basis, DW, w->stride, n, w->coef_rt, w->coef_rs, F, rv, w->ritz_part,
                                         w->ritz_ctr, w->inv_norm);
         LZ_CK(cudaGetLastError());
-        k_scale<<<g, kLzThreads, 0, s>>>(out, DW, w->inv_norm);
+        k_scale<<<g, kLzThreads, 0, s>>>(rv, DW, w->inv_norm);
         LZ_CK(cudaGetLastError());
         launches += 2;
+        if (op->striped) {
+            LZ_CK(launch_permute_f64(op, rv, out, 0, s));
+            ++launches;
+        }
         if (evec_mem != ED_MEM_DEVICE)
             LZ_CK(cudaMemcpyAsync(evec, out, sizeof(double) * DW, cudaMemcpyDeviceToHost, s));
         LZ_CK(cudaStreamSynchronize(s));
@@ -688,8 +702,13 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         LZ_CK(cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s));
         LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
         LZ_CK(cudaMemsetAsync(H.counter, 0, sizeof(unsigned int) * 4, s));
-        LZ_CK(launch_emax(w->fbuf, DW, w->emax, w->flag, s));
-        k_lz_start<<<lz_grid(DW), kLzThreads, 0, s>>>(w->fbuf, DW, w->emax, w->flag, slot(0), lz);
+        const double* sv = w->fbuf;
+        if (op->striped) {
+            LZ_CK(launch_permute_f64(op, w->fbuf, reinterpret_cast<double*>(w->u), 1, s));
+            sv = reinterpret_cast<const double*>(w->u);
+        }
+        LZ_CK(launch_emax(sv, DW, w->emax, w->flag, s));
+        k_lz_start<<<lz_grid(DW), kLzThreads, 0, s>>>(sv, DW, w->emax, w->flag, slot(0), lz);
         LZ_CK(cudaGetLastError());
         // the start vector in fbuf is consumed: fbuf can hold the sum
         double* out = evec_mem == ED_MEM_DEVICE ? evec : w->fbuf;
@@ -711,6 +730,13 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         k_scale<<<g, kLzThreads, 0, s>>>(out, DW, w->inv_norm);
         LZ_CK(cudaGetLastError());
         launches += 2;
+        if (op->striped) {
+            // back to the table order of the down index
+            double* tmp = reinterpret_cast<double*>(w->u);
+            LZ_CK(launch_permute_f64(op, out, tmp, 0, s));
+            LZ_CK(cudaMemcpyAsync(out, tmp, sizeof(double) * DW, cudaMemcpyDeviceToDevice, s));
+            ++launches;
+        }
         if (evec_mem != ED_MEM_DEVICE)
             LZ_CK(cudaMemcpyAsync(evec, out, sizeof(double) * DW, cudaMemcpyDeviceToHost, s));
         int err2 = 0;

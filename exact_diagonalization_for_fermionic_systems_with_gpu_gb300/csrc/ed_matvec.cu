@@ -278,12 +278,35 @@ static cudaError_t launch_mv(const ed_op* op, const MvArgs& a, cudaStream_t s) {
     return op->mv_fast ? launch_mv3<CPLX, OUT, true>(op, a, s) : launch_mv3<CPLX, OUT, false>(op, a, s);
 }
 
+cudaError_t striped_args(ed_op* op, const int64_t* xq, StripedArgs* g) {
+    if (!op->d_sdn) {
+        cudaError_t e = cudaMalloc(&op->d_sdn, sizeof(int64_t) * (size_t)op->D);
+        if (e != cudaSuccess) return e;
+    }
+    g->xq = xq;
+    g->sdn = op->d_sdn;
+    g->dimUP = op->dimUP;
+    g->dimDN = op->dimDN;
+    g->sched32 = op->d_sched32;
+    g->steps32 = op->d_steps32;
+    g->cpad = op->st_cpad;
+    g->bw = op->st_bw;
+    g->chunk = op->st_chunk;
+    g->dDNq = op->d_dDNqP;
+    g->stDN = op->d_stDNp;
+    g->err = op->d_err;
+    return cudaSuccess;
+}
+
 cudaError_t launch_matvec_f64(const ed_op* op, const int64_t* xq, const int* d_emax, double* y,
                               cudaStream_t s) {
     MvArgs a = op->mv;
     a.xq = xq;
     a.p_emax = d_emax;
     a.y = y;
+    // the FP64 apply stays in table order: for one product the two-pass
+    // matvec's permutations in and out cost more than they save (the
+    // Lanczos path, which permutes once per solve, uses it)
     if (op->tma_smem > 0) return launch_matvec_tma(op, a, 0, s);
     return op->cplx ? launch_mv<true, 0>(op, a, s) : launch_mv<false, 0>(op, a, s);
 }
@@ -296,6 +319,13 @@ cudaError_t launch_matvec_lz(const ed_op* op, const int64_t* xq, int64_t* uq, vo
     a.lz = lz;
     a.step = step;
     a.p_mx = d_mx;
+    if (op->striped) {
+        StripedArgs g;
+        cudaError_t e = striped_args(const_cast<ed_op*>(op), xq, &g);
+        if (e == cudaSuccess) e = launch_striped_down(op, g, s);
+        if (e == cudaSuccess) e = launch_striped_up(op, a, g, 1, s);
+        return e;
+    }
     if (op->tma_smem > 0) return launch_matvec_tma(op, a, 1, s);
     return op->cplx ? launch_mv<true, 1>(op, a, s) : launch_mv<false, 1>(op, a, s);
 }

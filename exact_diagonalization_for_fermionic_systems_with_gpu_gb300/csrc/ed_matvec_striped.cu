@@ -1,0 +1,240 @@
+// ed_matvec_striped.cu — two-pass matvec for sectors whose down rows do not
+// fit in shared memory (Lieb18 9+9: 48,620 x 48,620, 18.9 GB per vector), for
+// real operators with one coefficient class per spin.
+//
+// Inside this path the down index is in reverse Cuthill-McKee order (the
+// vectors are permuted on the way in and out), so the down hops of column c
+// stay within +-B of c (B = the order's bandwidth, 8,672 at Lieb18).
+//
+// Pass D (k_mv_down): row-major.  A work item is (row u, chunk of C columns);
+//   the CTA copies the window x[u, c0-B .. c0+C+B) of the row into shared
+//   memory with one bulk copy (consecutive chunks overlap, so most of it
+//   comes from L2) and every column of the chunk sums its down-hop entries
+//   from the window through a conflict-free gather schedule (32-bit words:
+//   permuted column | sign).  Output: the exact int64 down sums S_dn.
+// Pass U (k_mv_up): column stripes of kStripe columns, stripe-major over all
+//   rows so that the stripe of x (dim_up x kStripe x 8 B) stays in L2 while
+//   every row's up neighbours gather from it; a warp computes one row of a
+//   stripe (2 columns per lane, 16-byte loads), adds S_dn and the diagonal,
+//   rounds once, and writes u (FX, Lanczos) or y (FP64, permuted order; the
+//   operator apply keeps the table-order kernels).
+// HBM traffic per matvec: pass D reads x and writes S_dn, pass U reads x,
+// S_dn and writes the result: 5 x 8 B per element (vs 2 x 8 B ideal, and
+// ~14 x 8 B when every up neighbour row is re-read from HBM).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "ed_device.cuh"
+#include "ed_internal.hpp"
+#include "ed_matvec_common.cuh"
+#include "ed_matvec_tma.cuh"
+
+namespace ed {
+using namespace dev;
+
+constexpr int kStripe = 64;        // columns of a pass-U stripe (32 lanes x 2)
+constexpr int kDownThreads = 1024;
+constexpr int kUpThreads = 1024;   // 32 warps: 32 rows of a stripe per item
+
+// ---------------------------------------------------------------- pass D --
+__global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int give_up;
+    int64_t* win = reinterpret_cast<int64_t*>(sm);
+    const int64_t dimDN = g.dimDN;
+    const int64_t nchunk = (dimDN + g.chunk - 1) / g.chunk;
+    const int64_t nitems = g.dimUP * nchunk;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        tma::mbar_init(&bar, 1);
+        tma::fence_mbar_init();
+        give_up = 0;
+    }
+    __syncthreads();
+    uint32_t phase = 0;
+    for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x, phase ^= 1) {
+        const int64_t u = it / nchunk, k = it - u * nchunk;
+        const int64_t c0 = k * g.chunk, c1 = min(c0 + (int64_t)g.chunk, dimDN);
+        const int64_t w0 = max((int64_t)0, c0 - g.bw) & ~(int64_t)15;
+        int64_t w1 = min(dimDN, c1 + g.bw);
+        w1 = (w1 + 1) & ~(int64_t)1;  // dim_dn is even: 16-byte copy sizes
+        if (tid == 0) {
+            tma::fence_proxy_async_smem();
+            const uint32_t bytes = (uint32_t)((w1 - w0) * 8);
+            tma::expect_tx(&bar, bytes);
+            tma::bulk_g2s(win, g.xq + u * dimDN + w0, bytes, &bar);
+        }
+        if (!tma::mbar_wait(&bar, phase)) {
+            if (tid == 0) atomicExch(g.err, 1);
+            give_up = 1;
+        }
+        __syncthreads();
+        if (give_up) return;  // the copy this CTA waited for has given up; none other is in flight
+        for (int64_t c = c0 + tid; c < c1; c += kDownThreads) {
+            const int n = __ldg(g.steps32 + (c >> 5));
+            const uint32_t* sc = g.sched32 + c;
+            int64_t acc = 0;
+#pragma unroll 4
+            for (int s = 0; s < n; ++s) {
+                const uint32_t e = __ldg(sc + (size_t)s * g.cpad);
+                if (e != kSched32None) {
+                    const int64_t v = win[(int64_t)(e & 0x7FFFFFFFu) - w0];
+                    acc += (e & 0x80000000u) ? -v : v;
+                }
+            }
+            g.sdn[u * dimDN + c] = acc;
+        }
+        __syncthreads();  // the window is free for the next copy
+    }
+}
+
+// ---------------------------------------------------------------- pass U --
+// Column-stripe-major items: item = stripe * dim_up + row, one warp each;
+// warp w of CTA b takes items b * 32 + w, + 32 * gridDim.x, ...
+template <int OUT>
+__global__ void __launch_bounds__(kUpThreads, 1) k_mv_up(const MvArgs a, const StripedArgs g) {
+    const int64_t dimUP = g.dimUP, dimDN = g.dimDN;
+    const int64_t nstripe = (dimDN + kStripe - 1) / kStripe;
+    const int64_t nitems = nstripe * dimUP;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t nwarps = (int64_t)gridDim.x * (kUpThreads / 32);
+    const int64_t* __restrict__ xq = g.xq;
+    int E_out = 0, s_u = 0;
+    if (OUT == 0) {
+        E_out = fx_exp_from_emax(*a.p_emax) - a.Fc;
+    } else {
+        const int b = a.bq_bits + bitlen_u64(*a.p_mx) - 62;
+        s_u = b > 0 ? b : 0;
+    }
+    const bool merge = a.mergeUD != 0;
+    const bool unitU = a.unitUP != 0 && a.nclsUP == 1;
+    const bool unitD = a.unitDN != 0 && a.nclsDN == 1;
+    i128 dot = 0;
+    uint64_t mx = 0;
+    for (int64_t it = (int64_t)blockIdx.x * (kUpThreads / 32) + warp; it < nitems; it += nwarps) {
+        const int64_t st = it / dimUP, u = it - st * dimUP;
+        const int64_t c = st * kStripe + lane * 2;  // dim_dn is even: both columns exist
+        if (c >= dimDN) continue;
+        // the row's own values and down sums first: their HBM latency overlaps the gathers
+        const longlong2 dsv = __ldcs(reinterpret_cast<const longlong2*>(g.sdn + u * dimDN + c));
+        const longlong2 xs = __ldcg(reinterpret_cast<const longlong2*>(xq + u * dimDN + c));
+        const uint32_t p0 = __ldg(a.upPtr + u), len = __ldg(a.upPtr + u + 1) - p0;
+        const int npos = (int)__ldg(a.upNpos + u);
+        int64_t sp0 = 0, sp1 = 0, sn0 = 0, sn1 = 0;
+        int k = 0;
+#pragma unroll 4
+        for (; k < npos; ++k) {
+            const int64_t j = __ldg(a.upEntC + p0 + k) & kColMask;
+            const longlong2 v = __ldcg(reinterpret_cast<const longlong2*>(xq + j * dimDN + c));
+            sp0 += v.x;
+            sp1 += v.y;
+        }
+#pragma unroll 4
+        for (; k < (int)len; ++k) {
+            const int64_t j = __ldg(a.upEntC + p0 + k) & kColMask;
+            const longlong2 v = __ldcg(reinterpret_cast<const longlong2*>(xq + j * dimDN + c));
+            sn0 += v.x;
+            sn1 += v.y;
+        }
+        const uint64_t stu = __ldg(a.stUP + u);
+        const int64_t du = __ldg(a.dUPq + u);
+        int64_t oq[2];
+        double of[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int64_t up_sum = q ? sp1 - sn1 : sp0 - sn0;
+            const int64_t dn_sum = q ? dsv.y : dsv.x;
+            const int64_t xv = q ? xs.y : xs.x;
+            i128 ar = 0, ai = 0;
+            if (merge) {
+                apply_class<false>(ar, ai, up_sum + dn_sum, 0, a.coefUP, 0, unitU, a.Fc);
+            } else {
+                if (len) apply_class<false>(ar, ai, up_sum, 0, a.coefUP, 0, unitU, a.Fc);
+                if (a.nclsDN) apply_class<false>(ar, ai, dn_sum, 0, a.coefDN, 0, unitD, a.Fc);
+            }
+            const int64_t dq = du + __ldg(g.dDNq + c + q) + a.Uq * (int64_t)__popcll(stu & __ldg(g.stDN + c + q) & a.mask);
+            ar += mul_wide(dq, xv);
+            if (OUT == 0) {
+                of[q] = i128_to_f64(ar, E_out);
+            } else {
+                oq[q] = shr_round_i64(ar, s_u);
+                dot += mul_wide(xv, oq[q]) >> 24;
+                const uint64_t aq = (uint64_t)(oq[q] < 0 ? -oq[q] : oq[q]);
+                mx = aq > mx ? aq : mx;
+            }
+        }
+        if (OUT == 0) {
+            // the FP64 result overwrites S_dn in place (permuted order)
+            *reinterpret_cast<double2*>(g.sdn + u * dimDN + c) = make_double2(of[0], of[1]);
+        } else {
+            __stcs(reinterpret_cast<longlong2*>(a.uq + u * dimDN + c), make_longlong2(oq[0], oq[1]));
+        }
+    }
+    if (OUT == 1) mv_lanczos_epilogue(a, dot, mx, s_u);
+}
+
+// ---------------------------------------------------- down-index permutes --
+// out[u, c'] = in[u, perm[c']] (forward: table order -> permuted order) or
+// out[u, perm[c']] = in[u, c'] (back).  Grid-stride over elements, so each
+// row's random reads or writes stay within one L2-resident row.
+template <typename T>
+__global__ void k_permute_rows(const T* __restrict__ in, T* __restrict__ out, int64_t dimUP, int64_t dimDN,
+                               const uint32_t* __restrict__ perm, int forward) {
+    const int64_t D = dimUP * dimDN;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = i / dimDN, c = i - u * dimDN;
+        const int64_t p = u * dimDN + __ldg(perm + c);
+        if (forward) out[i] = in[p];
+        else out[p] = in[i];
+    }
+}
+
+// xq[u, c'] = FX(x[u, perm[c']]) at the exponent of d_emax
+__global__ void k_to_fx_perm(const double* __restrict__ x, int64_t dimUP, int64_t dimDN,
+                             const uint32_t* __restrict__ perm, const int* __restrict__ emax, int64_t* __restrict__ xq) {
+    const int E = fx_exp_from_emax(*emax);
+    const int64_t D = dimUP * dimDN;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = i / dimDN, c = i - u * dimDN;
+        xq[i] = f64_to_fx(x[u * dimDN + __ldg(perm + c)], E);
+    }
+}
+
+static int grid_of(int64_t n) {
+    int64_t g = (n + 255) / 256;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(g, 152 * 16));
+}
+
+cudaError_t launch_striped_down(const ed_op* op, const StripedArgs& g, cudaStream_t s) {
+    const int smem = op->st_win * 8;
+    cudaError_t e = cudaFuncSetAttribute(k_mv_down, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_mv_down<<<op->st_grid, kDownThreads, smem, s>>>(g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_striped_up(const ed_op* op, const MvArgs& a, const StripedArgs& g, int out, cudaStream_t s) {
+    if (out == 0) k_mv_up<0><<<op->st_grid, kUpThreads, 0, s>>>(a, g);
+    else k_mv_up<1><<<op->st_grid, kUpThreads, 0, s>>>(a, g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_permute_f64(const ed_op* op, const double* in, double* out, int forward, cudaStream_t s) {
+    k_permute_rows<double><<<grid_of(op->D), 256, 0, s>>>(in, out, op->dimUP, op->dimDN, op->d_permDN, forward);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_permute_i64(const ed_op* op, const int64_t* in, int64_t* out, int forward, cudaStream_t s) {
+    k_permute_rows<int64_t><<<grid_of(op->D), 256, 0, s>>>(in, out, op->dimUP, op->dimDN, op->d_permDN, forward);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_to_fx_perm(const ed_op* op, const double* x, const int* d_emax, int64_t* xq, cudaStream_t s) {
+    k_to_fx_perm<<<grid_of(op->D), 256, 0, s>>>(x, op->dimUP, op->dimDN, op->d_permDN, d_emax, xq);
+    return cudaGetLastError();
+}
+
+}  // namespace ed

@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 
 namespace ed {
@@ -255,6 +256,89 @@ ed_status build_spin(const SpinBasis& basis, const ed_term* terms, int n_terms,
     return ED_OK;
 }
 
+namespace {
+
+struct GroupEdge {
+    int lane, bank;
+    uint32_t word;
+};
+
+// Proper edge colouring of one 16-column group (lanes x bank pairs) with as
+// many colours as the largest degree; pick[c * 16 + l] = edge of lane l in
+// colour c or -1, *free_banks[c] = bank pairs no edge of colour c uses.
+bool colour_group(const std::vector<GroupEdge>& edges, int* Dout, std::vector<int>* pick,
+                  std::vector<int>* free_banks, std::string* err) {
+    constexpr int kL = 16, kB = 16;
+    int degL[kL] = {0}, degB[kB] = {0};
+    for (const GroupEdge& e : edges) {
+        ++degL[e.lane];
+        ++degB[e.bank];
+    }
+    int D = 0;
+    for (int i = 0; i < kL; ++i) D = std::max(D, degL[i]);
+    for (int i = 0; i < kB; ++i) D = std::max(D, degB[i]);
+    std::vector<int> cL((size_t)kL * D, -1), cB((size_t)kB * D, -1), color(edges.size(), -1);
+    auto setc = [&](int e, int c) {
+        color[e] = c;
+        cL[(size_t)edges[e].lane * D + c] = e;
+        cB[(size_t)edges[e].bank * D + c] = e;
+    };
+    for (int e = 0; e < (int)edges.size(); ++e) {
+        const int l = edges[e].lane, b = edges[e].bank;
+        int a = 0, bb = 0;
+        while (cL[(size_t)l * D + a] != -1) ++a;   // free at the lane
+        while (cB[(size_t)b * D + bb] != -1) ++bb; // free at the bank
+        if (cB[(size_t)b * D + a] != -1) {
+            // swap colours a and bb along the alternating path that leaves
+            // bank b on colour a; it cannot reach lane l (no a-edge there)
+            std::vector<int> path;
+            bool at_bank = true;
+            int node = b, c = a;
+            for (;;) {
+                const int pe = at_bank ? cB[(size_t)node * D + c] : cL[(size_t)node * D + c];
+                if (pe == -1) break;
+                path.push_back(pe);
+                node = at_bank ? edges[pe].lane : edges[pe].bank;
+                at_bank = !at_bank;
+                c = (c == a) ? bb : a;
+            }
+            for (int pe : path) {
+                cL[(size_t)edges[pe].lane * D + color[pe]] = -1;
+                cB[(size_t)edges[pe].bank * D + color[pe]] = -1;
+            }
+            for (int pe : path) setc(pe, color[pe] == a ? bb : a);
+        }
+        setc(e, a);
+    }
+    // verify: one entry per lane and per bank pair in every colour
+    pick->assign((size_t)D * kL, -1);
+    free_banks->assign(D, 0);
+    for (int c = 0; c < D; ++c) {
+        int seen = 0;
+        for (int l = 0; l < kL; ++l) {
+            const int e = cL[(size_t)l * D + c];
+            if (e < 0) continue;
+            const int bit = 1 << edges[e].bank;
+            if (seen & bit || color[e] != c) {
+                if (err) *err = "gather schedule: colouring check failed";
+                return false;
+            }
+            seen |= bit;
+            (*pick)[(size_t)c * kL + l] = e;
+        }
+        (*free_banks)[c] = ~seen & 0xFFFF;
+    }
+    for (int e = 0; e < (int)edges.size(); ++e)
+        if (color[e] < 0) {
+            if (err) *err = "gather schedule: uncoloured entry";
+            return false;
+        }
+    *Dout = D;
+    return true;
+}
+
+}  // namespace
+
 bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* err) {
     if (t.complex_coef || t.coef.size() > 1) {
         if (err) *err = "gather schedule: needs a real single-class table";
@@ -269,94 +353,39 @@ bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* e
     const int64_t neg_base = (count + 15) / 16 * 16;
     const int64_t zero_base = 2 * neg_base;
     const int64_t ngroups = cpad / 16;
-    constexpr int kL = 16, kB = 16;
-    struct Edge {
-        int lane, bank;
-        uint16_t word;
-    };
+    constexpr int kL = 16;
     std::vector<std::vector<uint16_t>> group_steps(ngroups);  // [group] -> words by (step*16 + lane)
     std::vector<int> group_deg(ngroups, 0);
     int smax = 0;
     for (int64_t gi = 0; gi < ngroups; ++gi) {
-        std::vector<Edge> edges;
-        int degL[kL] = {0}, degB[kB] = {0};
+        std::vector<GroupEdge> edges;
         for (int l = 0; l < kL; ++l) {
             const int64_t d = gi * 16 + l;
             if (d >= count) continue;
             for (int k = 0; k < t.len[d]; ++k) {
                 const uint32_t e = t.ent[(size_t)k * count + d];
                 const uint32_t col = e & kColMask;
-                const int bank = (int)(col % 16);
-                edges.push_back({l, bank, (uint16_t)(col + ((e & kSignBit) ? neg_base : 0))});
-                ++degL[l];
-                ++degB[bank];
+                edges.push_back({l, (int)(col % 16), (uint32_t)(col + ((e & kSignBit) ? neg_base : 0))});
             }
         }
         int D = 0;
-        for (int i = 0; i < kL; ++i) D = std::max(D, degL[i]);
-        for (int i = 0; i < kB; ++i) D = std::max(D, degB[i]);
-        std::vector<int> cL((size_t)kL * D, -1), cB((size_t)kB * D, -1), color(edges.size(), -1);
-        auto setc = [&](int e, int c) {
-            color[e] = c;
-            cL[(size_t)edges[e].lane * D + c] = e;
-            cB[(size_t)edges[e].bank * D + c] = e;
-        };
-        for (int e = 0; e < (int)edges.size(); ++e) {
-            const int l = edges[e].lane, b = edges[e].bank;
-            int a = 0, bb = 0;
-            while (cL[(size_t)l * D + a] != -1) ++a;   // free at the lane
-            while (cB[(size_t)b * D + bb] != -1) ++bb; // free at the bank
-            if (cB[(size_t)b * D + a] != -1) {
-                // swap colours a and bb along the alternating path that leaves
-                // bank b on colour a; it cannot reach lane l (no a-edge there)
-                std::vector<int> path;
-                bool at_bank = true;
-                int node = b, c = a;
-                for (;;) {
-                    const int pe = at_bank ? cB[(size_t)node * D + c] : cL[(size_t)node * D + c];
-                    if (pe == -1) break;
-                    path.push_back(pe);
-                    node = at_bank ? edges[pe].lane : edges[pe].bank;
-                    at_bank = !at_bank;
-                    c = (c == a) ? bb : a;
-                }
-                for (int pe : path) {
-                    cL[(size_t)edges[pe].lane * D + color[pe]] = -1;
-                    cB[(size_t)edges[pe].bank * D + color[pe]] = -1;
-                }
-                for (int pe : path) setc(pe, color[pe] == a ? bb : a);
-            }
-            setc(e, a);
-        }
-        // verify: one entry per lane and per bank pair in every step; idle
-        // lanes take the zeros of the bank pairs left free
+        std::vector<int> pick, freeb;
+        if (!colour_group(edges, &D, &pick, &freeb, err)) return false;
+        // idle lanes take the zeros of the bank pairs left free
         std::vector<uint16_t> words((size_t)D * kL, 0);
         for (int c = 0; c < D; ++c) {
-            int seen = 0;
+            int fb = freeb[c];
             for (int l = 0; l < kL; ++l) {
-                const int e = cL[(size_t)l * D + c];
-                if (e < 0) continue;
-                const int bit = 1 << edges[e].bank;
-                if (seen & bit || color[e] != c) {
-                    if (err) *err = "gather schedule: colouring check failed";
-                    return false;
+                const int e = pick[(size_t)c * kL + l];
+                if (e >= 0) {
+                    words[(size_t)c * kL + l] = (uint16_t)edges[e].word;
+                } else {
+                    const int b = __builtin_ctz(fb);
+                    fb &= fb - 1;
+                    words[(size_t)c * kL + l] = (uint16_t)(zero_base + b);
                 }
-                seen |= bit;
-                words[(size_t)c * kL + l] = edges[e].word;
-            }
-            int b = 0;
-            for (int l = 0; l < kL; ++l) {
-                if (cL[(size_t)l * D + c] >= 0) continue;
-                while (seen & (1 << b)) ++b;
-                words[(size_t)c * kL + l] = (uint16_t)(zero_base + b);
-                seen |= 1 << b;
             }
         }
-        for (int e = 0; e < (int)edges.size(); ++e)
-            if (color[e] < 0) {
-                if (err) *err = "gather schedule: uncoloured entry";
-                return false;
-            }
         group_steps[gi] = std::move(words);
         group_deg[gi] = D;
         smax = std::max(smax, D);
@@ -372,6 +401,146 @@ bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* e
     g->ent.assign((size_t)std::max(smax, 1) * cpad, 0);
     for (int s2 = 0; s2 < std::max(smax, 1); ++s2)
         for (int64_t d = 0; d < cpad; ++d) g->ent[(size_t)s2 * cpad + d] = (uint16_t)(zero_base + d % 16);
+    g->steps32.assign(cpad / 32, 0);
+    for (int64_t gi = 0; gi < ngroups; ++gi) {
+        const int D = group_deg[gi];
+        for (int c = 0; c < D; ++c)
+            for (int l = 0; l < kL; ++l) g->ent[(size_t)c * cpad + gi * 16 + l] = group_steps[gi][(size_t)c * kL + l];
+        uint8_t& st = g->steps32[gi / 2];
+        st = (uint8_t)std::max<int>(st, D);
+    }
+    return true;
+}
+
+void rcm_order(const SpinTable& t, std::vector<uint32_t>* perm, std::vector<uint32_t>* inv, int64_t* bandwidth) {
+    const int64_t n = t.count;
+    std::vector<std::vector<uint32_t>> adj(n);
+    for (int64_t a = 0; a < n; ++a)
+        for (int k = 0; k < t.len[a]; ++k) {
+            const uint32_t col = t.ent[(size_t)k * n + a] & kColMask;
+            if ((int64_t)col != a) adj[a].push_back(col);
+        }
+    std::vector<int> deg(n);
+    for (int64_t a = 0; a < n; ++a) {
+        std::sort(adj[a].begin(), adj[a].end());
+        adj[a].erase(std::unique(adj[a].begin(), adj[a].end()), adj[a].end());
+        deg[a] = (int)adj[a].size();
+    }
+    std::vector<char> seen(n, 0);
+    std::vector<uint32_t> order;
+    order.reserve(n);
+    // breadth-first levels from s; returns the last level's minimum-degree state
+    auto bfs_far = [&](uint32_t s0) {
+        std::vector<int> lvl(n, -1);
+        std::vector<uint32_t> q{s0};
+        lvl[s0] = 0;
+        size_t h = 0;
+        while (h < q.size()) {
+            const uint32_t v = q[h++];
+            for (uint32_t w : adj[v])
+                if (lvl[w] < 0) {
+                    lvl[w] = lvl[v] + 1;
+                    q.push_back(w);
+                }
+        }
+        const int last = lvl[q.back()];
+        uint32_t best = q.back();
+        for (uint32_t v : q)
+            if (lvl[v] == last && deg[v] < deg[best]) best = v;
+        return best;
+    };
+    for (int64_t s = 0; s < n; ++s) {
+        if (seen[s]) continue;
+        // the component's minimum-degree state, then two sweeps towards the periphery
+        uint32_t start = (uint32_t)s;
+        {
+            std::vector<uint32_t> comp{(uint32_t)s};
+            size_t h = 0;
+            std::vector<char>& vis = seen;  // temporarily mark the component
+            vis[s] = 2;
+            while (h < comp.size()) {
+                const uint32_t v = comp[h++];
+                if (deg[v] < deg[start]) start = v;
+                for (uint32_t w : adj[v])
+                    if (!vis[w]) {
+                        vis[w] = 2;
+                        comp.push_back(w);
+                    }
+            }
+            for (uint32_t v : comp) vis[v] = 0;
+        }
+        start = bfs_far(bfs_far(start));
+        std::vector<uint32_t> q{start};
+        seen[start] = 1;
+        size_t h = 0;
+        while (h < q.size()) {
+            const uint32_t v = q[h++];
+            std::vector<uint32_t> nb;
+            for (uint32_t w : adj[v])
+                if (!seen[w]) {
+                    seen[w] = 1;
+                    nb.push_back(w);
+                }
+            std::stable_sort(nb.begin(), nb.end(), [&](uint32_t x, uint32_t y) { return deg[x] < deg[y]; });
+            q.insert(q.end(), nb.begin(), nb.end());
+        }
+        order.insert(order.end(), q.begin(), q.end());
+    }
+    std::reverse(order.begin(), order.end());
+    perm->assign(order.begin(), order.end());
+    inv->assign(n, 0);
+    for (int64_t i = 0; i < n; ++i) (*inv)[(*perm)[i]] = (uint32_t)i;
+    int64_t bw = 0;
+    for (int64_t a = 0; a < n; ++a)
+        for (uint32_t b : adj[a]) bw = std::max<int64_t>(bw, std::llabs((int64_t)(*inv)[a] - (int64_t)(*inv)[b]));
+    *bandwidth = bw;
+}
+
+bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
+                             GatherSchedule32* g, std::string* err) {
+    if (t.complex_coef || t.coef.size() > 1) {
+        if (err) *err = "gather schedule: needs a real single-class table";
+        return false;
+    }
+    const int64_t count = t.count;
+    const int64_t cpad = (count + 31) / 32 * 32;
+    const int64_t ngroups = cpad / 16;
+    constexpr int kL = 16;
+    std::vector<std::vector<uint32_t>> group_steps(ngroups);
+    std::vector<int> group_deg(ngroups, 0);
+    int smax = 0;
+    for (int64_t gi = 0; gi < ngroups; ++gi) {
+        std::vector<GroupEdge> edges;
+        for (int l = 0; l < kL; ++l) {
+            const int64_t c = gi * 16 + l;  // permuted column
+            if (c >= count) continue;
+            const int64_t d = perm[c];      // its state in table order
+            for (int k = 0; k < t.len[d]; ++k) {
+                const uint32_t e = t.ent[(size_t)k * count + d];
+                const uint32_t tc = inv[e & kColMask];
+                edges.push_back({l, (int)(tc % 16), tc | (e & kSignBit)});
+            }
+        }
+        int D = 0;
+        std::vector<int> pick, freeb;
+        if (!colour_group(edges, &D, &pick, &freeb, err)) return false;
+        std::vector<uint32_t> words((size_t)D * kL, kSched32None);
+        for (int c = 0; c < D; ++c)
+            for (int l = 0; l < kL; ++l) {
+                const int e = pick[(size_t)c * kL + l];
+                if (e >= 0) words[(size_t)c * kL + l] = edges[e].word;
+            }
+        group_steps[gi] = std::move(words);
+        group_deg[gi] = D;
+        smax = std::max(smax, D);
+    }
+    if (smax > 255) {
+        if (err) *err = "gather schedule: more than 255 steps";
+        return false;
+    }
+    g->steps = smax;
+    g->count_pad = cpad;
+    g->ent.assign((size_t)std::max(smax, 1) * cpad, kSched32None);
     g->steps32.assign(cpad / 32, 0);
     for (int64_t gi = 0; gi < ngroups; ++gi) {
         const int D = group_deg[gi];

@@ -103,6 +103,30 @@ struct GatherSchedule {
 // classes, more than kSchedMaxCount states, or more than 255 steps.
 bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* err);
 
+// Reverse Cuthill-McKee order of a table's hop graph (breadth-first from a
+// pseudo-peripheral state, neighbours by increasing degree, reversed; every
+// connected component in turn): perm[new] = old, inv[old] = new, and the
+// bandwidth max |inv[a] - inv[b]| over the table's entries.  With this order
+// the hops of a state stay within +-bandwidth of it.
+void rcm_order(const SpinTable& t, std::vector<uint32_t>* perm, std::vector<uint32_t>* inv, int64_t* bandwidth);
+
+// Conflict-free gather schedule over permuted columns for the two-pass
+// matvec: column c' = inv[d] of the permuted table reads its entries
+// (targets inv[col]) one per step, 32-bit words col' | sign << 31, idle
+// lanes kSched32None; bank pair of a target = col' % 16 (the kernel's
+// windows start at multiples of 16).
+constexpr uint32_t kSched32None = 0xFFFFFFFFu;
+
+struct GatherSchedule32 {
+    int steps = 0;
+    int64_t count_pad = 0;         // count rounded up to 32 (row stride of ent)
+    std::vector<uint32_t> ent;     // ent[s * count_pad + c']
+    std::vector<uint8_t> steps32;  // steps the warp of 32-column block k runs
+};
+
+bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
+                             GatherSchedule32* g, std::string* err);
+
 // Build both layouts for one spin from a term list.  Returns ED_OK or an
 // error (bad site, table overflow, complex term in a real operator when
 // allow_complex is false).

@@ -5,6 +5,7 @@
 // the per-block step counts cover the entries.  Prints one line
 // per case: "<name> count <n> max_len <L> steps <S> ok".
 #include <cstdio>
+#include <algorithm>
 #include <cstdlib>
 #include <map>
 #include <string>
@@ -70,7 +71,70 @@ static int check(const char* name, int n, int q, const std::vector<ed_term>& ter
             }
         }
     }
-    std::printf("%s count %lld max_len %d steps %d ok\n", name, (long long)cnt, t.max_len, g.steps);
+    // the reverse Cuthill-McKee order and the permuted 32-bit schedule
+    std::vector<uint32_t> perm, inv;
+    int64_t bw = 0;
+    rcm_order(t, &perm, &inv, &bw);
+    std::vector<char> hit(cnt, 0);
+    for (int64_t c = 0; c < cnt; ++c) {
+        if (perm[c] >= cnt || hit[perm[c]] || inv[perm[c]] != c) {
+            std::printf("%s rcm order is not a permutation\n", name);
+            return 1;
+        }
+        hit[perm[c]] = 1;
+    }
+    GatherSchedule32 g32;
+    if (!build_gather_schedule32(t, perm, inv, &g32, &err)) {
+        std::printf("%s schedule32 failed: %s\n", name, err.c_str());
+        return 1;
+    }
+    int64_t bw_seen = 0;
+    for (int64_t c = 0; c < g32.count_pad; ++c) {
+        std::map<int64_t, int> want, got;
+        if (c < cnt) {
+            const int64_t d = perm[c];
+            for (int k = 0; k < t.len[d]; ++k) {
+                const uint32_t e = t.ent[(size_t)k * cnt + d];
+                const int64_t tc = (int64_t)inv[e & kColMask] + 1;
+                ++want[(e & kSignBit) ? -tc : tc];
+                bw_seen = std::max<int64_t>(bw_seen, std::llabs((int64_t)inv[e & kColMask] - c));
+            }
+        }
+        for (int s = 0; s < g32.steps; ++s) {
+            const uint32_t w = g32.ent[(size_t)s * g32.count_pad + c];
+            if (w == kSched32None) continue;
+            if (s >= g32.steps32[c / 32]) {
+                std::printf("%s schedule32 entry beyond the block's steps\n", name);
+                return 1;
+            }
+            const int64_t tc = (int64_t)(w & 0x7FFFFFFFu) + 1;
+            ++got[(w & 0x80000000u) ? -tc : tc];
+        }
+        if (want != got) {
+            std::printf("%s schedule32 column %lld differs from the table\n", name, (long long)c);
+            return 1;
+        }
+    }
+    for (int64_t g0 = 0; g0 < g32.count_pad; g0 += 16)
+        for (int s = 0; s < g32.steps; ++s) {
+            int seen = 0;
+            for (int l = 0; l < 16; ++l) {
+                const uint32_t w = g32.ent[(size_t)s * g32.count_pad + g0 + l];
+                if (w == kSched32None) continue;
+                const int bit = 1 << ((w & 0x7FFFFFFFu) % 16);
+                if (seen & bit) {
+                    std::printf("%s schedule32 bank conflict\n", name);
+                    return 1;
+                }
+                seen |= bit;
+            }
+        }
+    if (bw_seen > bw) {
+        std::printf("%s rcm bandwidth %lld below an entry's distance %lld\n", name, (long long)bw, (long long)bw_seen);
+        return 1;
+    }
+    std::printf("%s count %lld max_len %d steps %d rcm_bandwidth %lld steps32 %d ok\n", name, (long long)cnt, t.max_len,
+                g.steps, (long long)bw, g32.steps);
     return 0;
 }
 

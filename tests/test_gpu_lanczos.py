@@ -229,3 +229,24 @@ def test_ritz_recompute_matches_stored(ed, monkeypatch, case):
     assert e1 == e2 and l1.a == l2.a and l1.b == l2.b
     assert np.linalg.norm(v1 - v2) < 1e-12
     assert abs(np.linalg.norm(v2) - 1.0) < 1e-13
+
+
+@pytest.mark.parametrize("ritz", ["stored", "recompute"])
+def test_two_pass_matvec_lanczos_ritz_vector(ed, monkeypatch, ritz):
+    """The two-pass matvec runs Lanczos in a permuted down order; start and
+    Ritz vectors are permuted on the way in and out, so T, E0 and the Ritz
+    vector equal the generic kernel's (the vector to its last bits: only the
+    order of the FP64 norm sum differs)."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    runs = {}
+    for kind in ("striped", "generic"):
+        monkeypatch.setenv("ED_MATVEC", kind)
+        op = op_for(ed, 12, 6, 6, L.kagome12(), L.kagome12(), 8.0)
+        lz = ed.Lanczos()
+        e0, v = lz.eigen(op, max_steps=150, mode="fixed", ritz=ritz, seed=5)
+        runs[kind] = (lz.a, lz.b, e0, v)
+        op.close()
+    monkeypatch.delenv("ED_MATVEC")
+    s, g = runs["striped"], runs["generic"]
+    assert s[0] == g[0] and s[1] == g[1] and s[2] == g[2]
+    assert np.max(np.abs(s[3] - g[3])) < 1e-15

@@ -176,13 +176,13 @@ def kernel_cases():
 
 @pytest.mark.parametrize("case", kernel_cases(), ids=lambda c: c[0])
 def test_matvec_kernels_agree_bit_for_bit(ed, monkeypatch, case):
-    """The row-staged TMA kernel and the generic kernel compute the same exact
-    integer sums: their outputs and Lanczos coefficients agree bit for bit
-    (operators whose down table does not fit shared memory take the generic
-    kernel either way)."""
+    """The row-staged TMA kernel, the two-pass (striped) kernel over the
+    permuted down index and the generic kernel compute the same exact integer
+    sums: their outputs and Lanczos coefficients agree bit for bit (an
+    operator a kernel does not take falls through to the next one)."""
     name, N, qu, qd, ut, dt, U = case
     ops = {}
-    for kind in ("", "generic"):
+    for kind in ("", "striped", "generic"):
         if kind:
             monkeypatch.setenv("ED_MATVEC", kind)
         ops[kind or "auto"] = make_op(ed, N, qu, qd, ut, dt, U)
@@ -193,12 +193,13 @@ def test_matvec_kernels_agree_bit_for_bit(ed, monkeypatch, case):
     x = rng.standard_normal(n) + (1j * rng.standard_normal(n) if cplx else 0)
     ys = {k: op.matvec(x) for k, op in ops.items()}
     assert np.array_equal(ys["auto"], ys["generic"])
+    assert np.array_equal(ys["striped"], ys["generic"])
     runs = {}
     for k, op in ops.items():
         lz = ed.Lanczos()
         e, _ = lz.eigen(op, max_steps=min(30, n), mode="fixed", ritz="none", seed=4)
         runs[k] = (lz.a, lz.b, e)
-    assert runs["auto"] == runs["generic"]
+    assert runs["auto"] == runs["generic"] and runs["striped"] == runs["generic"]
 
 
 def test_lieb18_full_size_sampled_rows(ed, orc):
@@ -232,3 +233,26 @@ def test_lieb18_full_size_sampled_rows(ed, orc):
     yg = y[torch.from_numpy(idx).to("cuda")].cpu().numpy()
     assert np.all(np.abs(yg - ys) <= 1e-13 * scale + 1e-300)
     H.close()
+
+
+def test_lieb18_two_pass_lanczos_matches_generic(ed, monkeypatch):
+    """At full Lieb18 9+9 size the Lanczos recurrence through the two-pass
+    matvec (permuted down index, L2-striped up term) gives the same alpha and
+    beta, bit for bit, as through the generic kernel (4 steps each)."""
+    import torch
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    free, _ = torch.cuda.mem_get_info()
+    if free < 140e9:
+        pytest.skip("needs ~130 GB of free device memory")
+    t = L.lieb18()
+    runs = {}
+    for kind in ("", "generic"):
+        if kind:
+            monkeypatch.setenv("ED_MATVEC", kind)
+        op = make_op(ed, 18, 9, 9, t, t, 4.0)
+        lz = ed.Lanczos()
+        lz.eigen(op, max_steps=4, mode="fixed", ritz="none", seed=1)
+        runs[kind or "auto"] = (lz.a, lz.b)
+        op.close()
+        monkeypatch.delenv("ED_MATVEC", raising=False)
+    assert runs["auto"] == runs["generic"]
