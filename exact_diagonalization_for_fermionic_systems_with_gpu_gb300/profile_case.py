@@ -8,9 +8,11 @@
                  timed with device timestamps
 --what solve   : the same solve without timing hooks (what bench.py runs)
 --what perform : --steps operator applies through the FP64 C-ABI path
-Cases: kagome12 (6+6, dim 853,776, L2-resident vectors), chain14 (7+7 open
-chain with disorder, dim 11,778,624, vectors larger than L2), lieb18
-(9+9, dim 2.36e9; perform only, ~57 GB of device memory).
+Cases: kagome12 (6+6, dim 853,776, L2-resident vectors), kagome12_flux
+(complex, Peierls phases), chain12_66 / chain12_75 / chain12_84 (open L=12
+chain, W=6 disorder, the three sectors of the MBL sweep), chain14 (7+7 open
+chain with disorder, dim 11,778,624, vectors larger than L2), lieb18 (9+9,
+dim 2.36e9, ~100 GB of device memory for a Lanczos run).
 """
 from __future__ import annotations
 
@@ -39,6 +41,11 @@ def build_case(name: str):
     if name == "kagome12_flux":
         t = L.kagome12(flux=0.3)
         return Hubbard(H_TBq(12, 6).extend(t), H_TBq(12, 6).extend(t), 4.0)
+    if name.startswith("chain12_"):  # chain12_66 / chain12_75 / chain12_84: open L=12, W=6, U=1
+        qu, qd = int(name[-2]), int(name[-1])
+        eps = random_vector(12, 100) * 6.0
+        t = L.chain(12, periodic=False, eps=eps)
+        return Hubbard(H_TBq(12, qu).extend(t), H_TBq(12, qd).extend(t), 1.0)
     raise SystemExit(f"unknown case {name}")
 
 
