@@ -65,6 +65,15 @@ class ed_kubo_result(C.Structure):
     _fields_ = [("drude", C.c_double), ("kinetic", C.c_double), ("vertex", C.c_double)]
 
 
+class ed_krylov_cfg(C.Structure):
+    _fields_ = [("max_steps", C.c_int32), ("reorth", C.c_int32), ("tol", C.c_double)]
+
+
+class ed_krylov_result(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("runs", C.c_int32), ("norm", C.c_double), ("err_est", C.c_double),
+                ("launches", C.c_int64)]
+
+
 # name -> (restype, argtypes); the list is also the export check used by the tests
 SIGNATURES = {
     "ed_status_string": (C.c_char_p, [C.c_int]),
@@ -105,6 +114,10 @@ SIGNATURES = {
                               C.c_void_p, C.c_void_p]),
     "ed_entanglement_entropy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),
+    "ed_tridiag_eigen": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ed_tridiag_expm": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "ed_krylov_evolve": (C.c_int, [C.c_void_p, C.POINTER(ed_krylov_cfg), C.c_void_p, C.c_int, C.c_int, C.c_void_p,
+                                   C.c_void_p, C.c_int, C.POINTER(ed_krylov_result), C.c_void_p]),
 }
 
 

@@ -15,9 +15,7 @@
 #include "ed_internal.hpp"
 
 namespace ed {
-ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, const double* start, int start_mem,
-                      double* evec, int evec_mem, double* alpha_h, double* beta_h, ed_lanczos_result* res,
-                      cudaStream_t s);
+
 void lanczos_free_ws(void* p);
 cudaError_t launch_random(double* f, int64_t n, uint64_t seed, cudaStream_t s);
 
@@ -137,6 +135,10 @@ static ed_status plan_striped(ed_op* op, bool forced) {
 struct ed_op_ext : ed_op {
     OpExtra extra;
 };
+
+namespace ed {
+void** lanczos_ws_slot(ed_op* op) { return &static_cast<ed_op_ext*>(op)->extra.lz_ws; }
+}  // namespace ed
 
 extern "C" {
 
@@ -533,6 +535,32 @@ ed_status ed_tridiag_lowest(int n, const double* alpha, const double* offdiag, d
     if (n < 1 || !alpha || (n > 1 && !offdiag) || !e0) return ED_ERR_ARG;
     *e0 = ed::tridiag_lowest_host(n, alpha, offdiag, z);
     return ED_OK;
+}
+
+ed_status ed_tridiag_eigen(int n, const double* alpha, const double* offdiag, double* evals, double* z) {
+    if (n < 1 || !alpha || (n > 1 && !offdiag) || !evals) return ED_ERR_ARG;
+    std::vector<double> m;
+    std::vector<ed::TriRot> rots;
+    if (!ed::tridiag_eigen_rotations(n, alpha, offdiag, &m, &rots)) return ED_ERR_BREAKDOWN;
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return m[x] < m[y]; });
+    std::vector<double> col(n);
+    for (int j = 0; j < n; ++j) {
+        evals[j] = m[order[j]];
+        if (!z) continue;
+        std::fill(col.begin(), col.end(), 0.0);
+        col[order[j]] = 1.0;
+        ed::tri_apply_z(rots, col.data());
+        std::copy(col.begin(), col.end(), z + (size_t)j * n);
+    }
+    return ED_OK;
+}
+
+ed_status ed_tridiag_expm(int n, const double* alpha, const double* offdiag, int n_times, const double* times,
+                          double* out) {
+    if (n < 1 || !alpha || (n > 1 && !offdiag) || n_times < 0 || (n_times && (!times || !out))) return ED_ERR_ARG;
+    return ed::tridiag_expm_e0(n, alpha, offdiag, n_times, times, out) ? ED_OK : ED_ERR_BREAKDOWN;
 }
 
 }  // extern "C"

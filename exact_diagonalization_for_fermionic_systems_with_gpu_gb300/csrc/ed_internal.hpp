@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/ed_hubbard.h"
 #include "ed_tables.hpp"
 
 namespace ed {
@@ -165,5 +166,15 @@ cudaError_t launch_permute_i64(const ed_op* op, const int64_t* in, int64_t* out,
 cudaError_t launch_to_fx_perm(const ed_op* op, const double* x, const int* d_emax, int64_t* xq, cudaStream_t s);
 // the striped path's scratch (D int64) and its arguments for input xq
 cudaError_t striped_args(ed_op* op, const int64_t* xq, StripedArgs* g);
+
+// Lanczos recurrence (ed_lanczos.cu); stop_beta >= 0 ends it at the first
+// beta_k < stop_beta * beta_0 (Krylov time evolution).
+ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, const double* start, int start_mem,
+                      double* evec, int evec_mem, double* alpha_h, double* beta_h, ed_lanczos_result* res,
+                      cudaStream_t s, double stop_beta = -1.0);
+// The op's Lanczos workspace slot, and the stored basis of its last run:
+// slot k at basis + k * stride holds q_k with w_k = q_k 2^e[k] (e on the device).
+void** lanczos_ws_slot(ed_op* op);
+void lanczos_basis(void* ws_slot, const int64_t** basis, int64_t* stride, const int** e_dev);
 
 }  // namespace ed

@@ -442,9 +442,19 @@ void lanczos_free_ws(void* p) {
     delete h;
 }
 
+void lanczos_basis(void* ws_slot, const int64_t** basis, int64_t* stride, const int** e_dev) {
+    Workspace* w = &reinterpret_cast<WsHolder*>(ws_slot)->ws;
+    *basis = w->basis;
+    *stride = w->stride;
+    *e_dev = w->h.e;
+}
+
+// stop_beta >= 0: Krylov use (time evolution): the run ends at the first
+// beta_k < stop_beta * beta_0 (tested every ten steps like the reference
+// mode's stop test) and T is k x k.
 ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, const double* start, int start_mem,
                       double* evec, int evec_mem, double* alpha_h, double* beta_h, ed_lanczos_result* res,
-                      cudaStream_t s) {
+                      cudaStream_t s, double stop_beta) {
     if (!cfg || cfg->max_steps < 1 || cfg->max_steps > 100000) return ED_ERR_ARG;
     const int W = op->cplx ? 2 : 1;
     const int64_t DW = op->D * W;
@@ -520,7 +530,9 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     int j = 0;
     while (j < max_steps) {
         if (fused) {
-            const int j1 = cfg->mode == ED_LANCZOS_REFERENCE ? std::min(max_steps, (j / 10 + 1) * 10) : max_steps;
+            const int j1 = (cfg->mode == ED_LANCZOS_REFERENCE || stop_beta >= 0.0)
+                               ? std::min(max_steps, (j / 10 + 1) * 10)
+                               : max_steps;
             LZ_CK(cudaMemsetAsync(w->gbar, 0, kFusedSync, s));
             LzRedSet* red = reinterpret_cast<LzRedSet*>(reinterpret_cast<char*>(w->gbar) + 32);
             if (stamps) {
@@ -606,6 +618,15 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             ++j;
         }
         steps_run = j;
+        if (stop_beta >= 0.0 && j % 10 == 0 && j < max_steps) {
+            LZ_CK(cudaMemcpyAsync(hb.data(), H.beta, sizeof(double) * (j + 1), cudaMemcpyDeviceToHost, s));
+            LZ_CK(cudaMemcpyAsync(&status_dev, &lz->status, sizeof(int), cudaMemcpyDeviceToHost, s));
+            LZ_CK(cudaStreamSynchronize(s));
+            if (status_dev != 0) { n = j; break; }
+            bool small = false;
+            for (int k = 1; k <= j; ++k) small = small || hb[k] < stop_beta * hb[0];
+            if (small) { n = j; break; }
+        }
         if (cfg->mode == ED_LANCZOS_REFERENCE && j % 10 == 0) {
             const int nn = j;
             LZ_CK(cudaMemcpyAsync(ha.data(), H.alpha, sizeof(double) * nn, cudaMemcpyDeviceToHost, s));
@@ -647,6 +668,9 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     } else if (status != 0) {
         return ED_ERR_NONFINITE;
     }
+    if (stop_beta >= 0.0)
+        for (int k = 1; k < n; ++k)
+            if (hb[k] < stop_beta * hb[0]) { n = k; break; }
     tri[0] = tridiag_lowest_host(n, ha.data(), hb.data() + 1, tri.data() + 1);
     e0 = tri[0];
     resid = std::fabs(hb[n] * tri[n]);

@@ -136,4 +136,108 @@ double tridiag_lowest_host(int n, const double* a, const double* off, double* z)
     return lam;
 }
 
+// ----------------------------------------------------------------------------
+// All eigenpairs: implicit symmetric tridiagonal QR with the Wilkinson shift
+// (Golub & Van Loan, Matrix Computations, 4th ed., Algorithms 8.3.2-8.3.3):
+// each step chases the bulge of one shifted rotation down the unreduced block
+// [l, m]; off-diagonals below eps (|a_i| + |a_{i+1}|) deflate.  The rotations
+// G_1 .. G_K (plane (k, k+1), [[c, s], [-s, c]]) are recorded in order, so
+// Z = G_1 G_2 ... G_K holds the eigenvectors as columns and Z^T T Z = diag(m).
+// Applying the rotations to one vector costs O(K) = O(n^2) instead of the
+// O(n^3) of forming Z; this is what the Krylov propagator needs
+// (exp(-i T t) e_0 = Z exp(-i diag(m) t) Z^T e_0, HubMatrix_GPU.cuh:684-690).
+bool tridiag_eigen_rotations(int n, const double* a_in, const double* off, std::vector<double>* evals,
+                             std::vector<TriRot>* rots) {
+    std::vector<double> a(a_in, a_in + n), b(std::max(n - 1, 0));
+    for (int i = 0; i + 1 < n; ++i) b[i] = off[i];
+    rots->clear();
+    const double eps = std::numeric_limits<double>::epsilon();
+    int m = n - 1;
+    long long iters = 0;
+    const long long max_iters = 60LL * std::max(n, 1);
+    while (m > 0) {
+        if (std::fabs(b[m - 1]) <= eps * (std::fabs(a[m - 1]) + std::fabs(a[m]))) {
+            b[m - 1] = 0.0;
+            --m;
+            continue;
+        }
+        int l = m - 1;
+        while (l > 0 && std::fabs(b[l - 1]) > eps * (std::fabs(a[l - 1]) + std::fabs(a[l]))) --l;
+        if (l > 0) b[l - 1] = 0.0;
+        if (++iters > max_iters) return false;
+        // Wilkinson shift from the trailing 2x2 of the block
+        const double d = 0.5 * (a[m - 1] - a[m]);
+        const double bb = b[m - 1];
+        const double den = d + (d >= 0.0 ? 1.0 : -1.0) * std::hypot(d, bb);
+        const double mu = den != 0.0 ? a[m] - bb * bb / den : a[m] - std::fabs(bb);
+        double x = a[l] - mu, z = b[l];
+        for (int k = l; k < m; ++k) {
+            // rotation in plane (k, k+1) that zeroes z against x
+            double r = std::hypot(x, z);
+            double c = 1.0, s = 0.0;
+            if (r != 0.0) {
+                c = x / r;
+                s = -z / r;
+            }
+            if (k > l) b[k - 1] = r;  // the bulge at (k-1, k+1) is gone
+            const double ak = a[k], ak1 = a[k + 1], e = b[k];
+            a[k] = c * c * ak - 2.0 * c * s * e + s * s * ak1;
+            a[k + 1] = s * s * ak + 2.0 * c * s * e + c * c * ak1;
+            b[k] = c * s * (ak - ak1) + (c * c - s * s) * e;
+            rots->push_back(TriRot{k, c, s});
+            if (k + 1 < m) {
+                const double f = b[k + 1];
+                z = -s * f;  // new bulge at (k, k+2)
+                b[k + 1] = c * f;
+                x = b[k];
+            }
+        }
+    }
+    evals->assign(a.begin(), a.end());
+    return true;
+}
+
+// v <- Z^T v: G_1^T first
+void tri_apply_zt(const std::vector<TriRot>& rots, double* v) {
+    for (const TriRot& g : rots) {
+        const double x = v[g.k], y = v[g.k + 1];
+        v[g.k] = g.c * x - g.s * y;
+        v[g.k + 1] = g.s * x + g.c * y;
+    }
+}
+
+// v <- Z v: G_K first
+void tri_apply_z(const std::vector<TriRot>& rots, double* v) {
+    for (auto it = rots.rbegin(); it != rots.rend(); ++it) {
+        const TriRot& g = *it;
+        const double x = v[g.k], y = v[g.k + 1];
+        v[g.k] = g.c * x + g.s * y;
+        v[g.k + 1] = -g.s * x + g.c * y;
+    }
+}
+
+bool tridiag_expm_e0(int n, const double* a, const double* off, int n_times, const double* times, double* out) {
+    std::vector<double> m;
+    std::vector<TriRot> rots;
+    if (!tridiag_eigen_rotations(n, a, off, &m, &rots)) return false;
+    std::vector<double> y(n, 0.0), re(n), im(n);
+    y[0] = 1.0;
+    tri_apply_zt(rots, y.data());
+    for (int t = 0; t < n_times; ++t) {
+        for (int j = 0; j < n; ++j) {
+            const double ph = m[j] * times[t];
+            re[j] = std::cos(ph) * y[j];
+            im[j] = -std::sin(ph) * y[j];
+        }
+        tri_apply_z(rots, re.data());
+        tri_apply_z(rots, im.data());
+        double* o = out + (size_t)2 * n * t;
+        for (int k = 0; k < n; ++k) {
+            o[2 * k] = re[k];
+            o[2 * k + 1] = im[k];
+        }
+    }
+    return true;
+}
+
 }  // namespace ed

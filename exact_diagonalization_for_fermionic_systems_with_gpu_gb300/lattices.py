@@ -50,15 +50,17 @@ def chain(L: int, t: float = -1.0, periodic: bool = True, eps: Sequence[float] |
     return terms
 
 
-def kagome12(rand: Sequence[float] | None = None, onsite_shift: bool = True, flux: float = 0.0) -> List[Term]:
+def kagome12(rand: Sequence[float] | None = None, onsite_shift: bool = True, flux: float = 0.0,
+             peierls: bool = False) -> List[Term]:
     """KagomeLattice12 (drude_v2_cal_Kagome_randomHop.cu:794-808): hopping
     -r_i r_j on the 24 bonds and, with onsite_shift, Make_N(i, -2 r_i^2).
-    With flux != 0 every bond carries the Peierls phase flux * dx_b."""
+    With flux != 0 (or peierls=True, which keeps the operator complex at
+    flux 0) every bond carries the Peierls phase flux * dx_b."""
     r = [1.0] * 12 if rand is None else list(rand)
     terms: List[Term] = []
     for b, (i, j) in enumerate(zip(KAGOME12_FIRST, KAGOME12_SECOND)):
         t = -r[i] * r[j]
-        if flux != 0.0:
+        if flux != 0.0 or peierls:
             terms.append(("P", i, j, t, flux * KAGOME12_DX[b]))
         else:
             terms.append(("H", i, j, t, 0.0))

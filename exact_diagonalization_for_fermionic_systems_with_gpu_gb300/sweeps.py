@@ -1,0 +1,250 @@
+"""Parameter sweeps of the reference drivers, run through this library's
+ground-state path on one GPU.
+
+flux_sweep   Kagome12 6+6 with a twist Phi on every bond (phase Phi * dx_b):
+             E0, dE0/dPhi (Hellmann-Feynman) and d2E0/dPhi2 (linear response)
+             at n_phi points of [0, 2 pi / KAGOME12_LX].  d2E0/dPhi2 at
+             Phi = 0 is the twist-curvature form of the Drude weight that
+             DrudeWeight/src/drude_v2_cal_Kagome_randomHop.cu:144-155 obtains
+             from <K_x> and the current-current Kubo sum (drude_weight_Jx).
+mbl_sweep    open L=12 chain, t=1, U, on-site disorder W * uniform(-1, 1)
+             drawn separately for the up and the down spin operator, as
+             MBL_test/src/Hubbard_EE_test.cu:66-70 does with two Line16
+             calls on one random stream; for every realisation and every
+             (N_up, N_dn) sector: E0, the entanglement entropy of sites
+             0..L/2-1 (EEmatHubAB_GPU::Make_Write + cusolverZsvd + the
+             -sum S log S of Hubbard_EE_test.cu:76-83, taken here on the
+             ground state instead of the reference's dense-ED quench) and
+             dE0/d eps_{i,s} = <n_{i,s}> (Hellmann-Feynman on the site term).
+
+Disorder numbers come from Philox4x64-10 keyed by (seed, realisation), so the
+same realisation is used in every sector; each instance's Lanczos start
+vector is keyed by realisation * n_sectors + sector.  Every quantity stays on
+the device between the Lanczos run and the observables (the Ritz vector is
+written into a CUDA tensor).
+
+`python -m exact_diagonalization_for_fermionic_systems_with_gpu_gb300.sweeps
+--what flux|mbl` runs a sweep and prints one JSON line with its timing.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import time
+from dataclasses import dataclass, field
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import lattices as L
+from . import observables as ob
+from .hubbard import H_TBq, Hubbard, Lanczos, random_vector
+
+
+@dataclass
+class FluxPoint:
+    phi: float
+    e0: float
+    d1: float          # dE0/dPhi
+    d2: float          # d2E0/dPhi2
+    steps: int         # Lanczos steps of the ground-state run
+
+
+@dataclass
+class MblPoint:
+    realisation: int
+    sector: Tuple[int, int]
+    e0: float
+    s_vn: float        # -sum lambda log lambda of the reduced density matrix
+    s_ref: float       # the reference's -sum S log S over singular values
+    n_up: np.ndarray   # dE0/d eps_{i,up}
+    n_dn: np.ndarray   # dE0/d eps_{i,dn}
+    steps: int
+
+
+@dataclass
+class SweepTiming:
+    instances: int = 0
+    lanczos_steps: int = 0
+    build_s: float = 0.0       # operator construction (tables, plans, upload)
+    lanczos_s: float = 0.0     # ground state and Ritz vector
+    observables_s: float = 0.0
+    total_s: float = 0.0
+    per_instance: List[float] = field(default_factory=list)
+
+    def summary(self) -> dict:
+        return {"instances": self.instances, "lanczos_steps": self.lanczos_steps,
+                "total_s": round(self.total_s, 4), "build_s": round(self.build_s, 4),
+                "lanczos_s": round(self.lanczos_s, 4), "observables_s": round(self.observables_s, 4),
+                "instances_per_s": round(self.instances / self.total_s, 3) if self.total_s > 0 else None,
+                "lanczos_steps_per_s": round(self.lanczos_steps / self.lanczos_s, 1) if self.lanczos_s > 0 else None}
+
+
+def _sync():
+    import torch
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
+def _ground(H: Hubbard, steps: int, mode: str, seed: int):
+    """(E0, Ritz vector as a CUDA tensor, steps taken)."""
+    import torch
+    dt = torch.complex128 if H.is_complex else torch.float64
+    evec = torch.empty(H.rows(), dtype=dt, device="cuda")
+    lz = Lanczos()
+    e0, _ = lz.eigen(H, max_steps=steps, mode=mode, ritz="stored", seed=seed, evec_out=evec)
+    return e0, evec, int(lz.result.steps)
+
+
+def flux_phis(n_phi: int = 16) -> np.ndarray:
+    """n_phi twists evenly spaced over [0, 2 pi / KAGOME12_LX], both ends included."""
+    return np.linspace(0.0, 2.0 * math.pi / L.KAGOME12_LX, n_phi)
+
+
+def flux_sweep(phis: Optional[Sequence[float]] = None, n_up: int = 6, n_dn: int = 6, U: float = 4.0,
+               steps: int = 300, mode: str = "fixed", response_steps: int = 200, seed: int = 0,
+               rand: Optional[Sequence[float]] = None, timing: Optional[SweepTiming] = None) -> List[FluxPoint]:
+    """E0(Phi), dE0/dPhi, d2E0/dPhi2 of Kagome12 (complex operator at every
+    Phi, Phi = 0 included, so the second-order response sees the current)."""
+    phis = flux_phis() if phis is None else phis
+    t = timing if timing is not None else SweepTiming()
+    out: List[FluxPoint] = []
+    t0 = time.perf_counter()
+    for k, phi in enumerate(phis):
+        ti = time.perf_counter()
+        terms = L.kagome12(rand, flux=float(phi), peierls=True)
+        d1t, d2t = L.kagome12_flux_derivatives(float(phi), rand)
+        H = Hubbard(H_TBq(12, n_up).extend(terms), H_TBq(12, n_dn).extend(terms), U)
+        dH = Hubbard(H_TBq(12, n_up).extend(d1t), H_TBq(12, n_dn).extend(d1t), 0.0)
+        d2H = Hubbard(H_TBq(12, n_up).extend(d2t), H_TBq(12, n_dn).extend(d2t), 0.0)
+        _sync()
+        tb = time.perf_counter()
+        e0, psi, n = _ground(H, steps, mode, seed * 4096 + k)
+        _sync()
+        tl = time.perf_counter()
+        d1, d2 = ob.response(H, dH, d2H, psi, e0, steps=response_steps)
+        _sync()
+        te = time.perf_counter()
+        for op in (H, dH, d2H):
+            op.close()
+        out.append(FluxPoint(float(phi), e0, d1, d2, n))
+        t.instances += 1
+        t.lanczos_steps += n
+        t.build_s += tb - ti
+        t.lanczos_s += tl - tb
+        t.observables_s += te - tl
+        t.per_instance.append(te - ti)
+    t.total_s += time.perf_counter() - t0
+    return out
+
+
+def mbl_disorder(realisation: int, n_sites: int = 12, W: float = 6.0, seed: int = 0) -> Tuple[np.ndarray, np.ndarray]:
+    """(eps_up, eps_dn) = W * uniform(-1, 1), 2 * n_sites numbers from
+    Philox4x64-10 keyed by seed * 2^20 + realisation: the first n_sites for
+    the up operator, the next for the down operator (the order of the two
+    Line16 calls of Hubbard_EE_test.cu:68-69)."""
+    x = random_vector(2 * n_sites, seed * (1 << 20) + realisation) * W
+    return x[:n_sites].copy(), x[n_sites:].copy()
+
+
+def mbl_chain_terms(eps: Sequence[float], t: float = -1.0):
+    """Open chain with hopping t and on-site energies eps (Line16's bonds,
+    Hubbard_EE_test.cu:119-139, for len(eps) sites)."""
+    return L.chain(len(eps), t=t, periodic=False, eps=list(eps))
+
+
+MBL_SECTORS = ((6, 6), (7, 5), (8, 4))
+
+
+def mbl_sweep(n_real: int = 64, sectors: Sequence[Tuple[int, int]] = MBL_SECTORS, n_sites: int = 12,
+              W: float = 6.0, U: float = 1.0, steps: int = 300, mode: str = "fixed", seed: int = 0,
+              a_sites: Optional[Sequence[int]] = None, realisations: Optional[Sequence[int]] = None,
+              timing: Optional[SweepTiming] = None) -> List[MblPoint]:
+    """Ground-state sweep over disorder realisations and sectors."""
+    a_sites = list(range(n_sites // 2)) if a_sites is None else list(a_sites)
+    reals = range(n_real) if realisations is None else realisations
+    t = timing if timing is not None else SweepTiming()
+    out: List[MblPoint] = []
+    t0 = time.perf_counter()
+    for r in reals:
+        eu, edn = mbl_disorder(r, n_sites, W, seed)
+        tu, td = mbl_chain_terms(eu), mbl_chain_terms(edn)
+        for s, (qu, qd) in enumerate(sectors):
+            ti = time.perf_counter()
+            H = Hubbard(H_TBq(n_sites, qu).extend(tu), H_TBq(n_sites, qd).extend(td), U)
+            _sync()
+            tb = time.perf_counter()
+            e0, psi, n = _ground(H, steps, mode, seed * (1 << 20) + r * len(sectors) + s)
+            _sync()
+            tl = time.perf_counter()
+            nu, nd, _ = ob.site_densities(H, psi)
+            svn, sref = ob.entanglement_entropy(H, psi, a_sites)
+            _sync()
+            te = time.perf_counter()
+            H.close()
+            out.append(MblPoint(int(r), (qu, qd), e0, svn, sref, nu, nd, n))
+            t.instances += 1
+            t.lanczos_steps += n
+            t.build_s += tb - ti
+            t.lanczos_s += tl - tb
+            t.observables_s += te - tl
+            t.per_instance.append(te - ti)
+    t.total_s += time.perf_counter() - t0
+    return out
+
+
+def flux_rows(points: Sequence[FluxPoint]):
+    """Rows (Phi, E0, dE0/dPhi, d2E0/dPhi2) for datio.append_rows."""
+    return [(p.phi, p.e0, p.d1, p.d2) for p in points]
+
+
+def mbl_rows(points: Sequence[MblPoint]):
+    """Rows (realisation, N_up, N_dn, E0, S_vN, n_up[0..L-1], n_dn[0..L-1])."""
+    return [(p.realisation, p.sector[0], p.sector[1], p.e0, p.s_vn) + tuple(p.n_up) + tuple(p.n_dn)
+            for p in points]
+
+
+FLUX_HEADER = "#       Phi       E0        dE0/dPhi        d2E0/dPhi2      "
+MBL_HEADER = "#       xid       Nup       Ndn       E0        S_A       n_up(i)...      n_dn(i)...      "
+
+
+def main(argv: Optional[Sequence[str]] = None) -> None:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--what", choices=["flux", "mbl"], default="mbl")
+    ap.add_argument("--n", type=int, default=None, help="flux points (16) or realisations (64)")
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--mode", choices=["fixed", "reference"], default="fixed")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--warmup", type=int, default=1, help="instances run (untimed) before the sweep")
+    ap.add_argument("--out", default=None, help="append the result rows to this .dat file")
+    a = ap.parse_args(argv)
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("sweeps need a CUDA device")
+    tm = SweepTiming()
+    if a.what == "flux":
+        n = 16 if a.n is None else a.n
+        if a.warmup:
+            flux_sweep(flux_phis(n)[: a.warmup], steps=a.steps, mode=a.mode, seed=a.seed)
+        pts = flux_sweep(flux_phis(n), steps=a.steps, mode=a.mode, seed=a.seed, timing=tm)
+        rows, header = flux_rows(pts), FLUX_HEADER
+        cfg = {"workload": f"Kagome12 6+6 U=4, {n} twists in [0, 2pi/{L.KAGOME12_LX:g}], complex FP64",
+               "lanczos_steps": a.steps, "response_steps": 200, "mode": a.mode}
+    else:
+        n = 64 if a.n is None else a.n
+        if a.warmup:
+            mbl_sweep(realisations=range(a.warmup), steps=a.steps, mode=a.mode, seed=a.seed + 1)
+        pts = mbl_sweep(n, steps=a.steps, mode=a.mode, seed=a.seed, timing=tm)
+        rows, header = mbl_rows(pts), MBL_HEADER
+        cfg = {"workload": f"open chain L=12 t=1 U=1 W=6, {n} realisations x sectors (6,6),(7,5),(8,4)",
+               "lanczos_steps": a.steps, "mode": a.mode, "entanglement_sites": "0..5"}
+    if a.out:
+        from .datio import append_rows
+        append_rows(a.out, header, rows)
+    print(json.dumps({"sweep": a.what, "config": cfg, **tm.summary(),
+                      "ms_per_instance_median": round(1e3 * float(np.median(tm.per_instance)), 3)}))
+
+
+if __name__ == "__main__":
+    main()

@@ -245,6 +245,21 @@ ed_status ed_s2_expect(ed_op* op, const double* psi, int mem, double* out, void*
 ed_status ed_tridiag_lowest(int n, const double* alpha, const double* offdiag,
                             double* e0, double* z);
 
+/* All eigenpairs of the same tridiagonal (LAPACKf77::dsted with compz = 'I',
+ * MBL_test/include/MAGMA_LAPACK.h:296-326, as Krylov::Make_tridiagonal_eigen
+ * calls it, HubMatrix_GPU.cuh:672-680): evals ascending (n doubles), z the unit
+ * eigenvectors as columns (n x n, column j = eigenvector of evals[j]; may be
+ * NULL).  Implicit QR with Wilkinson shifts on the host.  ED_ERR_BREAKDOWN if
+ * the iteration does not converge. */
+ed_status ed_tridiag_eigen(int n, const double* alpha, const double* offdiag,
+                           double* evals, double* z);
+
+/* out[t] = exp(-i T times[t]) e_0 (n complex values, interleaved re, im;
+ * n_times x 2n doubles): the Krylov propagator coefficients of
+ * Krylov::Krylov_time_evol (HubMatrix_GPU.cuh:684-690).  Host in/out. */
+ed_status ed_tridiag_expm(int n, const double* alpha, const double* offdiag,
+                          int n_times, const double* times, double* out);
+
 /* ------------------------------------------------------------ observables --
  * What the reference drivers compute from a ground state.  psi is the Ritz
  * vector (rows doubles, or 2*rows for complex operators) at `mem`. */
@@ -306,6 +321,39 @@ ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double
  * drivers print, Hubbard_EE_test.cu:80-83).  Real operators. */
 ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_t a_mask, double* s_vn,
                                   double* s_ref, void* stream);
+
+/* ------------------------------------------------------- time evolution --
+ * psi(t) = exp(-i H t) psi0 in the Krylov space of psi0
+ * (Krylov::Make_tridiagonal_eigen + Krylov::Krylov_time_evol,
+ * MBL_test/include/HubMatrix_GPU.cuh:619-728): the Lanczos recurrence from
+ * psi0 (the same persistent Lanczos step as ed_lanczos_run, the basis kept in
+ * device memory) stops at the first beta_k < tol * |psi0| (the reference:
+ * 1e-10 for a normalised psi0) or after max_steps; then, for every time,
+ * c = exp(-i T t) e_0 (ed_tridiag_expm) and psi(t) = |psi0| sum_k c_k v_k on
+ * the device.  A real operator applied to a complex psi0 runs one recurrence
+ * for each nonzero part (exp(-iHt) is linear).  psi0: 2*rows doubles
+ * (complex, interleaved re, im) at psi0_mem; psi_out: n_times x 2*rows
+ * doubles at out_mem, time-major, overwritten (the reference adds into phi);
+ * times: host.  Operators that need the two-pass matvec return
+ * ED_ERR_NOT_BUILT.  Synchronous. */
+typedef struct {
+    int32_t max_steps;   /* Krylov dimension cap (the reference's loop: 1000) */
+    int32_t reorth;      /* 1: full reorthogonalisation of the basis */
+    double tol;          /* stop at beta_k < tol * |psi0| */
+} ed_krylov_cfg;
+
+typedef struct {
+    int32_t steps;       /* Krylov dimension used (largest of the recurrences) */
+    int32_t runs;        /* recurrences run (0, 1 or 2) */
+    double norm;         /* |psi0| */
+    double err_est;      /* max over times and runs of beta_m |c_{m-1}(t)| |psi0_part|,
+                            the a-posteriori error estimate of the truncation */
+    int64_t launches;    /* kernels this call launched */
+} ed_krylov_result;
+
+ed_status ed_krylov_evolve(ed_op* op, const ed_krylov_cfg* cfg, const double* psi0, int psi0_mem, int n_times,
+                           const double* times, double* psi_out, int out_mem, ed_krylov_result* res,
+                           void* stream);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,70 @@
+"""The host tridiagonal eigensolver and Krylov propagator (no GPU): all
+eigenpairs against scipy's eigh_tridiagonal, exp(-i T t) e_0 against
+scipy.linalg.expm, on random matrices, Lanczos-like matrices with clustered
+(ghost) eigenvalues, and split / tiny cases."""
+import numpy as np
+import pytest
+import scipy.linalg as sl
+
+
+def dense(a, b):
+    return np.diag(a) + np.diag(b, 1) + np.diag(b, -1)
+
+
+def cases():
+    rng = np.random.default_rng(7)
+    yield rng.standard_normal(1), np.zeros(0)
+    yield np.array([1.0, -2.0]), np.array([0.5])
+    yield rng.standard_normal(40), rng.standard_normal(39)
+    b = rng.standard_normal(59)
+    b[[10, 30]] = 0.0  # three decoupled blocks
+    yield rng.standard_normal(60), b
+    yield np.full(30, 2.0), np.full(29, 1e-9)  # near-degenerate
+    # a plain Lanczos T on a 200-dim diagonal matrix run 150 steps: ghosts
+    d = np.sort(rng.uniform(-5, 5, 200))
+    q = rng.standard_normal(200)
+    q /= np.linalg.norm(q)
+    al, be, qp = [], [], np.zeros(200)
+    bprev = 0.0
+    for _ in range(150):
+        w = d * q - bprev * qp
+        a = q @ w
+        w -= a * q
+        bn = np.linalg.norm(w)
+        al.append(a)
+        be.append(bn)
+        qp, q, bprev = q, w / bn, bn
+    yield np.array(al), np.array(be[:-1])
+
+
+@pytest.mark.parametrize("k", range(6))
+def test_tridiag_eigen_against_scipy(edlib, k):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import evolution as ev
+    a, b = list(cases())[k]
+    w, Z = ev.tridiag_eigen(a, b)
+    wr = sl.eigh_tridiagonal(a, b, eigvals_only=True) if a.size > 1 else a.copy()
+    scale = max(1.0, np.max(np.abs(wr)))
+    assert np.max(np.abs(w - wr)) < 1e-13 * scale * a.size
+    T = dense(a, b)
+    assert np.max(np.abs(Z.T @ Z - np.eye(a.size))) < 1e-13 * a.size
+    assert np.max(np.abs(T @ Z - Z * w)) < 1e-13 * scale * a.size
+
+
+@pytest.mark.parametrize("k", range(6))
+def test_tridiag_expm_against_scipy(edlib, k):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import evolution as ev
+    a, b = list(cases())[k]
+    times = [0.0, 0.02, 0.7, 3.0, 25.0]
+    c = ev.tridiag_expm(a, b, times)
+    T = dense(a, b)
+    for i, t in enumerate(times):
+        ref = sl.expm(-1j * t * T)[:, 0]
+        assert np.max(np.abs(c[i] - ref)) < 1e-12 * max(1.0, abs(t) * np.max(np.abs(T)))
+        assert abs(np.linalg.norm(c[i]) - 1.0) < 1e-13 * a.size
+
+
+def test_tridiag_bad_arguments(edlib):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import _capi
+    lib = _capi.load()
+    assert lib.ed_tridiag_eigen(0, None, None, None, None) == 1  # ED_ERR_ARG
+    assert lib.ed_tridiag_expm(3, None, None, 1, None, None) == 1  # ED_ERR_ARG
