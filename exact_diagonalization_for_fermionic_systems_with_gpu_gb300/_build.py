@@ -64,7 +64,7 @@ def build(force: bool = False) -> Path:
         objs = list(ex.map(_compile, SOURCES))
     LIBDIR.mkdir(parents=True, exist_ok=True)
     tmp = LIBDIR / (LIBNAME + ".tmp")
-    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lcusolver"]
+    cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart", "-lcusolver", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

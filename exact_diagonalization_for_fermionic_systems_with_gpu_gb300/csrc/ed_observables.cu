@@ -10,7 +10,10 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "../../include/ed_hubbard.h"
@@ -238,6 +241,122 @@ namespace {
 
 using ed::kObBlocks;
 using ed::kObThreads;
+
+// Block SVDs of the entanglement matrix.  cusolverDnDgesvd on a block of a
+// few hundred rows is latency-bound (one SM's worth of work per call), so
+// the blocks run concurrently: a per-device pool of workers, each a host
+// thread with its own stream, cuSOLVER handle and workspace (created on
+// first use, kept for the life of the process), takes the blocks
+// largest-first to the least-loaded worker.
+struct EeWorker {
+    cudaStream_t st = nullptr;
+    cusolverDnHandle_t h = nullptr;
+    double* work = nullptr;
+    int lwork = 0;
+    double* rwork = nullptr;
+    int rwork_n = 0;
+    int* info = nullptr;
+    cudaEvent_t done = nullptr;
+};
+
+struct EePool {
+    std::mutex mu;
+    std::vector<EeWorker> w;
+};
+
+int ee_workers() {
+    const char* e = std::getenv("ED_EE_STREAMS");
+    const int k = e ? std::atoi(e) : 8;
+    return std::max(1, std::min(k, 32));
+}
+
+EePool* ee_pool(int device) {
+    static std::mutex mu;
+    static std::vector<EePool*> pools;
+    std::lock_guard<std::mutex> g(mu);
+    if ((int)pools.size() <= device) pools.resize(device + 1, nullptr);
+    if (!pools[device]) pools[device] = new EePool();
+    return pools[device];
+}
+
+ed_status ee_block_svd(int device, cudaStream_t s, double* blocks, const std::vector<int64_t>& off,
+                       const std::vector<int>& mm, const std::vector<int>& nn, const std::vector<int64_t>& svo,
+                       double* sv_all) {
+    EePool* pool = ee_pool(device);
+    std::lock_guard<std::mutex> g(pool->mu);
+    const int K = ee_workers();
+    while ((int)pool->w.size() < K) {
+        EeWorker w;
+        if (cudaStreamCreateWithFlags(&w.st, cudaStreamNonBlocking) != cudaSuccess) return ED_ERR_CUDA;
+        if (cusolverDnCreate(&w.h) != CUSOLVER_STATUS_SUCCESS) return ED_ERR_CUDA;
+        cusolverDnSetStream(w.h, w.st);
+        if (cudaMalloc(&w.info, sizeof(int)) != cudaSuccess) return ED_ERR_ALLOC;
+        if (cudaEventCreateWithFlags(&w.done, cudaEventDisableTiming) != cudaSuccess) return ED_ERR_CUDA;
+        pool->w.push_back(w);
+    }
+    // largest first, each to the least-loaded worker (cost ~ m n^2)
+    std::vector<int> order;
+    for (size_t k = 0; k < off.size(); ++k)
+        if (nn[k] > 0) order.push_back((int)k);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        return (double)mm[a] * nn[a] * nn[a] > (double)mm[b] * nn[b] * nn[b];
+    });
+    std::vector<std::vector<int>> part(K);
+    std::vector<double> load(K, 0.0);
+    for (int k : order) {
+        const int q = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        part[q].push_back(k);
+        load[q] += (double)mm[k] * nn[k] * nn[k] + 2e5;  // + a per-call overhead
+    }
+    cudaEvent_t ready;
+    if (cudaEventCreateWithFlags(&ready, cudaEventDisableTiming) != cudaSuccess) return ED_ERR_CUDA;
+    cudaEventRecord(ready, s);
+    std::vector<ed_status> res(K, ED_OK);
+    auto run = [&](int q) {
+        EeWorker& w = pool->w[q];
+        if (cudaSetDevice(device) != cudaSuccess || cudaStreamWaitEvent(w.st, ready, 0) != cudaSuccess) {
+            res[q] = ED_ERR_CUDA;
+            return;
+        }
+        for (int k : part[q]) {
+            int lw = 0;
+            if (cusolverDnDgesvd_bufferSize(w.h, mm[k], nn[k], &lw) != CUSOLVER_STATUS_SUCCESS) { res[q] = ED_ERR_CUDA; return; }
+            if (lw > w.lwork) {
+                cudaFree(w.work);
+                w.work = nullptr;
+                w.lwork = 0;
+                if (cudaMalloc(&w.work, sizeof(double) * lw) != cudaSuccess) { res[q] = ED_ERR_ALLOC; return; }
+                w.lwork = lw;
+            }
+            if (nn[k] > w.rwork_n) {
+                cudaFree(w.rwork);
+                w.rwork = nullptr;
+                w.rwork_n = 0;
+                if (cudaMalloc(&w.rwork, sizeof(double) * nn[k]) != cudaSuccess) { res[q] = ED_ERR_ALLOC; return; }
+                w.rwork_n = nn[k];
+            }
+            if (cusolverDnDgesvd(w.h, 'N', 'N', mm[k], nn[k], blocks + off[k], mm[k], sv_all + svo[k], nullptr,
+                                 mm[k], nullptr, nn[k], w.work, w.lwork, w.rwork, w.info) != CUSOLVER_STATUS_SUCCESS) {
+                res[q] = ED_ERR_CUDA;
+                return;
+            }
+        }
+        if (cudaEventRecord(w.done, w.st) != cudaSuccess) res[q] = ED_ERR_CUDA;
+    };
+    std::vector<std::thread> th;
+    for (int q = 1; q < K; ++q)
+        if (!part[q].empty()) th.emplace_back(run, q);
+    if (!part[0].empty()) run(0);
+    for (std::thread& t : th) t.join();
+    cudaEventDestroy(ready);
+    ed_status st = ED_OK;
+    for (int q = 0; q < K; ++q) {
+        if (res[q] != ED_OK) st = res[q];
+        if (!part[q].empty() && res[q] == ED_OK && cudaStreamWaitEvent(s, pool->w[q].done, 0) != cudaSuccess)
+            st = ED_ERR_CUDA;
+    }
+    return st;
+}
 
 struct ObScratch {
     double* part = nullptr;
@@ -687,43 +806,26 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
     m.nqd = nqd;
     ed::k_ee_scatter<<<ob_grid(op->D), kObThreads, 0, s>>>(dpsi, op->dimUP, op->dimDN, m, blocks);
     // singular values of every block (cusolverDnDgesvd, jobu = jobvt = 'N',
-    // as entangle_entropy.h:231-291)
-    cusolverDnHandle_t h = nullptr;
-    double svn = 0.0, sref = 0.0;
-    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) st = ED_ERR_CUDA;
-    if (st == ED_OK) cusolverDnSetStream(h, s);
-    int lwork_max = 0;
-    for (size_t k = 0; st == ED_OK && k < off.size(); ++k) {
-        const int mm = std::max(rA[k], cB[k]), nn = std::min(rA[k], cB[k]);
-        if (nn == 0) continue;
-        int lw = 0;
-        if (cusolverDnDgesvd_bufferSize(h, mm, nn, &lw) != CUSOLVER_STATUS_SUCCESS) st = ED_ERR_CUDA;
-        lwork_max = std::max(lwork_max, lw);
+    // as entangle_entropy.h:231-291), the blocks spread over the device's
+    // worker streams; all singular values land in one device array
+    std::vector<int> mmv(off.size()), nnv(off.size());
+    std::vector<int64_t> svo(off.size() + 1, 0);
+    for (size_t k = 0; k < off.size(); ++k) {
+        mmv[k] = std::max(rA[k], cB[k]);
+        nnv[k] = std::min(rA[k], cB[k]);
+        svo[k + 1] = svo[k] + nnv[k];
     }
-    double *work = nullptr, *sv = nullptr, *rwork = nullptr;
-    int* info = nullptr;
-    int max_n = 0;
-    for (size_t k = 0; k < off.size(); ++k) max_n = std::max(max_n, (int)std::min(rA[k], cB[k]));
-    if (st == ED_OK && (cudaMalloc(&work, sizeof(double) * std::max(lwork_max, 1)) != cudaSuccess ||
-                        cudaMalloc(&sv, sizeof(double) * std::max(max_n, 1)) != cudaSuccess ||
-                        cudaMalloc(&rwork, sizeof(double) * std::max(max_n, 1)) != cudaSuccess ||
-                        cudaMalloc(&info, sizeof(int)) != cudaSuccess))
-        st = ED_ERR_ALLOC;
-    std::vector<double> hs(std::max(max_n, 1));
-    for (size_t k = 0; st == ED_OK && k < off.size(); ++k) {
-        const int mm = std::max(rA[k], cB[k]), nn = std::min(rA[k], cB[k]);
-        if (nn == 0) continue;
-        if (cusolverDnDgesvd(h, 'N', 'N', mm, nn, blocks + off[k], mm, sv, nullptr, mm, nullptr, nn, work, lwork_max,
-                             rwork, info) != CUSOLVER_STATUS_SUCCESS) {
+    double* sv_all = nullptr;
+    if (cudaMalloc(&sv_all, sizeof(double) * std::max<int64_t>(svo.back(), 1)) != cudaSuccess) st = ED_ERR_ALLOC;
+    if (st == ED_OK) st = ee_block_svd(op->device, s, blocks, off, mmv, nnv, svo, sv_all);
+    double svn = 0.0, sref = 0.0;
+    if (st == ED_OK) {
+        std::vector<double> hs(std::max<int64_t>(svo.back(), 1));
+        if (cudaMemcpyAsync(hs.data(), sv_all, sizeof(double) * svo.back(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
             st = ED_ERR_CUDA;
-            break;
-        }
-        if (cudaMemcpyAsync(hs.data(), sv, sizeof(double) * nn, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-            cudaStreamSynchronize(s) != cudaSuccess) {
-            st = ED_ERR_CUDA;
-            break;
-        }
-        for (int i = 0; i < nn; ++i) {
+        // block by block, each in descending order: a fixed summation order
+        for (int64_t i = 0; st == ED_OK && i < svo.back(); ++i) {
             const double x = hs[i];
             if (x > 0.0) {
                 sref += -x * std::log(x);
@@ -732,8 +834,7 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
             }
         }
     }
-    if (h) cusolverDnDestroy(h);
-    cudaFree(work); cudaFree(sv); cudaFree(rwork); cudaFree(info);
+    cudaFree(sv_all);
     cudaFree(blocks); cudaFree(dmi); cudaFree(doff);
     if (owned) cudaFreeAsync(owned, s);
     cudaStreamSynchronize(s);
