@@ -66,7 +66,8 @@ class ed_kubo_result(C.Structure):
 
 
 class ed_krylov_cfg(C.Structure):
-    _fields_ = [("max_steps", C.c_int32), ("reorth", C.c_int32), ("tol", C.c_double)]
+    _fields_ = [("max_steps", C.c_int32), ("reorth", C.c_int32), ("tol", C.c_double), ("accumulate", C.c_int32),
+                ("pad_", C.c_int32)]
 
 
 class ed_krylov_result(C.Structure):

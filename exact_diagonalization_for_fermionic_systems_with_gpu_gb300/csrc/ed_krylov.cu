@@ -158,8 +158,10 @@ ed_status ed_krylov_evolve(ed_op* op, const ed_krylov_cfg* cfg, const double* ps
     } else {
         d0 = const_cast<double*>(psi0);
     }
+    const bool acc = cfg->accumulate != 0;
     if (out_mem == ED_MEM_HOST) {
         if (n_times > 0 && cudaMallocAsync(&dout, vbytes * n_times, s) != cudaSuccess) { release(); return ED_ERR_ALLOC; }
+        if (n_times > 0 && acc) KR_CK(cudaMemcpyAsync(dout, psi_out, vbytes * n_times, cudaMemcpyHostToDevice, s));
     } else {
         dout = psi_out;
     }
@@ -189,7 +191,7 @@ ed_status ed_krylov_evolve(ed_op* op, const ed_krylov_cfg* cfg, const double* ps
         for (int p = 0; p < 2; ++p)
             if (n2[p] > 0.0) runs.push_back({tmp, p});
     }
-    if (runs.empty() && n_times > 0) KR_CK(cudaMemsetAsync(dout, 0, vbytes * n_times, s));
+    if (runs.empty() && n_times > 0 && !acc) KR_CK(cudaMemsetAsync(dout, 0, vbytes * n_times, s));
 
     ed_lanczos_cfg lc{};
     lc.max_steps = cfg->max_steps;
@@ -200,7 +202,7 @@ ed_status ed_krylov_evolve(ed_op* op, const ed_krylov_cfg* cfg, const double* ps
     std::vector<double> alpha(cfg->max_steps + 2), beta(cfg->max_steps + 2);
     int max_n = 0;
     double err = 0.0;
-    bool written = false;
+    bool written = acc;
     if (n_times > 0 && cudaMallocAsync(&dcoef, sizeof(double2) * (size_t)n_times * (cfg->max_steps + 1), s) != cudaSuccess) {
         release();
         return ED_ERR_ALLOC;

@@ -40,13 +40,14 @@ def tridiag_expm(alpha: Sequence[float], offdiag: Sequence[float], times: Sequen
 
 
 def krylov_evolve(H: Hubbard, psi0, times: Sequence[float], max_steps: int = 1000, tol: float = 1e-10,
-                  reorth: bool = False, result: Optional[dict] = None):
+                  reorth: bool = False, result: Optional[dict] = None, out=None):
     """exp(-i H t) psi0 for every t in times.  psi0: complex numpy array (host)
     or complex CUDA tensor (device); the result is (len(times), rows) of the
-    same kind.  result, when given, receives steps / runs / norm / err_est /
+    same kind.  out, when given (that shape and kind), is added to and
+    returned.  result, when given, receives steps / runs / norm / err_est /
     launches."""
     lib = _capi.load()
-    cfg = _capi.ed_krylov_cfg(int(max_steps), 1 if reorth else 0, float(tol))
+    cfg = _capi.ed_krylov_cfg(int(max_steps), 1 if reorth else 0, float(tol), 0 if out is None else 1, 0)
     res = _capi.ed_krylov_result()
     t = np.ascontiguousarray(times, dtype=np.float64)
     n = H.rows()
@@ -54,7 +55,10 @@ def krylov_evolve(H: Hubbard, psi0, times: Sequence[float], max_steps: int = 100
         p0 = np.ascontiguousarray(psi0, dtype=np.complex128)
         if p0.size != n:
             raise ValueError(f"psi0 has {p0.size} values, the operator {n} rows")
-        out = np.empty((t.size, n), dtype=np.complex128)
+        if out is None:
+            out = np.empty((t.size, n), dtype=np.complex128)
+        elif out.dtype != np.complex128 or out.shape != (t.size, n) or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous complex128 array of shape (len(times), rows)")
         check(lib.ed_krylov_evolve(H.handle, C.byref(cfg), _ptr(p0), _capi.ED_MEM_HOST, int(t.size),
                                    _ptr(t) if t.size else None, _ptr(out) if t.size else None, _capi.ED_MEM_HOST,
                                    C.byref(res), None), "ed_krylov_evolve")
@@ -63,7 +67,10 @@ def krylov_evolve(H: Hubbard, psi0, times: Sequence[float], max_steps: int = 100
         p0 = psi0.to(torch.complex128).contiguous()
         if p0.numel() != n:
             raise ValueError(f"psi0 has {p0.numel()} values, the operator {n} rows")
-        out = torch.empty((t.size, n), dtype=torch.complex128, device=p0.device)
+        if out is None:
+            out = torch.empty((t.size, n), dtype=torch.complex128, device=p0.device)
+        elif out.dtype != torch.complex128 or tuple(out.shape) != (t.size, n) or not out.is_contiguous():
+            raise ValueError("out must be a contiguous complex128 tensor of shape (len(times), rows)")
         check(lib.ed_krylov_evolve(H.handle, C.byref(cfg), C.c_void_p(p0.data_ptr()), _capi.ED_MEM_DEVICE,
                                    int(t.size), _ptr(t) if t.size else None,
                                    C.c_void_p(out.data_ptr()) if t.size else None, _capi.ED_MEM_DEVICE,
@@ -91,9 +98,8 @@ class Krylov:
         self.steps = self.info["steps"]
 
     def Krylov_time_evol(self, Hub: Hubbard, phi0, phi, dt: float) -> None:
-        out = krylov_evolve(Hub, phi0, [dt], self.max_steps, self.tol, result=self.info)
+        krylov_evolve(Hub, phi0, [dt], self.max_steps, self.tol, result=self.info, out=phi.reshape(1, -1))
         self.steps = self.info["steps"]
-        phi += out[0]
 
     def clear(self) -> None:
         self.steps = 0

@@ -333,13 +333,15 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
  * the device.  A real operator applied to a complex psi0 runs one recurrence
  * for each nonzero part (exp(-iHt) is linear).  psi0: 2*rows doubles
  * (complex, interleaved re, im) at psi0_mem; psi_out: n_times x 2*rows
- * doubles at out_mem, time-major, overwritten (the reference adds into phi);
+ * doubles at out_mem, time-major, overwritten (added to with accumulate);
  * times: host.  Operators that need the two-pass matvec return
  * ED_ERR_NOT_BUILT.  Synchronous. */
 typedef struct {
     int32_t max_steps;   /* Krylov dimension cap (the reference's loop: 1000) */
     int32_t reorth;      /* 1: full reorthogonalisation of the basis */
     double tol;          /* stop at beta_k < tol * |psi0| */
+    int32_t accumulate;  /* 1: psi_out += psi(t) (Krylov_time_evol adds into phi) */
+    int32_t pad_;
 } ed_krylov_cfg;
 
 typedef struct {

@@ -8,6 +8,8 @@
 //                            pointers — the Spectra operator concept
 //                                                             (HubMatrix_TotalSpin.cuh:181-322)
 //   ed::Lanczos              random_vector / eigen            (HubMatrix_GPU.cuh:477-613)
+//   ed::Krylov               Make_tridiagonal_eigen / Krylov_time_evol on device
+//                            complex vectors                  (HubMatrix_GPU.cuh:619-728)
 // Errors surface as ed::Error (std::runtime_error) carrying the ed_status.
 #pragma once
 
@@ -145,6 +147,31 @@ public:
         a.resize(result.steps);
         b.resize(result.steps + 1);
         return result.e0;
+    }
+};
+
+// Krylov<double>: phi0, phi are device arrays of rows() complex values
+// (interleaved re, im).  Krylov_time_evol ADDS exp(-i H dt) phi0 into phi, as
+// the reference's does; the Lanczos recurrence runs inside each call.
+class Krylov {
+public:
+    int max_steps = 1000;
+    double tol = 1e-10;  // stop at b < tol * |phi0|
+    ed_krylov_result result{};
+    Krylov(int64_t /*dimUP*/ = 0, int64_t /*dimDN*/ = 0) {}
+    // The Krylov dimension of phi0 (a recurrence with no output times).
+    void Make_tridiagonal_eigen(Hubbard& h, const double* phi0_dev, void* stream = nullptr) {
+        ed_krylov_cfg c{max_steps, 0, tol, 0, 0};
+        check(ed_krylov_evolve(h.handle(), &c, phi0_dev, ED_MEM_DEVICE, 0, nullptr, nullptr, ED_MEM_DEVICE, &result,
+                               stream),
+              "ed_krylov_evolve");
+    }
+    // phi += exp(-i H dt) phi0
+    void Krylov_time_evol(Hubbard& h, const double* phi0_dev, double* phi_dev, double dt, void* stream = nullptr) {
+        ed_krylov_cfg c{max_steps, 0, tol, 1, 0};
+        check(ed_krylov_evolve(h.handle(), &c, phi0_dev, ED_MEM_DEVICE, 1, &dt, phi_dev, ED_MEM_DEVICE, &result,
+                               stream),
+              "ed_krylov_evolve");
     }
 };
 
