@@ -65,6 +65,16 @@ class ed_kubo_result(C.Structure):
     _fields_ = [("drude", C.c_double), ("kinetic", C.c_double), ("vertex", C.c_double)]
 
 
+class ed_eigs_cfg(C.Structure):
+    _fields_ = [("nev", C.c_int32), ("ncv", C.c_int32), ("max_restarts", C.c_int32), ("start", C.c_int32),
+                ("tol", C.c_double), ("seed", C.c_uint64)]
+
+
+class ed_eigs_result(C.Structure):
+    _fields_ = [("nconv", C.c_int32), ("restarts", C.c_int32), ("n_matvec", C.c_int64), ("launches", C.c_int64),
+                ("max_resid", C.c_double)]
+
+
 class ed_krylov_cfg(C.Structure):
     _fields_ = [("max_steps", C.c_int32), ("reorth", C.c_int32), ("tol", C.c_double), ("accumulate", C.c_int32),
                 ("pad_", C.c_int32)]
@@ -117,6 +127,9 @@ SIGNATURES = {
                                           C.c_void_p]),
     "ed_tridiag_eigen": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_tridiag_expm": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
+    "ed_eigs_lowest": (C.c_int, [C.c_void_p, C.POINTER(ed_eigs_cfg), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                 C.c_int, C.c_void_p, C.POINTER(ed_eigs_result), C.c_void_p]),
+    "ed_dense_sym_eigen": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_krylov_evolve": (C.c_int, [C.c_void_p, C.POINTER(ed_krylov_cfg), C.c_void_p, C.c_int, C.c_int, C.c_void_p,
                                    C.c_void_p, C.c_int, C.POINTER(ed_krylov_result), C.c_void_p]),
 }

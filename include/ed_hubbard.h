@@ -322,6 +322,46 @@ ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double
 ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_t a_mask, double* s_vn,
                                   double* s_ref, void* stream);
 
+/* ---------------------------------------------------- several eigenpairs --
+ * The nev lowest eigenpairs of a real operator (what TotalSpinExcited_*.cu
+ * get from Spectra::SymEigsSolver<cuSpectra::Hubbard<double>> with
+ * SortRule::SmallestAlge, TotalSpinExcited_Lieb_randomHop.cu:133-143; the
+ * GPU copy of its restart logic is TotalSpin/include/SymEigsSolver.cuh):
+ * thick-restart Lanczos (equivalent to implicit restarting with the unwanted
+ * Ritz values as exact shifts) with full reorthogonalisation, every vector
+ * in device memory.  Converged when |last component of z_i| * |f| <
+ * tol * max(eps^(2/3), |theta_i|) for the nev wanted pairs (Spectra's test);
+ * the restart keeps nev + min(nconv, (ncv - nev) / 2) Ritz vectors (ARPACK's
+ * dsaup2 rule, as Spectra).  evals (host, nev, ascending), evecs (nev x rows
+ * at evec_mem, vector i at evecs + i*rows; may be NULL), resid (host, nev;
+ * may be NULL).  ED_ERR_NOT_CONVERGED when max_restarts ran out (the pairs
+ * are still written).  Real operators.  Synchronous. */
+typedef struct {
+    int32_t nev;           /* eigenpairs wanted (lowest algebraic) */
+    int32_t ncv;           /* Krylov subspace size, nev < ncv (the reference: 4 (nev + 1)) */
+    int32_t max_restarts;  /* Spectra's maxit (the reference: 1000) */
+    int32_t start;         /* ED_START_RANDOM | ED_START_USER */
+    double tol;            /* Spectra's tol (the reference: 1e-10) */
+    uint64_t seed;         /* seed of the uniform(-1,1) start vector */
+} ed_eigs_cfg;
+
+typedef struct {
+    int32_t nconv;         /* converged pairs among the nev */
+    int32_t restarts;      /* restarts done */
+    int64_t n_matvec;      /* operator applications */
+    int64_t launches;      /* kernels this call launched */
+    double max_resid;      /* largest residual estimate of the nev pairs */
+} ed_eigs_result;
+
+ed_status ed_eigs_lowest(ed_op* op, const ed_eigs_cfg* cfg, const double* start, int start_mem, double* evals,
+                         double* evecs, int evec_mem, double* resid, ed_eigs_result* res, void* stream);
+
+/* Eigenpairs of a small dense symmetric matrix a (n x n, column-major; the
+ * symmetric part is used): w ascending, z (n x n, column j = unit eigenvector
+ * of w[j]; may be NULL).  Cyclic Jacobi on the host; the Rayleigh-Ritz solve
+ * of ed_eigs_lowest.  ED_ERR_NOT_CONVERGED after 100 sweeps. */
+ed_status ed_dense_sym_eigen(int n, const double* a, double* w, double* z);
+
 /* ------------------------------------------------------- time evolution --
  * psi(t) = exp(-i H t) psi0 in the Krylov space of psi0
  * (Krylov::Make_tridiagonal_eigen + Krylov::Krylov_time_evol,

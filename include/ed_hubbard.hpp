@@ -10,6 +10,9 @@
 //   ed::Lanczos              random_vector / eigen            (HubMatrix_GPU.cuh:477-613)
 //   ed::Krylov               Make_tridiagonal_eigen / Krylov_time_evol on device
 //                            complex vectors                  (HubMatrix_GPU.cuh:619-728)
+//   ed::SymEigsSolver        init / compute / eigenvalues / eigenvectors / info,
+//                            the nev lowest pairs on the device (Spectra::SymEigsSolver
+//                            as TotalSpinExcited_Lieb_randomHop.cu:133-143 uses it)
 // Errors surface as ed::Error (std::runtime_error) carrying the ed_status.
 #pragma once
 
@@ -148,6 +151,36 @@ public:
         b.resize(result.steps + 1);
         return result.e0;
     }
+};
+
+// Spectra::SymEigsSolver<OpType>(op, nev, ncv) with SortRule::SmallestAlge;
+// eigenvectors() is rows x nev column-major (Eigen's MatrixXd layout).
+class SymEigsSolver {
+public:
+    enum class Info { Successful, NotComputed, NotConverging };
+    SymEigsSolver(Hubbard& h, int nev, int ncv) : h_(h), nev_(nev), ncv_(ncv) {}
+    void init(uint64_t seed = 0) { seed_ = seed; }
+    int compute(int maxit = 1000, double tol = 1e-10) {
+        ed_eigs_cfg c{nev_, ncv_, maxit, ED_START_RANDOM, tol, seed_};
+        evals_.assign(nev_, 0.0);
+        evecs_.assign((size_t)nev_ * h_.rows(), 0.0);
+        const ed_status st = ed_eigs_lowest(h_.handle(), &c, nullptr, ED_MEM_HOST, evals_.data(), evecs_.data(),
+                                            ED_MEM_HOST, nullptr, &result, nullptr);
+        if (st != ED_OK && st != ED_ERR_NOT_CONVERGED) check(st, "ed_eigs_lowest");
+        info_ = st == ED_OK ? Info::Successful : Info::NotConverging;
+        return result.nconv;
+    }
+    Info info() const { return info_; }
+    const std::vector<double>& eigenvalues() const { return evals_; }
+    const std::vector<double>& eigenvectors() const { return evecs_; }
+    ed_eigs_result result{};
+
+private:
+    Hubbard& h_;
+    int nev_, ncv_;
+    uint64_t seed_ = 0;
+    Info info_ = Info::NotComputed;
+    std::vector<double> evals_, evecs_;
 };
 
 // Krylov<double>: phi0, phi are device arrays of rows() complex values

@@ -68,3 +68,28 @@ def test_tridiag_bad_arguments(edlib):
     lib = _capi.load()
     assert lib.ed_tridiag_eigen(0, None, None, None, None) == 1  # ED_ERR_ARG
     assert lib.ed_tridiag_expm(3, None, None, 1, None, None) == 1  # ED_ERR_ARG
+
+
+@pytest.mark.parametrize("n", [1, 2, 7, 40])
+def test_dense_sym_eigen_against_numpy(edlib, n):
+    """The Rayleigh-Ritz solve of ed_eigs_lowest (cyclic Jacobi) against
+    numpy's eigh, including a matrix with a repeated eigenvalue."""
+    import ctypes as C
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import _capi
+    rng = np.random.default_rng(n)
+    A = rng.standard_normal((n, n))
+    A = A + A.T
+    if n >= 7:
+        Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        d = np.sort(rng.standard_normal(n))
+        d[3] = d[2]
+        A = (Q * d) @ Q.T
+    a = np.asfortranarray(A)
+    w = np.empty(n)
+    z = np.empty((n, n), order="F")
+    assert _capi.load().ed_dense_sym_eigen(n, a.ctypes.data_as(C.c_void_p), w.ctypes.data_as(C.c_void_p),
+                                           z.ctypes.data_as(C.c_void_p)) == 0
+    wr = np.linalg.eigvalsh(A)
+    assert np.max(np.abs(w - wr)) < 1e-13 * max(1.0, np.max(np.abs(wr))) * n
+    assert np.max(np.abs(z.T @ z - np.eye(n))) < 1e-13 * n
+    assert np.max(np.abs(A @ z - z * w)) < 1e-13 * max(1.0, np.max(np.abs(wr))) * n
