@@ -126,6 +126,7 @@ SIGNATURES = {
     "ed_entanglement_entropy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),
     "ed_tridiag_eigen": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ed_bidiag_singular_values": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_tridiag_expm": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),
     "ed_eigs_lowest": (C.c_int, [C.c_void_p, C.POINTER(ed_eigs_cfg), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                  C.c_int, C.c_void_p, C.POINTER(ed_eigs_result), C.c_void_p]),

@@ -557,6 +557,16 @@ ed_status ed_tridiag_eigen(int n, const double* alpha, const double* offdiag, do
     return ED_OK;
 }
 
+ed_status ed_bidiag_singular_values(int n, const double* d, const double* e, double* s) {
+    if (n < 1 || !d || (n > 1 && !e) || !s) return ED_ERR_ARG;
+    std::vector<double> dd(d, d + n), ee(std::max(n - 1, 1), 0.0);
+    for (int i = 0; i + 1 < n; ++i) ee[i] = e[i];
+    if (!ed::bidiag_singular_values(n, dd.data(), ee.data())) return ED_ERR_NOT_CONVERGED;
+    std::sort(dd.begin(), dd.end(), [](double x, double y) { return x > y; });
+    std::copy(dd.begin(), dd.end(), s);
+    return ED_OK;
+}
+
 ed_status ed_tridiag_expm(int n, const double* alpha, const double* offdiag, int n_times, const double* times,
                           double* out) {
     if (n < 1 || !alpha || (n > 1 && !offdiag) || n_times < 0 || (n_times && (!times || !out))) return ED_ERR_ARG;

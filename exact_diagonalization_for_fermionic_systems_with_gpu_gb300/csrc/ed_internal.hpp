@@ -175,6 +175,13 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
 // The op's Lanczos workspace slot, and the stored basis of its last run:
 // slot k at basis + k * stride holds q_k with w_k = q_k 2^e[k] (e on the device).
 void** lanczos_ws_slot(ed_op* op);
+// Entanglement blocks (column-major m x n, m >= n, at blocks + off[k]) whose
+// singular values the cluster bidiagonalisation computes: handled[k] = 1 and
+// the values, descending, at (*sv_host)[svo[k] ..).  ED_EE_METHOD=gesvd
+// leaves every block to cuSOLVER.
+ed_status ee_bidiag_blocks(int device, cudaStream_t s, const double* blocks, const std::vector<int64_t>& off,
+                           const std::vector<int>& mm, const std::vector<int>& nn, const std::vector<int64_t>& svo,
+                           std::vector<double>* sv_host, std::vector<char>* handled);
 void lanczos_basis(void* ws_slot, const int64_t** basis, int64_t* stride, const int** e_dev);
 
 }  // namespace ed

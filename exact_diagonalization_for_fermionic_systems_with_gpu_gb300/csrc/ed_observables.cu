@@ -281,7 +281,7 @@ EePool* ee_pool(int device) {
 
 ed_status ee_block_svd(int device, cudaStream_t s, double* blocks, const std::vector<int64_t>& off,
                        const std::vector<int>& mm, const std::vector<int>& nn, const std::vector<int64_t>& svo,
-                       double* sv_all) {
+                       double* sv_all, const std::vector<char>& skip) {
     EePool* pool = ee_pool(device);
     std::lock_guard<std::mutex> g(pool->mu);
     const int K = ee_workers();
@@ -297,7 +297,8 @@ ed_status ee_block_svd(int device, cudaStream_t s, double* blocks, const std::ve
     // largest first, each to the least-loaded worker (cost ~ m n^2)
     std::vector<int> order;
     for (size_t k = 0; k < off.size(); ++k)
-        if (nn[k] > 0) order.push_back((int)k);
+        if (nn[k] > 0 && !skip[k]) order.push_back((int)k);
+    if (order.empty()) return ED_OK;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
         return (double)mm[a] * nn[a] * nn[a] > (double)mm[b] * nn[b] * nn[b];
     });
@@ -815,15 +816,27 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
         nnv[k] = std::min(rA[k], cB[k]);
         svo[k + 1] = svo[k] + nnv[k];
     }
+    // blocks that fit a thread-block cluster: Householder bidiagonalisation
+    // on the device + bidiagonal SVD on the host; the rest through cuSOLVER
+    std::vector<double> hs(std::max<int64_t>(svo.back(), 1), 0.0);
+    std::vector<char> done;
+    if (st == ED_OK) st = ed::ee_bidiag_blocks(op->device, s, blocks, off, mmv, nnv, svo, &hs, &done);
+    bool rest = false;
+    for (size_t k = 0; k < off.size(); ++k) rest = rest || (!done.empty() && !done[k] && nnv[k] > 0);
     double* sv_all = nullptr;
-    if (cudaMalloc(&sv_all, sizeof(double) * std::max<int64_t>(svo.back(), 1)) != cudaSuccess) st = ED_ERR_ALLOC;
-    if (st == ED_OK) st = ee_block_svd(op->device, s, blocks, off, mmv, nnv, svo, sv_all);
+    if (st == ED_OK && rest) {
+        if (cudaMalloc(&sv_all, sizeof(double) * std::max<int64_t>(svo.back(), 1)) != cudaSuccess) st = ED_ERR_ALLOC;
+        if (st == ED_OK) st = ee_block_svd(op->device, s, blocks, off, mmv, nnv, svo, sv_all, done);
+        std::vector<double> hg(std::max<int64_t>(svo.back(), 1));
+        if (st == ED_OK &&
+            (cudaMemcpyAsync(hg.data(), sv_all, sizeof(double) * svo.back(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+             cudaStreamSynchronize(s) != cudaSuccess))
+            st = ED_ERR_CUDA;
+        for (size_t k = 0; st == ED_OK && k < off.size(); ++k)
+            if (!done[k]) std::copy(hg.begin() + svo[k], hg.begin() + svo[k + 1], hs.begin() + svo[k]);
+    }
     double svn = 0.0, sref = 0.0;
     if (st == ED_OK) {
-        std::vector<double> hs(std::max<int64_t>(svo.back(), 1));
-        if (cudaMemcpyAsync(hs.data(), sv_all, sizeof(double) * svo.back(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-            cudaStreamSynchronize(s) != cudaSuccess)
-            st = ED_ERR_CUDA;
         // block by block, each in descending order: a fixed summation order
         for (int64_t i = 0; st == ED_OK && i < svo.back(); ++i) {
             const double x = hs[i];

@@ -241,3 +241,119 @@ bool tridiag_expm_e0(int n, const double* a, const double* off, int n_times, con
 }
 
 }  // namespace ed
+
+namespace ed {
+
+// sqrt(a^2 + b^2) without hypot's scaling (the bidiagonal entries here are
+// O(1) down to ~1e-150; a square that underflows gives a zero rotation angle,
+// which costs nothing at the eps |B| accuracy sought).
+inline double rot_norm(double a, double b) { return std::sqrt(a * a + b * b); }
+
+// Singular values of an upper bidiagonal B (d[0..n-1] diagonal, e[0..n-2]
+// superdiagonal; both overwritten, |values| left in d): the Golub-Kahan SVD
+// step with a Wilkinson shift from the trailing 2x2 of B^T B (Golub & Van
+// Loan, Matrix Computations, 4th ed., Algorithms 8.6.1-8.6.2).  A
+// superdiagonal entry deflates when |e_i| <= eps |B|; a diagonal entry with
+// |d_k| <= eps |B| is set to zero and its row is cleared by rotations from the
+// left, which moves the entry along the row until it leaves the block.
+// Absolute accuracy eps |B|, as LAPACK's gesvd gives after a Householder
+// bidiagonalisation.  False when 60 n sweeps did not converge.
+bool bidiag_singular_values(int n, double* d, double* e) {
+    if (n <= 0) return true;
+    const double eps = std::numeric_limits<double>::epsilon();
+    double bnorm = 0.0;
+    for (int i = 0; i < n; ++i) bnorm = std::max(bnorm, std::fabs(d[i]) + (i + 1 < n ? std::fabs(e[i]) : 0.0));
+    if (bnorm == 0.0) return true;
+    const double tol = eps * bnorm;
+    int q = n - 1;  // bottom of the active block
+    long long iters = 0;
+    const long long max_iters = 60LL * n;
+    while (q > 0) {
+        if (std::fabs(e[q - 1]) <= tol) {
+            e[q - 1] = 0.0;
+            --q;
+            continue;
+        }
+        int p = q - 1;
+        while (p > 0 && std::fabs(e[p - 1]) > tol) --p;
+        if (++iters > max_iters) return false;
+        // a (near-)zero diagonal entry in [p, q): clear its row
+        int z = -1;
+        for (int k = p; k < q; ++k)
+            if (std::fabs(d[k]) <= tol) { z = k; break; }
+        if (z >= 0) {
+            d[z] = 0.0;
+            double f = e[z];
+            e[z] = 0.0;
+            for (int j = z + 1; j <= q && f != 0.0; ++j) {
+                // rotate rows (z, j) so that the entry f in row z, column j
+                // goes to zero against d[j]
+                const double r = rot_norm(d[j], f);
+                const double ir = 1.0 / r;
+                const double c = d[j] * ir, s = f * ir;
+                d[j] = r;
+                if (j < q) {
+                    f = -s * e[j];
+                    e[j] = c * e[j];
+                }
+            }
+            continue;
+        }
+        if (std::fabs(d[q]) <= tol) {  // zero at the bottom: clear its column
+            d[q] = 0.0;
+            double f = e[q - 1];
+            e[q - 1] = 0.0;
+            for (int j = q - 1; j >= p && f != 0.0; --j) {
+                const double r = rot_norm(d[j], f);
+                const double ir = 1.0 / r;
+                const double c = d[j] * ir, s = f * ir;
+                d[j] = r;
+                if (j > p) {
+                    f = -s * e[j - 1];
+                    e[j - 1] = c * e[j - 1];
+                }
+            }
+            continue;
+        }
+        // Wilkinson shift: eigenvalue of the trailing 2x2 of B^T B nearer its last entry
+        const double dm = d[q - 1], em = e[q - 1], dq = d[q];
+        const double el = q - 1 > p ? e[q - 2] : 0.0;
+        const double t11 = dm * dm + el * el, t12 = dm * em, t22 = dq * dq + em * em;
+        const double h = 0.5 * (t11 - t22);
+        const double den = h + (h >= 0.0 ? 1.0 : -1.0) * rot_norm(h, t12);
+        const double mu = den != 0.0 ? t22 - t12 * t12 / den : t22;
+        double y = d[p] * d[p] - mu, zz = d[p] * e[p];
+        for (int k = p; k < q; ++k) {
+            // right rotation on columns (k, k+1): zero zz against y
+            double r = rot_norm(y, zz);
+            double ir = r != 0.0 ? 1.0 / r : 0.0;
+            double c = r != 0.0 ? y * ir : 1.0, s = -zz * ir;
+            if (k > p) e[k - 1] = r;
+            // [d_k e_k; 0 d_{k+1}] * [[c, s], [-s, c]] (the bulge below the diagonal)
+            const double dk = d[k], ek = e[k], dk1 = d[k + 1];
+            double a11 = c * dk - s * ek;
+            double a12 = s * dk + c * ek;
+            double a21 = -s * dk1;
+            double a22 = c * dk1;
+            // left rotation on rows (k, k+1): zero a21 against a11
+            r = rot_norm(a11, a21);
+            ir = r != 0.0 ? 1.0 / r : 0.0;
+            c = r != 0.0 ? a11 * ir : 1.0;
+            s = -a21 * ir;
+            d[k] = r;
+            // rows: [c -s; s c] * [[a11 a12 0], [a21 a22 e_{k+1}]]
+            e[k] = c * a12 - s * a22;
+            d[k + 1] = s * a12 + c * a22;
+            if (k + 1 < q) {
+                const double ek1 = e[k + 1];
+                y = e[k];
+                zz = -s * ek1;      // bulge at (k, k+2)
+                e[k + 1] = c * ek1;
+            }
+        }
+    }
+    for (int i = 0; i < n; ++i) d[i] = std::fabs(d[i]);
+    return true;
+}
+
+}  // namespace ed

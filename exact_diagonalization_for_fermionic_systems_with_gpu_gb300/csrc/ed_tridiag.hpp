@@ -28,4 +28,8 @@ void tri_apply_z(const std::vector<TriRot>& rots, double* v);   // v <- Z v
 // out[t][k] = (exp(-i T times[t]) e_0)_k as interleaved (re, im), n_times x 2n doubles.
 bool tridiag_expm_e0(int n, const double* a, const double* off, int n_times, const double* times, double* out);
 
+// Singular values of the upper bidiagonal (d, e) (both overwritten; the
+// values, unsorted and nonnegative, in d).  False when not converged.
+bool bidiag_singular_values(int n, double* d, double* e);
+
 }  // namespace ed

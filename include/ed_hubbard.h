@@ -254,6 +254,12 @@ ed_status ed_tridiag_lowest(int n, const double* alpha, const double* offdiag,
 ed_status ed_tridiag_eigen(int n, const double* alpha, const double* offdiag,
                            double* evals, double* z);
 
+/* Singular values (descending) of the upper bidiagonal with diagonal d
+ * (n) and superdiagonal e (n-1): Golub-Kahan SVD steps on the host, the
+ * second half of the entanglement entropy's block SVD (LAPACK's dbdsqr as
+ * cusolverDnDgesvd uses it).  ED_ERR_NOT_CONVERGED after 60 n sweeps. */
+ed_status ed_bidiag_singular_values(int n, const double* d, const double* e, double* s);
+
 /* out[t] = exp(-i T times[t]) e_0 (n complex values, interleaved re, im;
  * n_times x 2n doubles): the Krylov propagator coefficients of
  * Krylov::Krylov_time_evol (HubMatrix_GPU.cuh:684-690).  Host in/out. */

@@ -182,3 +182,24 @@ def test_s2_of_ground_states(ed):
     S = (-1 + math.sqrt(1 + 4 * s2)) / 2
     assert abs(s2 - (0.25 + sxy)) < 1e-14
     assert abs(2 * S - round(2 * S)) < 1e-6 and round(2 * S) % 2 == 1
+
+
+def test_entanglement_cluster_bidiag_matches_gesvd(ed, monkeypatch):
+    """The cluster Householder bidiagonalisation + host bidiagonal SVD
+    against cusolverDnDgesvd for every block (ED_EE_METHOD=gesvd), on the
+    open L=12 (6,6) and (7,5) ground states (blocks up to 400 x 400) and a
+    random vector (no small singular values)."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import observables as ob, sweeps
+    eu, edn = sweeps.mbl_disorder(2, 12, 6.0)
+    for qu, qd in ((6, 6), (7, 5)):
+        op = ed.Hubbard(ed.H_TBq(12, qu).extend(sweeps.mbl_chain_terms(eu)),
+                        ed.H_TBq(12, qd).extend(sweeps.mbl_chain_terms(edn)), 1.0)
+        e0, v = ed.Lanczos().eigen(op, max_steps=300, mode="fixed", seed=1)
+        x = ed.Lanczos().random_vector(op.rows(), 5)
+        x = x / np.linalg.norm(x)
+        for psi, sites in ((v, range(6)), (v, (0, 2, 4, 6, 8, 10)), (x, range(6))):
+            monkeypatch.delenv("ED_EE_METHOD", raising=False)
+            a = ob.entanglement_entropy(op, psi, list(sites))
+            monkeypatch.setenv("ED_EE_METHOD", "gesvd")
+            b = ob.entanglement_entropy(op, psi, list(sites))
+            assert abs(a[0] - b[0]) < 1e-12 and abs(a[1] - b[1]) < 1e-10 * max(1.0, b[1])

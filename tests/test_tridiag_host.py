@@ -93,3 +93,64 @@ def test_dense_sym_eigen_against_numpy(edlib, n):
     assert np.max(np.abs(w - wr)) < 1e-13 * max(1.0, np.max(np.abs(wr))) * n
     assert np.max(np.abs(z.T @ z - np.eye(n))) < 1e-13 * n
     assert np.max(np.abs(A @ z - z * w)) < 1e-13 * max(1.0, np.max(np.abs(wr))) * n
+
+
+def bidiag_cases():
+    rng = np.random.default_rng(11)
+    yield np.array([3.0]), np.zeros(0)
+    yield rng.standard_normal(2), rng.standard_normal(1)
+    yield rng.standard_normal(50), rng.standard_normal(49)
+    d = rng.standard_normal(40)
+    d[[0, 17, 39]] = 0.0  # zero diagonal entries, top / middle / bottom
+    yield d, rng.standard_normal(39)
+    e = rng.standard_normal(59)
+    e[[5, 30]] = 0.0
+    yield rng.standard_normal(60), e
+    # graded: singular values over 30 decades, as a ground state's Schmidt values
+    yield np.exp(-np.arange(80) * 0.9), np.exp(-np.arange(79) * 0.9) * 0.3
+    # the bidiagonal of a Householder reduction of a low-rank-plus-noise block
+    A = rng.standard_normal((120, 5)) @ rng.standard_normal((5, 100)) + 1e-13 * rng.standard_normal((120, 100))
+    yield householder_bidiag(A)
+
+
+def householder_bidiag(A):
+    """(d, e) of an upper bidiagonal B with the singular values of A (m >= n),
+    by alternating Householder reflections (numpy, small sizes)."""
+    A = A.copy()
+    m, n = A.shape
+    d, e = np.zeros(n), np.zeros(max(n - 1, 0))
+
+    def reflect(x):
+        a, rest = x[0], np.linalg.norm(x[1:])
+        if rest == 0.0:
+            return np.zeros_like(x), 0.0, a
+        b = -np.copysign(np.hypot(a, rest), a)
+        v = x.copy()
+        v[0] = 1.0
+        v[1:] = x[1:] / (a - b)
+        return v, (b - a) / b, b
+
+    for k in range(n):
+        v, tau, d[k] = reflect(A[k:, k])
+        A[k:, k + 1:] -= tau * np.outer(v, v @ A[k:, k + 1:])
+        if k < n - 1:
+            u, tau, e[k] = reflect(A[k, k + 1:])
+            A[k + 1:, k + 1:] -= tau * np.outer(A[k + 1:, k + 1:] @ u, u)
+    return d, e
+
+
+@pytest.mark.parametrize("k", range(7))
+def test_bidiag_singular_values_against_numpy(edlib, k):
+    import ctypes as C
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import _capi
+    d, e = list(bidiag_cases())[k]
+    n = d.size
+    B = np.diag(d) + (np.diag(e, 1) if n > 1 else 0)
+    ref = np.linalg.svd(B, compute_uv=False)
+    s = np.empty(n)
+    ptr = lambda a: a.ctypes.data_as(C.c_void_p)
+    ee = np.ascontiguousarray(e) if n > 1 else np.zeros(1)
+    assert _capi.load().ed_bidiag_singular_values(n, ptr(np.ascontiguousarray(d)), ptr(ee), ptr(s)) == 0
+    assert np.max(np.abs(s - ref)) < 8e-16 * n * ref[0]
+    if k == 5:  # graded values keep about eps * |B| absolute accuracy
+        assert np.max(np.abs(s - ref)) < 1e-15
