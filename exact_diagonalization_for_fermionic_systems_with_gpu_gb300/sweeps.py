@@ -209,6 +209,36 @@ FLUX_HEADER = "#       Phi       E0        dE0/dPhi        d2E0/dPhi2      "
 MBL_HEADER = "#       xid       Nup       Ndn       E0        S_A       n_up(i)...      n_dn(i)...      "
 
 
+# The plain per-instance GPU form the tuned sweep is compared with: the
+# generic matvec kernel, host-driven per-step Lanczos launches, and one
+# cusolverDnDgesvd per entanglement block on one stream.
+PLAIN_ENV = {"ED_MATVEC": "generic", "ED_LZ_FUSED": "0", "ED_EE_METHOD": "gesvd", "ED_EE_STREAMS": "1"}
+
+
+def _run(a, n, form: str):
+    import os
+    saved = {k: os.environ.get(k) for k in PLAIN_ENV}
+    if form == "plain":
+        os.environ.update(PLAIN_ENV)
+    try:
+        tm = SweepTiming()
+        if a.what == "flux":
+            if a.warmup:
+                flux_sweep(flux_phis(n)[: a.warmup], steps=a.steps, mode=a.mode, seed=a.seed)
+            pts = flux_sweep(flux_phis(n), steps=a.steps, mode=a.mode, seed=a.seed, timing=tm)
+        else:
+            if a.warmup:
+                mbl_sweep(realisations=range(a.warmup), steps=a.steps, mode=a.mode, seed=a.seed + 1)
+            pts = mbl_sweep(n, steps=a.steps, mode=a.mode, seed=a.seed, timing=tm)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    return pts, tm
+
+
 def main(argv: Optional[Sequence[str]] = None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--what", choices=["flux", "mbl"], default="mbl")
@@ -218,32 +248,39 @@ def main(argv: Optional[Sequence[str]] = None) -> None:
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=1, help="instances run (untimed) before the sweep")
     ap.add_argument("--out", default=None, help="append the result rows to this .dat file")
+    ap.add_argument("--form", choices=["tuned", "plain", "compare"], default="tuned",
+                    help="plain: the per-instance form of PLAIN_ENV; compare: both, with the largest "
+                         "differences of their outputs")
     a = ap.parse_args(argv)
     import torch
     if not torch.cuda.is_available():
         raise SystemExit("sweeps need a CUDA device")
-    tm = SweepTiming()
     if a.what == "flux":
         n = 16 if a.n is None else a.n
-        if a.warmup:
-            flux_sweep(flux_phis(n)[: a.warmup], steps=a.steps, mode=a.mode, seed=a.seed)
-        pts = flux_sweep(flux_phis(n), steps=a.steps, mode=a.mode, seed=a.seed, timing=tm)
-        rows, header = flux_rows(pts), FLUX_HEADER
         cfg = {"workload": f"Kagome12 6+6 U=4, {n} twists in [0, 2pi/{L.KAGOME12_LX:g}], complex FP64",
                "lanczos_steps": a.steps, "response_steps": 200, "mode": a.mode}
     else:
         n = 64 if a.n is None else a.n
-        if a.warmup:
-            mbl_sweep(realisations=range(a.warmup), steps=a.steps, mode=a.mode, seed=a.seed + 1)
-        pts = mbl_sweep(n, steps=a.steps, mode=a.mode, seed=a.seed, timing=tm)
-        rows, header = mbl_rows(pts), MBL_HEADER
         cfg = {"workload": f"open chain L=12 t=1 U=1 W=6, {n} realisations x sectors (6,6),(7,5),(8,4)",
                "lanczos_steps": a.steps, "mode": a.mode, "entanglement_sites": "0..5"}
+    forms = ["tuned", "plain"] if a.form == "compare" else [a.form]
+    runs = {f: _run(a, n, f) for f in forms}
+    pts, tm = runs[forms[0]]
+    rows, header = (flux_rows(pts), FLUX_HEADER) if a.what == "flux" else (mbl_rows(pts), MBL_HEADER)
     if a.out:
         from .datio import append_rows
         append_rows(a.out, header, rows)
-    print(json.dumps({"sweep": a.what, "config": cfg, **tm.summary(),
-                      "ms_per_instance_median": round(1e3 * float(np.median(tm.per_instance)), 3)}))
+    line = {"sweep": a.what, "form": forms[0], "config": cfg, **tm.summary(),
+            "ms_per_instance_median": round(1e3 * float(np.median(tm.per_instance)), 3)}
+    if a.form == "compare":
+        p_pts, p_tm = runs["plain"]
+        diff = np.abs(np.array(rows, dtype=float) -
+                      np.array(flux_rows(p_pts) if a.what == "flux" else mbl_rows(p_pts), dtype=float))
+        line["plain"] = p_tm.summary()
+        line["speedup_vs_plain"] = round(p_tm.total_s / tm.total_s, 3)
+        line["max_abs_diff_vs_plain"] = {"E0": float(np.max(diff[:, 1 if a.what == "flux" else 3])),
+                                         "all_columns": float(np.max(diff))}
+    print(json.dumps(line))
 
 
 if __name__ == "__main__":
