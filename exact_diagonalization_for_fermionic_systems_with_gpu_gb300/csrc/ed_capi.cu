@@ -356,6 +356,46 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
          upload(&op->d_dnEntC, dn_ent.data(), dn_ent.size()) == cudaSuccess &&
          cudaMalloc(&op->d_err, sizeof(int)) == cudaSuccess && cudaMemset(op->d_err, 0, sizeof(int)) == cudaSuccess;
     if (!ok) { ed_op_destroy(op); return ED_ERR_ALLOC; }
+    // class segments for multi-class tables with at most kSegCls classes
+    auto segments = [](const ed::SpinTable& t, std::vector<uint32_t>* se, std::vector<uint32_t>* sp) {
+        se->assign(t.count, 0u);
+        sp->assign(t.count, 0u);
+        for (int64_t r = 0; r < t.count; ++r) {
+            int k = 0;
+            uint32_t e = 0, p = 0;
+            for (int c = 0; c < ed::kSegCls; ++c) {
+                while (k < t.len[r] && ((t.ent[(size_t)k * t.count + r] >> ed::kClassShift) & ed::kClassMask) == (uint32_t)c &&
+                       !(t.ent[(size_t)k * t.count + r] & ed::kSignBit))
+                    ++k;
+                p |= (uint32_t)k << (8 * c);
+                while (k < t.len[r] && ((t.ent[(size_t)k * t.count + r] >> ed::kClassShift) & ed::kClassMask) == (uint32_t)c)
+                    ++k;
+                e |= (uint32_t)k << (8 * c);
+            }
+            (*se)[r] = e;
+            (*sp)[r] = p;
+        }
+    };
+    a.upSegE = a.upSegP = a.dnSegE = a.dnSegP = nullptr;
+    a.mergeMC = 0;
+    if ((a.nclsUP > 1 || a.nclsDN > 1) && a.nclsUP <= ed::kSegCls && a.nclsDN <= ed::kSegCls &&
+        !std::getenv("ED_NO_SEG")) {
+        std::vector<uint32_t> use, usp, dse, dsp;
+        segments(tu, &use, &usp);
+        segments(td, &dse, &dsp);
+        if (upload(&op->d_upSegE, use.data(), use.size()) != cudaSuccess ||
+            upload(&op->d_upSegP, usp.data(), usp.size()) != cudaSuccess ||
+            upload(&op->d_dnSegE, dse.data(), dse.size()) != cudaSuccess ||
+            upload(&op->d_dnSegP, dsp.data(), dsp.size()) != cudaSuccess) {
+            ed_op_destroy(op);
+            return ED_ERR_ALLOC;
+        }
+        a.upSegE = op->d_upSegE;
+        a.upSegP = op->d_upSegP;
+        a.dnSegE = op->d_dnSegE;
+        a.dnSegP = op->d_dnSegP;
+        a.mergeMC = (a.nclsUP == a.nclsDN && tu.coef == td.coef) ? 1 : 0;
+    }
     a.upPtr = op->d_upPtr;
     a.upEntC = op->d_upEntC;
     a.dnPtr = op->d_dnPtr;
@@ -443,6 +483,7 @@ ed_status ed_op_destroy(ed_op* op) {
     cudaFree(op->d_upNpos); cudaFree(op->d_dnNpos);
     cudaFree(op->d_upPtr); cudaFree(op->d_upEntC); cudaFree(op->d_dnPtr); cudaFree(op->d_dnEntC);
     cudaFree(op->d_dnSched); cudaFree(op->d_dnSteps); cudaFree(op->d_rowStart); cudaFree(op->d_rowList); cudaFree(op->d_rowQueue);
+    cudaFree(op->d_upSegE); cudaFree(op->d_upSegP); cudaFree(op->d_dnSegE); cudaFree(op->d_dnSegP);
     cudaFree(op->d_permDN); cudaFree(op->d_sched32); cudaFree(op->d_steps32); cudaFree(op->d_dDNqP);
     cudaFree(op->d_stDNp); cudaFree(op->d_sdn);
     cudaFree(op->d_err);

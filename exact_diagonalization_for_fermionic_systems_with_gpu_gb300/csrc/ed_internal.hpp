@@ -13,6 +13,7 @@
 namespace ed {
 
 constexpr int kMaxCls = kMaxClasses;
+constexpr int kSegCls = 4;  // classes a segmented row table describes (one byte each)
 
 // Everything the matvec kernel needs, passed by value (< 4 KB).
 struct MvArgs {
@@ -66,6 +67,15 @@ struct MvArgs {
     // Lanczos per-step reduction outputs
     void* lz;             // LzState* (device)
     int step;
+    // class segments of every row (tables with at most kSegCls classes,
+    // entries sorted by class, + before -): byte c of segE[r] is the end of
+    // class c's entries in row r, byte c of segP[r] the end of its + entries
+    // (both relative to the row start); null for tables with more classes
+    const uint32_t* upSegE;
+    const uint32_t* upSegP;
+    const uint32_t* dnSegE;
+    const uint32_t* dnSegP;
+    int mergeMC;          // segmented tables with equal class lists: one product per class
     // coefficient classes, interleaved (re, im), scale 2^-Fc
     int64_t coefUP[2 * kMaxCls];
     int64_t coefDN[2 * kMaxCls];
@@ -107,6 +117,7 @@ struct ed_op {
     uint16_t* d_dnSched = nullptr;
     uint8_t* d_dnSteps = nullptr;
     uint32_t *d_rowStart = nullptr, *d_rowList = nullptr, *d_rowQueue = nullptr;
+    uint32_t *d_upSegE = nullptr, *d_upSegP = nullptr, *d_dnSegE = nullptr, *d_dnSegP = nullptr;
     int* d_err = nullptr;
     int64_t *d_dUPq = nullptr, *d_dDNq = nullptr;
     uint64_t *d_stUP = nullptr, *d_stDN = nullptr;

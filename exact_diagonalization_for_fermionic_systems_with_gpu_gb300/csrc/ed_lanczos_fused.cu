@@ -149,7 +149,7 @@ __device__ __forceinline__ void slot_done(LzState* lz, int k, int e, i128 ss, ui
 
 }  // namespace
 
-template <bool CPLX, bool FAST, bool SCHED>
+template <bool CPLX, bool FAST, bool SCHED, bool SEG = false>
 __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, const LzFusedArgs f) {
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ uint32_t uoff[kTmaUpStage];
@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
         {
             i128 dot = 0;
             uint64_t mx = 0;
-            tma_rows<CPLX, 1, FAST, true, SCHED, true>(a, S, xq, f.u, nullptr, rc, 0, s_u, dot, mx,
+            tma_rows<CPLX, 1, FAST, true, SCHED, true, SEG>(a, S, xq, f.u, nullptr, rc, 0, s_u, dot, mx,
                                                        f.taken + (j & 1), &s_next);
             if (give_up) return;
             if (stamp) st[1] = global_ns();
@@ -328,9 +328,12 @@ cudaError_t launch_lz_fused(const ed_op* op, const LzFusedArgs& f, cudaStream_t 
     if (op->tma_smem <= 0) return cudaErrorNotSupported;
     const void* fn;
     if (op->cplx)
-        fn = op->mv_fast ? (const void*)k_lz_fused<true, true, false> : (const void*)k_lz_fused<true, false, false>;
+        fn = op->mv_fast ? (const void*)k_lz_fused<true, true, false>
+             : op->mv.upSegE ? (const void*)k_lz_fused<true, false, false, true>
+                             : (const void*)k_lz_fused<true, false, false>;
     else if (!op->mv_fast)
-        fn = (const void*)k_lz_fused<false, false, false>;
+        fn = op->mv.upSegE ? (const void*)k_lz_fused<false, false, false, true>
+                           : (const void*)k_lz_fused<false, false, false>;
     else
         fn = op->mv.dnSched ? (const void*)k_lz_fused<false, true, true> : (const void*)k_lz_fused<false, true, false>;
     cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, op->tma_smem);

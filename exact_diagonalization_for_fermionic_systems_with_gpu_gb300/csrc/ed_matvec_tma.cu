@@ -19,7 +19,7 @@ using namespace dev;
 
 constexpr double kRowCostUp = 0.8;  // up-term share of a row's cost at the mean up-row length
 
-template <bool CPLX, int OUT, bool FAST, bool SCHED>
+template <bool CPLX, int OUT, bool FAST, bool SCHED, bool SEG = false>
 __global__ void __launch_bounds__(kTmaThreads, 2) k_matvec_tma(const MvArgs a) {
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ uint32_t uoff[kTmaUpStage];
@@ -52,7 +52,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_matvec_tma(const MvArgs a) {
     uint64_t mx = 0;
     uint32_t rc = 0;
     if (!give_up) {
-        tma_rows<CPLX, OUT, FAST, false, SCHED, false>(a, S, a.xq, a.uq, a.y, rc, E_out, s_u, dot, mx);
+        tma_rows<CPLX, OUT, FAST, false, SCHED, false, SEG>(a, S, a.xq, a.uq, a.y, rc, E_out, s_u, dot, mx);
     } else if (threadIdx.x == 0 && has_row) {
         tma::mbar_wait(&S.bar[0], 0);  // the first row copy must land before the CTA exits
     }
@@ -101,9 +101,9 @@ int tma_plan(const ed_op* op, MvArgs* a) {
     return (int)off;
 }
 
-template <bool CPLX, int OUT, bool FAST, bool SCHED>
+template <bool CPLX, int OUT, bool FAST, bool SCHED, bool SEG = false>
 static cudaError_t launch_tma4(const ed_op* op, const MvArgs& a, cudaStream_t s) {
-    auto kern = k_matvec_tma<CPLX, OUT, FAST, SCHED>;
+    auto kern = k_matvec_tma<CPLX, OUT, FAST, SCHED, SEG>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, op->tma_smem);
     if (e != cudaSuccess) return e;
     kern<<<op->tma_grid, kTmaThreads, op->tma_smem, s>>>(a);
@@ -112,9 +112,12 @@ static cudaError_t launch_tma4(const ed_op* op, const MvArgs& a, cudaStream_t s)
 
 template <int OUT>
 static cudaError_t launch_tma_out(const ed_op* op, const MvArgs& a, cudaStream_t s) {
-    if (op->cplx)
-        return op->mv_fast ? launch_tma4<true, OUT, true, false>(op, a, s) : launch_tma4<true, OUT, false, false>(op, a, s);
-    if (!op->mv_fast) return launch_tma4<false, OUT, false, false>(op, a, s);
+    if (op->cplx) {
+        if (op->mv_fast) return launch_tma4<true, OUT, true, false>(op, a, s);
+        return a.upSegE ? launch_tma4<true, OUT, false, false, true>(op, a, s) : launch_tma4<true, OUT, false, false>(op, a, s);
+    }
+    if (!op->mv_fast)
+        return a.upSegE ? launch_tma4<false, OUT, false, false, true>(op, a, s) : launch_tma4<false, OUT, false, false>(op, a, s);
     return a.dnSched ? launch_tma4<false, OUT, true, true>(op, a, s) : launch_tma4<false, OUT, true, false>(op, a, s);
 }
 
@@ -126,9 +129,12 @@ int tma_grid(const ed_op* op) {
     int per_sm = 0;
     const void* f;
     if (op->cplx)
-        f = op->mv_fast ? (const void*)k_matvec_tma<true, 1, true, false> : (const void*)k_matvec_tma<true, 1, false, false>;
+        f = op->mv_fast ? (const void*)k_matvec_tma<true, 1, true, false>
+            : op->mv.upSegE ? (const void*)k_matvec_tma<true, 1, false, false, true>
+                            : (const void*)k_matvec_tma<true, 1, false, false>;
     else if (!op->mv_fast)
-        f = (const void*)k_matvec_tma<false, 1, false, false>;
+        f = op->mv.upSegE ? (const void*)k_matvec_tma<false, 1, false, false, true>
+                          : (const void*)k_matvec_tma<false, 1, false, false>;
     else
         f = op->mv.dnSched ? (const void*)k_matvec_tma<false, 1, true, true> : (const void*)k_matvec_tma<false, 1, true, false>;
     cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, op->tma_smem);

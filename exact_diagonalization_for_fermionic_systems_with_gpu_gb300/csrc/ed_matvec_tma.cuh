@@ -220,7 +220,7 @@ __device__ __forceinline__ bool tma_first_row_dyn(const MvArgs& a, uint32_t* u) 
     return true;
 }
 
-template <bool CPLX, int OUT, bool FAST, bool COH, bool SCHED, bool DYN>
+template <bool CPLX, int OUT, bool FAST, bool COH, bool SCHED, bool DYN, bool SEG = false>
 __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, const int64_t* __restrict__ xq,
                                          int64_t* __restrict__ uq, double* __restrict__ y, uint32_t& rc, int E_out,
                                          int s_u, i128& dot, uint64_t& mx, unsigned int* taken = nullptr,
@@ -361,6 +361,59 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                     if (a.nclsDN) {
                         apply_class<CPLX>(ar0, ai0, dr0, di0, a.coefDN, 0, unitD, a.Fc);
                         apply_class<CPLX>(ar1, ai1, dr1, di1, a.coefDN, 0, unitD, a.Fc);
+                    }
+                }
+            } else if (SEG) {
+                // at most kSegCls classes: class by class over segments taken
+                // from the rows' class-end bytes (+ entries first), the same
+                // loop bounds for every lane in the up row; with equal class
+                // lists the up and down sums of a class share one product.
+                // The two columns one after the other (register budget).
+                const uint32_t se_u = __ldg(a.upSegE + u), sp_u = __ldg(a.upSegP + u);
+                const int ncl = max(a.nclsUP, a.nclsDN);
+#pragma unroll 1
+                for (int cc = 0; cc < 2; ++cc) {
+                    const uint32_t d = cc ? d1c : d0;
+                    i128& ar = cc ? ar1 : ar0;
+                    i128& ai = cc ? ai1 : ai0;
+                    const uint32_t se = __ldg(a.dnSegE + d), sp = __ldg(a.dnSegP + d);
+                    const uint32_t q0 = S.dptr[d];
+                    uint32_t ub = 0, b = 0;
+                    for (int c = 0; c < ncl; ++c) {
+                        int64_t r = 0, i = 0;
+                        if (c < a.nclsUP) {
+                            const uint32_t up = (sp_u >> (8 * c)) & 0xFFu, ue = (se_u >> (8 * c)) & 0xFFu;
+                            for (uint32_t k = ub; k < up; ++k) acc_up<CPLX, COH>(xq, S.uoff[k] + d, r, i);
+                            for (uint32_t k = up; k < ue; ++k) {
+                                int64_t vr, vi;
+                                up_load<CPLX, COH>(xq, S.uoff[k] + d, vr, vi);
+                                r -= vr;
+                                i -= vi;
+                            }
+                            ub = ue;
+                            if (!a.mergeMC) {
+                                apply_class<CPLX>(ar, ai, r, i, a.coefUP, c, unitU, a.Fc);
+                                r = 0;
+                                i = 0;
+                            }
+                        }
+                        if (c < a.nclsDN) {
+                            const uint32_t pc = (sp >> (8 * c)) & 0xFFu, ec = (se >> (8 * c)) & 0xFFu;
+                            for (uint32_t q = q0 + b; q < q0 + pc; ++q) {
+                                const uint32_t col = (S.dent[q] & kColMask) * W;
+                                r += xrow[col];
+                                if (CPLX) i += xrow[col + 1];
+                            }
+                            for (uint32_t q = q0 + pc; q < q0 + ec; ++q) {
+                                const uint32_t col = (S.dent[q] & kColMask) * W;
+                                r -= xrow[col];
+                                if (CPLX) i -= xrow[col + 1];
+                            }
+                            b = ec;
+                            apply_class<CPLX>(ar, ai, r, i, a.coefDN, c, unitD, a.Fc);
+                        } else if (a.mergeMC) {
+                            apply_class<CPLX>(ar, ai, r, i, a.coefUP, c, unitU, a.Fc);
+                        }
                     }
                 }
             } else {

@@ -165,6 +165,8 @@ def kernel_cases():
         ("kagome12_66_U8", 12, 6, 6, L.kagome12(), L.kagome12(), 8.0),
         ("kagome12_66_U0", 12, 6, 6, L.kagome12(), L.kagome12(), 0.0),
         ("kagome12_54_flux", 12, 5, 4, L.kagome12(flux=0.3), L.kagome12(flux=0.3), 4.0),
+        ("kagome12_66_flux", 12, 6, 6, L.kagome12(flux=0.3), L.kagome12(flux=0.3), 4.0),
+        ("kagome12_66_flux_up_only", 12, 6, 6, L.kagome12(flux=0.3), L.kagome12(), 4.0),
         ("kagome12_55_Kx_2classes", 12, 5, 5, L.kagome12_kinetic_x(), L.kagome12_kinetic_x(), 1.0),
         ("chain12_open_W6_75", 12, 7, 5, L.chain(12, periodic=False, eps=eps12), L.chain(12, periodic=False, eps=eps12), 1.0),
         ("chain8_35", 8, 3, 5, L.chain(8), L.chain(8), 2.0),
