@@ -107,6 +107,8 @@ SIGNATURES = {
     "ed_op_perform_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_lanczos_run": (C.c_int, [C.c_void_p, C.POINTER(ed_lanczos_cfg), C.c_void_p, C.c_int, C.c_void_p,
                                  C.c_int, C.c_void_p, C.c_void_p, C.POINTER(ed_lanczos_result), C.c_void_p]),
+    "ed_lanczos_batch": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(ed_lanczos_cfg), C.c_void_p, C.c_int, C.c_void_p,
+                                   C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_random_vector": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p]),
     "ed_random_vector_device": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p, C.c_void_p]),
     "ed_tridiag_lowest": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

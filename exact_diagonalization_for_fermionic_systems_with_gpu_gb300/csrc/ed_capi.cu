@@ -553,6 +553,15 @@ ed_status ed_lanczos_run(ed_op* op, const ed_lanczos_cfg* cfg, const double* sta
                            reinterpret_cast<cudaStream_t>(stream));
 }
 
+ed_status ed_lanczos_batch(ed_op* const* ops, int n_ops, const ed_lanczos_cfg* cfg, const double* starts, int start_mem,
+                           double* evecs, int evec_mem, double* alpha, double* beta, ed_lanczos_result* res,
+                           void* stream) {
+    if (!ops || n_ops < 1 || !ops[0] || !cfg) return ED_ERR_ARG;
+    if (cudaSetDevice(ops[0]->device) != cudaSuccess) return ED_ERR_CUDA;
+    return ed::lanczos_batch_run(ops, n_ops, cfg, starts, start_mem, evecs, evec_mem, alpha, beta, res,
+                                 reinterpret_cast<cudaStream_t>(stream));
+}
+
 ed_status ed_random_vector(int64_t n, uint64_t seed, double* out_host) {
     if (n < 0 || (n && !out_host)) return ED_ERR_ARG;
     for (int64_t b = 0; b * 4 < n; ++b) {

@@ -186,6 +186,11 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
 // The op's Lanczos workspace slot, and the stored basis of its last run:
 // slot k at basis + k * stride holds q_k with w_k = q_k 2^e[k] (e on the device).
 void** lanczos_ws_slot(ed_op* op);
+// B fixed-step runs of operators sharing their hopping tables in one
+// persistent launch (ed_lanczos.cu).
+ed_status lanczos_batch_run(ed_op* const* ops, int B, const ed_lanczos_cfg* cfg, const double* starts, int start_mem,
+                            double* evecs, int evec_mem, double* alpha_h, double* beta_h, ed_lanczos_result* res,
+                            cudaStream_t s);
 // Entanglement blocks (column-major m x n, m >= n, at blocks + off[k]) whose
 // singular values the cluster bidiagonalisation computes: handled[k] = 1 and
 // the values, descending, at (*sv_host)[svo[k] ..).  ED_EE_METHOD=gesvd

@@ -15,6 +15,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <functional>
 #include <vector>
 
 #include "ed_device.cuh"
@@ -27,6 +28,7 @@ namespace ed {
 using namespace dev;
 
 cudaError_t launch_lz_fused(const ed_op* op, const LzFusedArgs& f, cudaStream_t s);
+cudaError_t launch_lz_batch(const ed_op* op, const LzBatchArgs& f, cudaStream_t s);
 
 constexpr int kLzThreads = 256;
 
@@ -830,6 +832,192 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
         res->residual = resid;
     }
     return ED_OK;
+}
+
+
+// B fixed-step Lanczos runs of operators that share their hopping tables, in
+// one persistent launch (k_lz_batch), each with its own workspace (the op's)
+// and start vector; then each run's T and Ritz vector as lanczos_run forms
+// them from the stored basis.
+ed_status lanczos_batch_run(ed_op* const* ops, int B, const ed_lanczos_cfg* cfg, const double* starts, int start_mem,
+                            double* evecs, int evec_mem, double* alpha_h, double* beta_h, ed_lanczos_result* res,
+                            cudaStream_t s) {
+    if (!ops || B < 1 || B > kLzBatchMax || !cfg || cfg->max_steps < 1 || cfg->max_steps > 100000) return ED_ERR_ARG;
+    if (cfg->mode != ED_LANCZOS_FIXED || cfg->reorth || cfg->ritz == ED_RITZ_RECOMPUTE) return ED_ERR_ARG;
+    if (cfg->start == ED_START_USER && !starts) return ED_ERR_ARG;
+    ed_op* op0 = ops[0];
+    for (int b = 0; b < B; ++b) {
+        const ed_op* o = ops[b];
+        if (!o) return ED_ERR_ARG;
+        if (o->cplx || !o->mv_fast || !o->mv.dnSched || o->tma_smem <= 0 || o->striped) return ED_ERR_NOT_BUILT;
+        if (o->device != op0->device || o->dimUP != op0->dimUP || o->dimDN != op0->dimDN || o->mask != op0->mask)
+            return ED_ERR_ARG;
+        // the kernel walks op0's tables for every instance
+        if (o->tup.ent != op0->tup.ent || o->tup.len != op0->tup.len || o->tup.npos != op0->tup.npos ||
+            o->tdn.ent != op0->tdn.ent || o->tdn.len != op0->tdn.len || o->tdn.npos != op0->tdn.npos)
+            return ED_ERR_ARG;
+    }
+    const int64_t DW = op0->D;
+    const int max_steps = cfg->max_steps;
+    const bool want_ritz = cfg->ritz == ED_RITZ_STORED && evecs;
+    std::vector<Workspace*> ws(B);
+    std::vector<LzInst> inst(B);
+    int64_t launches = 0;
+    for (int b = 0; b < B; ++b) {
+        ed_op* op = ops[b];
+        void** slot = lanczos_ws_slot(op);
+        if (!*slot) *slot = new WsHolder();
+        Workspace* w = &reinterpret_cast<WsHolder*>(*slot)->ws;
+        ed_status st = ensure_ws(op, w, (size_t)max_steps + 1, DW, max_steps);
+        if (st != ED_OK) return st;
+        ws[b] = w;
+        LZ_CK(cudaMemsetAsync(w->h.counter, 0, sizeof(unsigned int) * 4, s));
+        LZ_CK(cudaMemsetAsync(w->ritz_ctr, 0, sizeof(unsigned int), s));
+        if (cfg->start == ED_START_USER) {
+            LZ_CK(cudaMemcpyAsync(w->fbuf, starts + (size_t)b * DW, sizeof(double) * DW,
+                                  start_mem == ED_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+        } else {
+            LZ_CK(launch_random(w->fbuf, DW, cfg->seed + (uint64_t)b, s));
+            ++launches;
+        }
+        LZ_CK(launch_emax(w->fbuf, DW, w->emax, w->flag, s));
+        k_lz_start<<<lz_grid(DW), kLzThreads, 0, s>>>(w->fbuf, DW, w->emax, w->flag, w->basis, w->lz);
+        LZ_CK(cudaGetLastError());
+        launches += 2;
+        const MvArgs& m = op->mv;
+        inst[b] = LzInst{w->basis, w->u, w->lz, m.dUPq, m.dDNq, m.Uq, m.coefUP[0], m.coefDN[0], m.Fc,
+                         m.unitUP, m.unitDN, m.mergeUD, m.nclsUP, m.nclsDN, m.bq_bits, 0};
+    }
+    // One persistent launch per range of instances; a range whose row
+    // buffers do not fit shared memory is split in two.
+    // Sync buffer: barrier counter at 0, item-queue counters at 64,
+    // reduction sets at 128.
+    std::function<ed_status(int, int)> run = [&](int b0, int b1) -> ed_status {
+        const int Bn = b1 - b0;
+        const size_t sync_bytes = 128 + sizeof(LzRedSet) * 4 * (size_t)Bn;
+        unsigned char* sync = nullptr;
+        LzInst* dinst = nullptr;
+        if (cudaMallocAsync(&sync, sync_bytes, s) != cudaSuccess) return ED_ERR_ALLOC;
+        if (cudaMallocAsync(&dinst, sizeof(LzInst) * Bn, s) != cudaSuccess) {
+            cudaFreeAsync(sync, s);
+            return ED_ERR_ALLOC;
+        }
+        cudaError_t le = cudaMemsetAsync(sync, 0, sync_bytes, s);
+        if (le == cudaSuccess)
+            le = cudaMemcpyAsync(dinst, inst.data() + b0, sizeof(LzInst) * Bn, cudaMemcpyHostToDevice, s);
+        if (le == cudaSuccess) {
+            LzBatchArgs fa{dinst, Bn, 0, max_steps, ws[0]->stride, DW, reinterpret_cast<unsigned int*>(sync),
+                           reinterpret_cast<LzRedSet*>(sync + 128), reinterpret_cast<unsigned int*>(sync + 64)};
+            le = launch_lz_batch(op0, fa, s);
+        }
+        cudaFreeAsync(sync, s);
+        cudaFreeAsync(dinst, s);
+        if (le == cudaSuccess) {
+            ++launches;
+            return ED_OK;
+        }
+        cudaGetLastError();
+        if (le == cudaErrorNotSupported || le == cudaErrorCooperativeLaunchTooLarge) {
+            if (Bn == 1) return ED_ERR_NOT_BUILT;
+            const int mid = b0 + (Bn + 1) / 2;
+            const ed_status st = run(b0, mid);
+            return st != ED_OK ? st : run(mid, b1);
+        }
+        return ED_ERR_CUDA;
+    };
+    {
+        const ed_status st = run(0, B);
+        if (st != ED_OK) {
+            cudaStreamSynchronize(s);
+            return st;
+        }
+    }
+    // every instance: T, status, Ritz vector
+    ed_status result = ED_OK;
+    for (int b = 0; b < B && result == ED_OK; ++b) {
+        ed_op* op = ops[b];
+        Workspace* w = ws[b];
+        const LzState& H = w->h;
+        LzState hs;
+        std::vector<double> ha(max_steps + 2), hb(max_steps + 2), tri(max_steps + 2);
+        int n = max_steps, err_flag = 0;
+        if (cudaMemcpyAsync(&hs, w->lz, sizeof(LzState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(ha.data(), H.alpha, sizeof(double) * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(hb.data(), H.beta, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(&err_flag, op0->d_err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            result = ED_ERR_CUDA;
+            break;
+        }
+        if (err_flag) {
+            cudaMemset(op0->d_err, 0, sizeof(int));
+            result = ED_ERR_TIMEOUT;
+            break;
+        }
+        if (hs.status == 7) {
+            int nb = n;
+            for (int k = 0; k < n; ++k)
+                if (hb[k + 1] == 0.0) { nb = k + 1; break; }
+            n = std::max(1, nb);
+        } else if (hs.status != 0) {
+            result = ED_ERR_NONFINITE;
+            break;
+        }
+        tri[0] = tridiag_lowest_host(n, ha.data(), hb.data() + 1, tri.data() + 1);
+        if (want_ritz) {
+            std::vector<int> ev(n);
+            if (cudaMemcpy(ev.data(), H.e, sizeof(int) * n, cudaMemcpyDeviceToHost) != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+            std::vector<double> r(n);
+            for (int k = 0; k < n; ++k) r[k] = tri[1 + k] / hb[k] * std::ldexp(1.0, ev[k]);
+            std::vector<int64_t> rt;
+            std::vector<int> rs;
+            int F;
+            fx_coefs(r, &rt, &rs, &F);
+            double* out = evec_mem == ED_MEM_DEVICE ? evecs + (size_t)b * DW : w->fbuf;
+            int64_t gr = (DW / 2 + kLzThreads - 1) / kLzThreads;
+            gr = std::max<int64_t>(1, std::min<int64_t>(gr, kLzMaxPartials));
+            if (cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+                cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+            k_ritz<<<(int)gr, kLzThreads, 0, s>>>(w->basis, DW, w->stride, n, w->coef_rt, w->coef_rs, F, out,
+                                                  w->ritz_part, w->ritz_ctr, w->inv_norm);
+            k_scale<<<lz_grid(DW), kLzThreads, 0, s>>>(out, DW, w->inv_norm);
+            launches += 2;
+            if (cudaGetLastError() != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+            if (evec_mem != ED_MEM_DEVICE &&
+                cudaMemcpyAsync(evecs + (size_t)b * DW, out, sizeof(double) * DW, cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+            if (cudaStreamSynchronize(s) != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+        }
+        if (alpha_h) std::memcpy(alpha_h + (size_t)b * max_steps, ha.data(), sizeof(double) * n);
+        if (beta_h) std::memcpy(beta_h + (size_t)b * (max_steps + 1), hb.data(), sizeof(double) * (n + 1));
+        if (res) {
+            ed_lanczos_result& R = res[b];
+            std::memset(&R, 0, sizeof(R));
+            R.e0 = tri[0];
+            R.steps = n;
+            R.status = hs.status == 7 ? ED_ERR_BREAKDOWN : ED_OK;
+            R.min_bits = hs.min_bits;
+            R.residual = std::fabs(hb[n] * tri[n]);
+            R.n_matvec = max_steps;
+            R.launches = b == 0 ? launches : 0;
+        }
+    }
+    cudaStreamSynchronize(s);
+    return result;
 }
 
 }  // namespace ed

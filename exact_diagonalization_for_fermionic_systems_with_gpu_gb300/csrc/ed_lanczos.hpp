@@ -64,4 +64,36 @@ struct LzFusedArgs {
                                      // times, [step][2][gridDim.x]
 };
 
+// One instance of a batched run (k_lz_batch): instances share the hopping
+// tables of the first operator (same sector and lattice terms) and differ in
+// their folded diagonals and scalars.
+constexpr int kLzBatchMax = 8;
+
+struct LzInst {
+    int64_t* basis;        // stored Krylov basis (slot stride LzBatchArgs::stride)
+    int64_t* u;            // matvec output
+    LzState* lz;
+    const int64_t* dUPq;   // folded diagonals at the instance's scale 2^-Fc
+    const int64_t* dDNq;
+    int64_t Uq;            // U 2^Fc
+    int64_t coefUP;        // the single hopping class of each table, 2^Fc units
+    int64_t coefDN;
+    int Fc;
+    int unitUP, unitDN, mergeUD;
+    int nclsUP, nclsDN;
+    int bq_bits;
+    int pad_;
+};
+
+struct LzBatchArgs {
+    const LzInst* inst;    // B instances (device)
+    int B;
+    int j0, j1;
+    int64_t stride;        // slot stride in elements
+    int64_t n;             // stored values per vector
+    unsigned int* gbar;    // grid-barrier arrivals, zero at launch
+    LzRedSet* red;         // 4 * B accumulator sets (set r % 4 of instance b at (r % 4) * B + b), zero at launch
+    unsigned int* taken;   // two item-queue counters (step parity), zero at launch
+};
+
 }  // namespace ed

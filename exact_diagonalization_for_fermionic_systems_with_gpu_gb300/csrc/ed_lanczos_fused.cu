@@ -321,6 +321,348 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
     }
 }
 
+// ---------------------------------------------------------------- batch --
+// B Lanczos runs in lockstep in one persistent launch (k_lz_batch): the
+// instances share the first operator's hopping tables (in shared memory, as
+// in k_lz_fused) and differ in their diagonals and scalars (LzInst).  The
+// work items of a matvec phase are (instance, row) pairs, instance-major,
+// handed out through a queue like k_lz_fused's rows; a CTA keeps the
+// instance's <x, u> and max|u| partials in registers while consecutive items
+// belong to it and every warp adds them to per-instance shared limb sums
+// when the instance changes (and its norm partials after each instance's
+// axpy slice).  The barriers, the four rotating reduction sets (B sets each)
+// and the scalar update (thread b of every CTA for instance b) are
+// k_lz_fused's, so every instance's coefficients are bit-identical to its own
+// single run; what the batch saves is the per-step barrier and scalar time
+// of B - 1 runs.  Real operators with one hopping class and a gather
+// schedule.
+
+// A warp's (v, m) into per-instance shared limb sums (all 32 lanes call it).
+__device__ __forceinline__ void batch_flush(i128 v, uint64_t m, unsigned long long* accl, unsigned long long* accm) {
+    v = warp_sum_i128(v);
+    m = warp_max_u64(m);
+    if ((threadIdx.x & 31) == 0) {
+        const u128 uv = (u128)v;
+        atomicAdd(&accl[0], (unsigned long long)(uv & kLimb));
+        atomicAdd(&accl[1], (unsigned long long)((uv >> 42) & kLimb));
+        atomicAdd(&accl[2], (unsigned long long)(int64_t)(v >> 84));
+        atomicMax(accm, (unsigned long long)m);
+    }
+}
+
+__device__ __forceinline__ i128 batch_total(const unsigned long long* accl) {
+    return (i128)((u128)accl[0] + ((u128)accl[1] << 42) + ((u128)(i128)(int64_t)accl[2] << 84));
+}
+
+__device__ __forceinline__ void class_add(i128& ar, int64_t s, int64_t coef, bool unit, int Fc) {
+    ar += unit ? (((i128)s) << Fc) : mul_wide(s, coef);
+}
+
+__global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, const LzBatchArgs f) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint32_t uoff[kTmaUpStage];
+    __shared__ uint32_t uent[kTmaUpStage];
+    __shared__ int give_up;
+    __shared__ uint32_t s_next;
+    __shared__ SlotScalars sX[kLzBatchMax], sP[kLzBatchMax];
+    __shared__ int s_status[kLzBatchMax], s_min_bits[kLzBatchMax], s_ew[kLzBatchMax];
+    __shared__ LzCoefs s_coef[kLzBatchMax];
+    __shared__ unsigned long long accl[kLzBatchMax][3], accm[kLzBatchMax];
+    const TmaSmem S = tma_view(a, sm, uoff, uent, &give_up);
+    const int tid = threadIdx.x, T = blockDim.x;
+    const int B = f.B;
+    const uint32_t nq = (uint32_t)a.dimUP, dimDN = (uint32_t)a.dimDN;
+    const uint32_t nitems = (uint32_t)B * nq;
+    const uint32_t G = gridDim.x;
+    const bool has_item = blockIdx.x < nitems;
+
+    if (tid == 0) {
+        tma_init(S);
+        tma_issue_tables(a, S);
+    }
+    if (tid < B) {
+        const LzState* lz = f.inst[tid].lz;
+        const int j = f.j0;
+        sX[tid] = {lz->e[j], lz->m[j], lz->beta[j], lz_inv(lz->beta[j])};
+        if (j > 0) sP[tid] = {lz->e[j - 1], lz->m[j - 1], lz->beta[j - 1], lz_inv(lz->beta[j - 1])};
+        else sP[tid] = {0, 0, 0.0, 0.0};
+        s_status[tid] = lz->status;
+        s_min_bits[tid] = lz->min_bits;
+        s_ew[tid] = 0;
+        accl[tid][0] = accl[tid][1] = accl[tid][2] = 0;
+        accm[tid] = 0;
+    }
+    tma_zero_slots(a, S);
+    __syncthreads();
+    if (!tma::mbar_wait(&S.bar[2], 0)) {
+        if (tid == 0) atomicExch(a.err, 1);
+        give_up = 1;
+    }
+    __syncthreads();
+    if (give_up) return;  // no row copy has been issued yet
+
+    uint32_t rc = 0;          // rows streamed through the row buffers
+    unsigned int target = 0;  // grid-barrier arrivals expected so far
+    for (int j = f.j0; j < f.j1; ++j) {
+        const int rM = 2 * (j - f.j0), rA = rM + 1;
+        // ---- phase M: u_b = H_b w_j of every instance, item by item --------
+        uint32_t it = blockIdx.x;
+        if (tid == 0 && has_item) {
+            tma::fence_proxy_async_global();
+            tma::fence_proxy_async_smem();
+            const uint32_t b0 = it / nq;
+            tma_issue_row<false>(a, S, f.inst[b0].basis + (size_t)j * f.stride, __ldg(a.rowQueue + (it - b0 * nq)),
+                                 rc & 1);
+        }
+        {
+            i128 dot = 0;
+            uint64_t mx = 0;
+            int cur = has_item ? (int)(it / nq) : -1;
+            while (it < nitems) {
+                const uint32_t b = it / nq;
+                const uint32_t u = __ldg(a.rowQueue + (it - b * nq));
+                const LzInst& I = f.inst[b];
+                const int64_t* xq = I.basis + (size_t)j * f.stride;
+                const int buf = rc & 1;
+                const uint32_t parity = (rc >> 1) & 1;
+                bool issued_next = false;
+                if (tid == 0) {
+                    const uint32_t rn = G + atomicAdd(f.taken + (j & 1), 1u);
+                    s_next = rn;
+                    if (rn < nitems) {
+                        const uint32_t bn = rn / nq;
+                        tma::fence_proxy_async_smem();
+                        tma_issue_row<false>(a, S, f.inst[bn].basis + (size_t)j * f.stride,
+                                             __ldg(a.rowQueue + (rn - bn * nq)), buf ^ 1);
+                        issued_next = true;
+                    }
+                }
+                const uint32_t p0 = __ldg(a.upPtr + u), lenU = __ldg(a.upPtr + u + 1) - p0;
+                const int nposU = (int)__ldg(a.upNpos + u);
+                for (uint32_t k = tid; k < lenU; k += T) S.uoff[k] = (__ldg(a.upEntC + p0 + k) & kColMask) * dimDN;
+                if (!tma::mbar_wait(&S.bar[buf], parity)) {
+                    if (tid == 0) atomicExch(a.err, 1);
+                    give_up = 1;
+                } else {
+                    int64_t* xb = buf ? S.row1 : S.row0;
+                    for (uint32_t i = tid; i < dimDN; i += T) xb[a.schedNeg + i] = -xb[i];
+                }
+                __syncthreads();
+                if (give_up) {
+                    if (tid == 0 && issued_next) tma::mbar_wait(&S.bar[buf ^ 1], ((rc + 1) >> 1) & 1);
+                    return;
+                }
+                const uint32_t r_next = s_next;
+                const int64_t* xrow = buf ? S.row1 : S.row0;
+                const uint64_t stu = __ldg(a.stUP + u);
+                const int64_t du = __ldg(I.dUPq + u);
+                const int64_t* ddq = I.dDNq;
+                const int64_t Uq = I.Uq, cU = I.coefUP, cD = I.coefDN;
+                const int Fc = I.Fc;
+                const uint32_t ubase = u * dimDN;
+                const int sb = I.bq_bits + kFxBits - 62;
+                const int s_u = sb > 0 ? sb : 0;
+                const bool unitU = I.unitUP != 0 && I.nclsUP == 1;
+                const bool unitD = I.unitDN != 0 && I.nclsDN == 1;
+                const bool merge = I.mergeUD != 0, hasD = I.nclsDN != 0;
+                int64_t* uq = I.u;
+                const uint32_t dp = (uint32_t)a.dimDNp;
+                for (uint32_t d0 = tid; d0 < dimDN; d0 += 2 * T) {
+                    const uint32_t d1 = d0 + T;
+                    const bool v1 = d1 < dimDN;
+                    int64_t up0 = 0, un0 = 0, up1 = 0, un1 = 0;
+                    int k = 0;
+                    if (v1) {
+#pragma unroll 4
+                        for (; k < nposU; ++k) {
+                            const uint32_t o = S.uoff[k];
+                            up0 += __ldcg(xq + o + d0);
+                            up1 += __ldcg(xq + o + d1);
+                        }
+#pragma unroll 4
+                        for (; k < (int)lenU; ++k) {
+                            const uint32_t o = S.uoff[k];
+                            un0 += __ldcg(xq + o + d0);
+                            un1 += __ldcg(xq + o + d1);
+                        }
+                    } else {
+#pragma unroll 4
+                        for (; k < nposU; ++k) up0 += __ldcg(xq + S.uoff[k] + d0);
+#pragma unroll 4
+                        for (; k < (int)lenU; ++k) un0 += __ldcg(xq + S.uoff[k] + d0);
+                    }
+                    int64_t dr0 = 0, dr1 = 0;
+                    {
+                        const uint16_t* sc0 = S.sched + d0;
+                        const int n0 = S.steps[d0 >> 5];
+#pragma unroll 4
+                        for (int s = 0; s < n0; ++s) dr0 += xrow[sc0[s * dp]];
+                    }
+                    if (v1) {
+                        const uint16_t* sc1 = S.sched + d1;
+                        const int n1 = S.steps[d1 >> 5];
+#pragma unroll 4
+                        for (int s = 0; s < n1; ++s) dr1 += xrow[sc1[s * dp]];
+                    }
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        if (c == 1 && !v1) break;
+                        const uint32_t d = c ? d1 : d0;
+                        const int64_t su = c ? up1 - un1 : up0 - un0;
+                        const int64_t sd = c ? dr1 : dr0;
+                        i128 ar = 0;
+                        if (merge) {
+                            class_add(ar, su + sd, cU, unitU, Fc);
+                        } else {
+                            if (lenU) class_add(ar, su, cU, unitU, Fc);
+                            if (hasD) class_add(ar, sd, cD, unitD, Fc);
+                        }
+                        const int64_t xr = xrow[d];
+                        const int64_t dq = du + __ldg(ddq + d) + Uq * (int64_t)__popcll(stu & S.dst[d] & a.mask);
+                        ar += mul_wide(dq, xr);
+                        const int64_t qr = shr_round_i64(ar, s_u);
+                        uq[(size_t)ubase + d] = qr;
+                        dot += mul_wide(xr, qr) >> 24;
+                        const uint64_t aq = (uint64_t)(qr < 0 ? -qr : qr);
+                        mx = aq > mx ? aq : mx;
+                    }
+                }
+                __syncthreads();  // row buffer and uoff are free for the next item
+                ++rc;
+                it = r_next;
+                const int nb = it < nitems ? (int)(it / nq) : -1;
+                if (nb != cur) {
+                    batch_flush(dot, mx, accl[cur], &accm[cur]);
+                    dot = 0;
+                    mx = 0;
+                    cur = nb;
+                }
+            }
+        }
+        __syncthreads();
+        if (tid < B) {
+            red_push(&f.red[(rM % 4) * B + tid], batch_total(accl[tid]), accm[tid]);
+            accl[tid][0] = accl[tid][1] = accl[tid][2] = 0;
+            accm[tid] = 0;
+        }
+        if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
+        if (tid < B) {
+            const int b = tid;
+            LzState* lz = f.inst[b].lz;
+            i128 s;
+            uint64_t m;
+            red_pull(&f.red[(rM % 4) * B + b], s, m);
+            if (j > f.j0) {
+                i128 ss;
+                uint64_t mw;
+                red_pull(&f.red[((rM - 1) % 4) * B + b], ss, mw);
+                slot_done(lz, j, s_ew[b], ss, mw, sX[b], sP[b], s_status[b], s_min_bits[b], blockIdx.x == 0);
+            }
+            if (blockIdx.x == 0) {
+                if (rM >= 2) f.red[((rM - 2) % 4) * B + b] = LzRedSet{0, 0, 0, 0};
+                if (b == 0) f.taken[(j + 1) & 1] = 0;
+            }
+            const LzInst& I = f.inst[b];
+            const int sb = I.bq_bits + kFxBits - 62;
+            const int s_u = sb > 0 ? sb : 0;
+            const int e_u = sX[b].e - I.Fc + s_u;
+            s_coef[b] = lz_coefs(j, s, e_u, m, sX[b].e, sX[b].m, sX[b].beta, sP[b].e, sP[b].m, sP[b].ib, s_status[b]);
+            s_ew[b] = s_coef[b].e_w;
+            if (blockIdx.x == 0) {
+                lz->s_u = s_u;
+                lz->e_u = e_u;
+                lz->m_u = m;
+                lz->alpha[j] = s_coef[b].alpha;
+                for (int k = 0; k < 3; ++k) {
+                    lz->at[k] = s_coef[b].at[k];
+                    lz->sh[k] = 0;
+                }
+                lz->Fa = s_coef[b].Fa;
+                lz->e_w = s_coef[b].e_w;
+            }
+        }
+        __syncthreads();
+
+        // ---- phase A: w_{j+1} of every instance ----------------------------
+        for (int b = 0; b < B; ++b) {
+            const LzInst& I = f.inst[b];
+            const int64_t* xq = I.basis + (size_t)j * f.stride;
+            const int64_t* pq = j > 0 ? I.basis + (size_t)(j - 1) * f.stride : xq;
+            int64_t* wq = I.basis + (size_t)(j + 1) * f.stride;
+            const int64_t a0 = s_coef[b].at[0], a1 = s_coef[b].at[1], a2 = s_coef[b].at[2];
+            const int Fa = s_coef[b].Fa;
+            i128 ss = 0;
+            uint64_t mw = 0;
+            const int64_t npair = f.n >> 1;
+            const longlong2* u2 = reinterpret_cast<const longlong2*>(I.u);
+            const longlong2* x2 = reinterpret_cast<const longlong2*>(xq);
+            const longlong2* p2 = reinterpret_cast<const longlong2*>(pq);
+            longlong2* w2 = reinterpret_cast<longlong2*>(wq);
+            for (int64_t i = (int64_t)blockIdx.x * blockDim.x + tid; i < npair; i += (int64_t)G * blockDim.x) {
+                const longlong2 uu = __ldcg(u2 + i), xx = __ldcg(x2 + i), pp = __ldcg(p2 + i);
+                longlong2 w;
+                w.x = shr_round_i64(mul_wide(a0, uu.x) + mul_wide(a1, xx.x) + mul_wide(a2, pp.x), Fa);
+                w.y = shr_round_i64(mul_wide(a0, uu.y) + mul_wide(a1, xx.y) + mul_wide(a2, pp.y), Fa);
+                w2[i] = w;
+                ss += (mul_wide(w.x, w.x) >> 16) + (mul_wide(w.y, w.y) >> 16);
+                const uint64_t ax = (uint64_t)(w.x < 0 ? -w.x : w.x), ay = (uint64_t)(w.y < 0 ? -w.y : w.y);
+                mw = ax > mw ? ax : mw;
+                mw = ay > mw ? ay : mw;
+            }
+            if ((f.n & 1) && blockIdx.x == 0 && tid == 0) {
+                const int64_t i = f.n - 1;
+                const int64_t w = shr_round_i64(
+                    mul_wide(a0, __ldcg(I.u + i)) + mul_wide(a1, __ldcg(xq + i)) + mul_wide(a2, __ldcg(pq + i)), Fa);
+                wq[i] = w;
+                ss += mul_wide(w, w) >> 16;
+                const uint64_t aw = (uint64_t)(w < 0 ? -w : w);
+                mw = aw > mw ? aw : mw;
+            }
+            batch_flush(ss, mw, accl[b], &accm[b]);
+        }
+        __syncthreads();
+        if (tid < B) {
+            red_push(&f.red[(rA % 4) * B + tid], batch_total(accl[tid]), accm[tid]);
+            accl[tid][0] = accl[tid][1] = accl[tid][2] = 0;
+            accm[tid] = 0;
+        }
+        if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
+        if (tid < B && blockIdx.x == 0) {
+            const int b = tid;
+            if (rA >= 2) f.red[((rA - 2) % 4) * B + b] = LzRedSet{0, 0, 0, 0};
+            if (j + 1 == f.j1) {
+                i128 ss;
+                uint64_t mw;
+                red_pull(&f.red[(rA % 4) * B + b], ss, mw);
+                slot_done(f.inst[b].lz, j + 1, s_coef[b].e_w, ss, mw, sX[b], sP[b], s_status[b], s_min_bits[b], true);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Cooperative launch of the batch: grid and shared memory of the first
+// operator's plan.
+// Cooperative launch of the batch: grid and shared memory of the first
+// operator's plan.
+cudaError_t launch_lz_batch(const ed_op* op, const LzBatchArgs& f, cudaStream_t s) {
+    if (op->tma_smem <= 0 || op->cplx || !op->mv_fast || !op->mv.dnSched) return cudaErrorNotSupported;
+    const void* fn = (const void*)k_lz_batch;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, op->tma_smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, sms = 0, coop = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTmaThreads, op->tma_smem)) != cudaSuccess)
+        return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op->device)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, op->device)) != cudaSuccess) return e;
+    if (!coop || (int64_t)per_sm * sms < op->tma_grid) return cudaErrorNotSupported;
+    MvArgs av = op->mv;
+    LzBatchArgs fv = f;
+    void* args[] = {&av, &fv};
+    return cudaLaunchCooperativeKernel(fn, dim3((unsigned)op->tma_grid), dim3(kTmaThreads), args,
+                                       (size_t)op->tma_smem, s);
+}
+
 // Cooperative launch of steps j0 .. j1-1; cudaErrorNotSupported when the
 // operator has no shared-memory plan, or the grid cannot be co-resident.
 // f.gbar and the four sets at f.red must be zero.

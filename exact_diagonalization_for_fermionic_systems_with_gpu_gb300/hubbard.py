@@ -290,3 +290,48 @@ class Lanczos:
         self.a = list(alpha[: res.steps])
         self.b = list(beta[: res.steps + 1])
         return res.e0, evec
+
+
+def lanczos_batch(ops: Sequence[Hubbard], max_steps: int, seed: int = 0, starts: Optional[np.ndarray] = None,
+                  ritz: bool = True, evec_out=None):
+    """ed_lanczos_batch: fixed-step Lanczos of up to 8 operators that share
+    their hopping tables (one sector, disorder in the on-site terms) in one
+    persistent launch.  Run b starts from Philox(seed + b) or starts[b]
+    (a numpy array or a float64 CUDA tensor, (B, rows)).
+    Returns (e0 [B], evecs, alpha [B, max_steps], beta [B, max_steps + 1]):
+    evecs a (B, rows) numpy array, or evec_out (a (B, rows) float64 CUDA
+    tensor) when given, or None without ritz."""
+    lib = _capi.load()
+    B = len(ops)
+    n = ops[0].rows()
+    cfg = _capi.ed_lanczos_cfg()
+    cfg.max_steps = int(max_steps)
+    cfg.mode = _capi.ED_LANCZOS_FIXED
+    cfg.reorth = 0
+    cfg.ritz = _capi.ED_RITZ_STORED if ritz else _capi.ED_RITZ_NONE
+    cfg.seed = int(seed)
+    handles = (C.c_void_p * B)(*[op.handle for op in ops])
+    st_ptr, st_mem = None, _capi.ED_MEM_HOST
+    if starts is not None and not isinstance(starts, np.ndarray):  # CUDA tensor (B, rows)
+        cfg.start = _capi.ED_START_USER
+        st_ptr, st_mem = C.c_void_p(starts.data_ptr()), _capi.ED_MEM_DEVICE
+    elif starts is not None:
+        f = np.ascontiguousarray(starts, dtype=np.float64).reshape(B, n)
+        cfg.start = _capi.ED_START_USER
+        st_ptr = _ptr(f)
+    else:
+        cfg.start = _capi.ED_START_RANDOM
+    evecs, ev_ptr, ev_mem = None, None, _capi.ED_MEM_HOST
+    if ritz:
+        if evec_out is not None:
+            evecs, ev_ptr, ev_mem = evec_out, C.c_void_p(evec_out.data_ptr()), _capi.ED_MEM_DEVICE
+        else:
+            evecs = np.empty((B, n))
+            ev_ptr = _ptr(evecs)
+    alpha = np.zeros((B, max_steps))
+    beta = np.zeros((B, max_steps + 1))
+    res = (_capi.ed_lanczos_result * B)()
+    check(lib.ed_lanczos_batch(handles, B, C.byref(cfg), st_ptr, st_mem, ev_ptr, ev_mem, _ptr(alpha), _ptr(beta),
+                               res, None), "ed_lanczos_batch")
+    return np.array([r.e0 for r in res]), evecs, alpha, beta
+

@@ -29,6 +29,7 @@ written into a CUDA tensor).
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import math
 import time
@@ -39,7 +40,7 @@ import numpy as np
 
 from . import lattices as L
 from . import observables as ob
-from .hubbard import H_TBq, Hubbard, Lanczos, random_vector
+from .hubbard import H_TBq, Hubbard, Lanczos, lanczos_batch, random_vector
 
 
 @dataclass
@@ -157,16 +158,77 @@ def mbl_chain_terms(eps: Sequence[float], t: float = -1.0):
 MBL_SECTORS = ((6, 6), (7, 5), (8, 4))
 
 
+def _mbl_batched(reals, sectors, n_sites, W, U, steps, seed, a_sites, batch, t) -> List[MblPoint]:
+    """mbl_sweep with the realisations of each sector in batches of `batch`
+    Lanczos runs per persistent launch (ed_lanczos_batch); a sector the
+    batched kernel does not take runs instance by instance.  Same start
+    vectors, so the same results bit for bit."""
+    import torch
+    from ._capi import EdError, load
+    lib = load()
+    out: List[MblPoint] = []
+    reals = list(reals)
+    for s, (qu, qd) in enumerate(sectors):
+        for g0 in range(0, len(reals), batch):
+            group = reals[g0:g0 + batch]
+            ti = time.perf_counter()
+            ops = []
+            for r in group:
+                eu, edn = mbl_disorder(r, n_sites, W, seed)
+                ops.append(Hubbard(H_TBq(n_sites, qu).extend(mbl_chain_terms(eu)),
+                                   H_TBq(n_sites, qd).extend(mbl_chain_terms(edn)), U))
+            _sync()
+            tb = time.perf_counter()
+            n = ops[0].rows()
+            starts = torch.empty((len(ops), n), dtype=torch.float64, device="cuda")
+            for b, r in enumerate(group):
+                lib.ed_random_vector_device(n, seed * (1 << 20) + r * len(sectors) + s,
+                                            C.c_void_p(starts[b].data_ptr()), None)
+            evecs = torch.empty_like(starts)
+            try:
+                e0s, _, _, _ = lanczos_batch(ops, steps, starts=starts, evec_out=evecs)
+            except EdError:
+                e0s = []
+                for b, op in enumerate(ops):
+                    lz = Lanczos()
+                    e, _ = lz.eigen(op, max_steps=steps, mode="fixed", ritz="stored",
+                                    f=starts[b].cpu().numpy(), evec_out=evecs[b])
+                    e0s.append(e)
+            _sync()
+            tl = time.perf_counter()
+            for b, r in enumerate(group):
+                nu, nd, _ = ob.site_densities(ops[b], evecs[b])
+                svn, sref = ob.entanglement_entropy(ops[b], evecs[b], a_sites)
+                out.append(MblPoint(int(r), (qu, qd), float(e0s[b]), svn, sref, nu, nd, steps))
+            _sync()
+            te = time.perf_counter()
+            for op in ops:
+                op.close()
+            t.instances += len(group)
+            t.lanczos_steps += steps * len(group)
+            t.build_s += tb - ti
+            t.lanczos_s += tl - tb
+            t.observables_s += te - tl
+            t.per_instance.extend([(te - ti) / len(group)] * len(group))
+    order = {(r, sec): k for k, (r, sec) in enumerate((r, sec) for r in reals for sec in sectors)}
+    return sorted(out, key=lambda p: order[(p.realisation, p.sector)])
+
+
 def mbl_sweep(n_real: int = 64, sectors: Sequence[Tuple[int, int]] = MBL_SECTORS, n_sites: int = 12,
               W: float = 6.0, U: float = 1.0, steps: int = 300, mode: str = "fixed", seed: int = 0,
               a_sites: Optional[Sequence[int]] = None, realisations: Optional[Sequence[int]] = None,
-              timing: Optional[SweepTiming] = None) -> List[MblPoint]:
-    """Ground-state sweep over disorder realisations and sectors."""
+              timing: Optional[SweepTiming] = None, batch: int = 1) -> List[MblPoint]:
+    """Ground-state sweep over disorder realisations and sectors; batch > 1
+    (fixed-step mode) runs up to 8 realisations of a sector per launch."""
     a_sites = list(range(n_sites // 2)) if a_sites is None else list(a_sites)
     reals = range(n_real) if realisations is None else realisations
     t = timing if timing is not None else SweepTiming()
-    out: List[MblPoint] = []
     t0 = time.perf_counter()
+    if batch > 1 and mode == "fixed":
+        out = _mbl_batched(reals, sectors, n_sites, W, U, steps, seed, a_sites, min(batch, 8), t)
+        t.total_s += time.perf_counter() - t0
+        return out
+    out: List[MblPoint] = []
     for r in reals:
         eu, edn = mbl_disorder(r, n_sites, W, seed)
         tu, td = mbl_chain_terms(eu), mbl_chain_terms(edn)
@@ -227,9 +289,10 @@ def _run(a, n, form: str):
                 flux_sweep(flux_phis(n)[: a.warmup], steps=a.steps, mode=a.mode, seed=a.seed)
             pts = flux_sweep(flux_phis(n), steps=a.steps, mode=a.mode, seed=a.seed, timing=tm)
         else:
+            bt = a.batch if form == "tuned" else 1
             if a.warmup:
-                mbl_sweep(realisations=range(a.warmup), steps=a.steps, mode=a.mode, seed=a.seed + 1)
-            pts = mbl_sweep(n, steps=a.steps, mode=a.mode, seed=a.seed, timing=tm)
+                mbl_sweep(realisations=range(max(a.warmup, bt)), steps=a.steps, mode=a.mode, seed=a.seed + 1, batch=bt)
+            pts = mbl_sweep(n, steps=a.steps, mode=a.mode, seed=a.seed, timing=tm, batch=bt)
     finally:
         for k, v in saved.items():
             if v is None:
@@ -248,6 +311,8 @@ def main(argv: Optional[Sequence[str]] = None) -> None:
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=1, help="instances run (untimed) before the sweep")
     ap.add_argument("--out", default=None, help="append the result rows to this .dat file")
+    ap.add_argument("--batch", type=int, default=8,
+                    help="disorder realisations per Lanczos launch in the tuned form (1: one launch per run)")
     ap.add_argument("--form", choices=["tuned", "plain", "compare"], default="tuned",
                     help="plain: the per-instance form of PLAIN_ENV; compare: both, with the largest "
                          "differences of their outputs")

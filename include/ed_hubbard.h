@@ -217,6 +217,23 @@ ed_status ed_lanczos_run(ed_op* op, const ed_lanczos_cfg* cfg,
                          double* alpha, double* beta,
                          ed_lanczos_result* res, void* stream);
 
+/* n_ops (1..8) fixed-step Lanczos runs in one persistent launch, for
+ * operators that share their hopping tables (same sector and lattice terms;
+ * the on-site terms, U and so the folded diagonals may differ): the
+ * disorder realisations of one sector, the batched form of the sweeps that
+ * call Lanczos::eigen once per realisation (MBL_test/src/Hubbard_EE_test.cu:
+ * 62-72, TotalSpinExcited_Lieb_randomHop.cu:110-136).  Real operators with one
+ * hopping class and a shared-memory plan (else ED_ERR_NOT_BUILT).  cfg: mode
+ * ED_LANCZOS_FIXED, no reorthogonalisation, ritz ED_RITZ_STORED (evecs:
+ * n_ops x rows at evec_mem) or ED_RITZ_NONE; start ED_START_RANDOM (run b
+ * seeded cfg->seed + b) or ED_START_USER (starts: n_ops x rows at start_mem).
+ * alpha (n_ops x max_steps), beta (n_ops x (max_steps+1)) and res (n_ops) are
+ * optional host outputs; each run's coefficients equal those of its own
+ * ed_lanczos_run bit for bit.  Synchronous. */
+ed_status ed_lanczos_batch(ed_op* const* ops, int n_ops, const ed_lanczos_cfg* cfg, const double* starts,
+                           int start_mem, double* evecs, int evec_mem, double* alpha, double* beta,
+                           ed_lanczos_result* res, void* stream);
+
 /* Same generator on the device: out (device, n doubles), async on stream. */
 ed_status ed_random_vector_device(int64_t n, uint64_t seed, double* out_device, void* stream);
 

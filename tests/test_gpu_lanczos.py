@@ -250,3 +250,34 @@ def test_two_pass_matvec_lanczos_ritz_vector(ed, monkeypatch, ritz):
     s, g = runs["striped"], runs["generic"]
     assert s[0] == g[0] and s[1] == g[1] and s[2] == g[2]
     assert np.max(np.abs(s[3] - g[3])) < 1e-15
+
+
+def test_lanczos_batch_matches_single_runs(ed):
+    """ed_lanczos_batch: four disorder realisations of the open L=12 (6,6)
+    sector in one persistent launch give, run by run, the alpha, beta, E0 and
+    Ritz vector of the run's own ed_lanczos_run bit for bit; a batch of one
+    equals a single run too."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import sweeps
+    ops = []
+    for r in range(4):
+        eu, edn = sweeps.mbl_disorder(r, 12, 6.0)
+        ops.append(ed.Hubbard(ed.H_TBq(12, 6).extend(sweeps.mbl_chain_terms(eu)),
+                              ed.H_TBq(12, 6).extend(sweeps.mbl_chain_terms(edn)), 1.0 + 0.5 * r))
+    steps = 60
+    for group in (ops, ops[2:3]):
+        base = 7 if len(group) > 1 else 9
+        e0, ev, al, be = ed.lanczos_batch(group, steps, seed=base)
+        for b, op in enumerate(group):
+            lz = ed.Lanczos()
+            e, v = lz.eigen(op, max_steps=steps, mode="fixed", seed=base + b)
+            assert e0[b] == e
+            assert np.array_equal(al[b], np.array(lz.a)) and np.array_equal(be[b], np.array(lz.b))
+            assert np.array_equal(ev[b], v)
+
+
+def test_lanczos_batch_rejects_other_tables(ed):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    a = ed.Hubbard(ed.H_TBq(12, 6).extend(L.chain(12, periodic=False)), ed.H_TBq(12, 6).extend(L.chain(12, periodic=False)), 1.0)
+    b = ed.Hubbard(ed.H_TBq(12, 6).extend(L.chain(12)), ed.H_TBq(12, 6).extend(L.chain(12)), 1.0)
+    with pytest.raises(ed.EdError):
+        ed.lanczos_batch([a, b], 10)

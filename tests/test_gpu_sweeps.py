@@ -55,3 +55,17 @@ def test_flux_sweep_matches_dense(ed, orc):
         assert abs(p.e0 - w[0]) < 1e-10 * abs(w[0])
         assert abs(p.d1 - exact1) < 1e-9 * max(1.0, abs(exact1))
         assert abs(p.d2 - exact2) < 1e-8 * max(1.0, abs(exact2))
+
+
+def test_mbl_sweep_batched_equals_unbatched(ed):
+    """The disorder sweep with its realisations batched per sector
+    (ed_lanczos_batch) returns the unbatched sweep's E0, entropies and
+    densities exactly (same start vectors, bit-identical coefficients)."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import sweeps
+    kw = dict(realisations=range(5), sectors=((6, 6), (8, 4)), steps=80)
+    a = sweeps.mbl_sweep(**kw)
+    b = sweeps.mbl_sweep(batch=3, **kw)
+    assert [(p.realisation, p.sector) for p in a] == [(p.realisation, p.sector) for p in b]
+    for p, q in zip(a, b):
+        assert p.e0 == q.e0 and p.s_vn == q.s_vn and p.s_ref == q.s_ref
+        assert np.array_equal(p.n_up, q.n_up) and np.array_equal(p.n_dn, q.n_dn)
