@@ -506,7 +506,8 @@ ed_status ed_op_perform(ed_op* op, const double* x, double* y, int mem, void* st
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const int W = op->cplx ? 2 : 1;
     const int64_t DW = op->D * W;
-    if (!op->d_xq && cudaMalloc(&op->d_xq, sizeof(int64_t) * (size_t)DW) != cudaSuccess) return ED_ERR_ALLOC;
+    // two elements of padding: the row engine copies whole 16-byte words around a row
+    if (!op->d_xq && cudaMalloc(&op->d_xq, sizeof(int64_t) * ((size_t)DW + 2)) != cudaSuccess) return ED_ERR_ALLOC;
     const double* dx = x;
     double* dy = y;
     if (mem == ED_MEM_HOST) {

@@ -363,7 +363,8 @@ ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_s
     w->stride = (DW + 31) / 32 * 32;
     w->max_steps = max_steps;
     const size_t ns = (size_t)max_steps + 2;
-    LZ_CK(cudaMalloc(&w->basis, sizeof(int64_t) * slots * (size_t)w->stride));
+    // + 32 elements: the row engine's 16-byte-aligned row copies may read one past a slot's end
+    LZ_CK(cudaMalloc(&w->basis, sizeof(int64_t) * (slots * (size_t)w->stride + 32)));
     LZ_CK(cudaMalloc(&w->u, sizeof(int64_t) * (size_t)DW));
     LZ_CK(cudaMalloc(&w->fbuf, sizeof(double) * (size_t)DW));
     LZ_CK(cudaMalloc(&w->lz, sizeof(LzState)));

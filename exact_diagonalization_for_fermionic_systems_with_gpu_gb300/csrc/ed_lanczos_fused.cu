@@ -444,7 +444,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
                     if (tid == 0) atomicExch(a.err, 1);
                     give_up = 1;
                 } else {
-                    int64_t* xb = buf ? S.row1 : S.row0;
+                    int64_t* xb = (buf ? S.row1 : S.row0) + tma_row_off<false>(a, u);
                     for (uint32_t i = tid; i < dimDN; i += T) xb[a.schedNeg + i] = -xb[i];
                 }
                 __syncthreads();
@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
                     return;
                 }
                 const uint32_t r_next = s_next;
-                const int64_t* xrow = buf ? S.row1 : S.row0;
+                const int64_t* xrow = (buf ? S.row1 : S.row0) + tma_row_off<false>(a, u);
                 const uint64_t stu = __ldg(a.stUP + u);
                 const int64_t du = __ldg(I.dUPq + u);
                 const int64_t* ddq = I.dDNq;

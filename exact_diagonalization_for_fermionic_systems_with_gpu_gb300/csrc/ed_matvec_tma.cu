@@ -64,8 +64,8 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_matvec_tma(const MvArgs a) {
 int tma_plan(const ed_op* op, MvArgs* a) {
     const int W = op->cplx ? 2 : 1;
     const int64_t dimDN = op->dimDN;
-    const int64_t row_bytes = dimDN * W * 8;
-    if (row_bytes % 16 != 0) return 0;
+    // an odd real row is copied with one element before or after it
+    const int64_t row_bytes = ((dimDN * W + 2) & ~(int64_t)1) * 8;
     // the gather schedule serves the single-class real kernel only
     if (op->cplx || !op->mv_fast) {
         a->dnSched = nullptr;
@@ -73,7 +73,7 @@ int tma_plan(const ed_op* op, MvArgs* a) {
     }
     auto up128 = [](int64_t v) { return (v + 127) / 128 * 128; };
     // with the schedule a row buffer holds [x | -x | 16 zeros]
-    const int64_t buf_bytes = a->dnSched ? ((int64_t)2 * a->schedNeg + 16) * 8 : row_bytes;
+    const int64_t buf_bytes = a->dnSched ? ((int64_t)2 * a->schedNeg + 18) * 8 : row_bytes;
     int64_t off = 128;  // mbarriers
     a->sm_row0 = (int)off;
     off += up128(buf_bytes);

@@ -155,20 +155,33 @@ __device__ __forceinline__ void tma_issue_tables(const MvArgs& a, const TmaSmem&
 // The 16 zeros of both row buffers that idle lanes of the gather schedule
 // read (the bulk copies only ever write [0, dimDN)).
 __device__ __forceinline__ void tma_zero_slots(const MvArgs& a, const TmaSmem& S) {
-    if (threadIdx.x < 16) {
+    if (threadIdx.x < 17) {  // 16 zeros after [x | -x] at either row offset
         S.row0[2 * a.schedNeg + threadIdx.x] = 0;
         S.row1[2 * a.schedNeg + threadIdx.x] = 0;
     }
 }
 
-// Thread 0: start the copy of row u of x into row buffer `buf`.
+// Offset (0 or 1 element) of row u inside its row buffer: a bulk copy starts
+// on a 16-byte boundary, so with an odd dim_dn (real vectors) every other
+// row is copied from the element before it.
+template <bool CPLX>
+__device__ __forceinline__ uint32_t tma_row_off(const MvArgs& a, uint32_t u) {
+    return CPLX ? 0u : (uint32_t)(((uint64_t)u * (uint64_t)a.dimDN) & 1u);
+}
+
+// Thread 0: start the copy of row u of x into row buffer `buf`: the
+// 16-byte-aligned run of whole 16-byte words around the row (one element
+// before it when it starts at an odd index, one after it to round up; the
+// vectors carry two elements of padding), the row at tma_row_off.
 template <bool CPLX>
 __device__ __forceinline__ void tma_issue_row(const MvArgs& a, const TmaSmem& S, const int64_t* xq, uint32_t u,
                                               int buf) {
     constexpr int W = CPLX ? 2 : 1;
-    const uint32_t row_bytes = (uint32_t)a.dimDN * W * 8u;
-    tma::expect_tx(&S.bar[buf], row_bytes);
-    tma::bulk_g2s(buf ? S.row1 : S.row0, xq + (size_t)u * a.dimDN * W, row_bytes, &S.bar[buf]);
+    const uint32_t off = tma_row_off<CPLX>(a, u);
+    const uint32_t n = CPLX ? (uint32_t)a.dimDN * 2u : (((uint32_t)a.dimDN + off + 1u) & ~1u);
+    const uint32_t bytes = n * 8u;
+    tma::expect_tx(&S.bar[buf], bytes);
+    tma::bulk_g2s(buf ? S.row1 : S.row0, xq + (size_t)u * a.dimDN * W - off, bytes, &S.bar[buf]);
 }
 
 // Up-term element load: read-only path for a one-launch matvec, L2
@@ -267,7 +280,7 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
             *S.give_up = 1;
         } else if (SCHED) {
             // -x beside x, so that a schedule index carries the sign
-            int64_t* xb = buf ? S.row1 : S.row0;
+            int64_t* xb = (buf ? S.row1 : S.row0) + tma_row_off<CPLX>(a, u);
             for (uint32_t i = tid; i < dimDN; i += T) xb[a.schedNeg + i] = -xb[i];
         }
         __syncthreads();
@@ -278,7 +291,7 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
             return;
         }
         const uint32_t r_next = DYN ? *snext : r + 1;  // written by thread 0 before the barrier above
-        const int64_t* xrow = buf ? S.row1 : S.row0;
+        const int64_t* xrow = (buf ? S.row1 : S.row0) + tma_row_off<CPLX>(a, u);
         const uint64_t stu = __ldg(a.stUP + u);
         const int64_t du = __ldg(a.dUPq + u);
         const uint32_t ubase = u * dimDN;

@@ -26,7 +26,7 @@ constexpr int kMaxDevices = 64;
 
 // Device-side scratch.  In host code these names are only stand-ins: the
 // device addresses come from cudaGetSymbolAddress, once per device.
-static __device__ __align__(256) int64_t g_noalloc_xq[kNoAllocMaxElems];
+static __device__ __align__(256) int64_t g_noalloc_xq[kNoAllocMaxElems + 2];  // + padding read by row copies
 static __device__ __align__(256) int g_noalloc_words[2];  // [0] max exponent, [1] non-finite flag
 
 struct Resolved {

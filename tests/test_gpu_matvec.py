@@ -169,6 +169,10 @@ def kernel_cases():
         ("kagome12_66_flux_up_only", 12, 6, 6, L.kagome12(flux=0.3), L.kagome12(), 4.0),
         ("kagome12_55_Kx_2classes", 12, 5, 5, L.kagome12_kinetic_x(), L.kagome12_kinetic_x(), 1.0),
         ("chain12_open_W6_75", 12, 7, 5, L.chain(12, periodic=False, eps=eps12), L.chain(12, periodic=False, eps=eps12), 1.0),
+        # odd down dimension (495): every other row starts off a 16-byte boundary
+        ("chain12_open_W6_84_odd_rows", 12, 8, 4, L.chain(12, periodic=False, eps=eps12),
+         L.chain(12, periodic=False, eps=eps12), 1.0),
+        ("kagome12_54_real_odd_rows", 12, 5, 4, L.kagome12(), L.kagome12(), 4.0),
         ("chain8_35", 8, 3, 5, L.chain(8), L.chain(8), 2.0),
         ("chain8_04_no_up_hops", 8, 0, 4, L.chain(8), L.chain(8), 2.0),
         ("chain2_11", 2, 1, 1, L.chain(2, periodic=False), L.chain(2, periodic=False), 3.0),
