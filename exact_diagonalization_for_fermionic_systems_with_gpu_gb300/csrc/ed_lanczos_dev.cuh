@@ -46,10 +46,10 @@ struct LzCoefs {
 };
 
 // alpha_j and the integer axpy coefficients of step j from the exact
-// <w_j, u> (alpha_raw), slot j (eX, mX, bj) and slot j-1 (eP, mP and the
-// reciprocal ibP = 1 / beta_{j-1}).  One division per step: 1 / bj.
+// <w_j, u> (alpha_raw), slot j (eX, mX, bj and ib = 1 / bj, computed when
+// slot j was completed) and slot j-1 (eP, mP and ibP = 1 / beta_{j-1}).
 __device__ inline LzCoefs lz_coefs(int j, i128 alpha_raw, int e_u, uint64_t m_u, int eX, uint64_t mX, double bj,
-                                   int eP, uint64_t mP, double ibP, int status) {
+                                   double ib, int eP, uint64_t mP, double ibP, int status) {
     LzCoefs c;
     if (!(bj > 0.0) || status != 0) {
         // after a breakdown (or a bad start) the recurrence only carries zeros
@@ -59,7 +59,6 @@ __device__ inline LzCoefs lz_coefs(int j, i128 alpha_raw, int e_u, uint64_t m_u,
         c.e_w = eX;
         return c;
     }
-    const double ib = 1.0 / bj;
     const double anum = i128_to_f64(alpha_raw, eX + e_u + 24);
     const double aj = (anum * ib) * ib;
     c.alpha = aj;
@@ -114,7 +113,8 @@ __device__ inline void lz_after_matvec(LzState* lz, int j, i128 alpha_raw, uint6
     lz->s_u = s_u;
     lz->e_u = e_u;
     lz->m_u = m_u;
-    const LzCoefs c = lz_coefs(j, alpha_raw, e_u, m_u, eX, lz->m[j], lz->beta[j], j > 0 ? lz->e[j - 1] : 0,
+    const LzCoefs c = lz_coefs(j, alpha_raw, e_u, m_u, eX, lz->m[j], lz->beta[j], lz_inv(lz->beta[j]),
+                               j > 0 ? lz->e[j - 1] : 0,
                                j > 0 ? lz->m[j - 1] : 0, j > 0 ? lz_inv(lz->beta[j - 1]) : 0.0, lz->status);
     lz->alpha[j] = c.alpha;
     for (int k = 0; k < 3; ++k) {

@@ -197,7 +197,6 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
     // later ones by the axpy bound), so the matvec shift needs no reduction
     const int sb = a.bq_bits + kFxBits - 62;
     const int s_u = sb > 0 ? sb : 0;
-    int e_w_prev = 0;         // exponent of w_j chosen at step j-1
     for (int j = f.j0; j < f.j1; ++j) {
         const int64_t* xq = slot(j);
         const int64_t* pq = j > 0 ? slot(j - 1) : slot(j);
@@ -212,6 +211,15 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
             tma::fence_proxy_async_global();
             tma::fence_proxy_async_smem();
             tma_issue_row<CPLX>(a, S, xq, u0, rc & 1);
+        }
+        if (tid == 32 && j > f.j0) {
+            // slot j from the previous step's axpy reduction, while the first
+            // row copy is in flight (read at the scalar update after the next
+            // barrier)
+            i128 ss;
+            uint64_t mw;
+            red_pull(&f.red[(rM - 1) % 4], ss, mw);
+            slot_done(lz, j, s_coef.e_w, ss, mw, sX, sP, s_status, s_min_bits, blockIdx.x == 0);
         }
         {
             i128 dot = 0;
@@ -231,13 +239,6 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
             i128 s;
             uint64_t m;
             red_pull(&f.red[rM % 4], s, m);
-            if (j > f.j0) {
-                // slot j from the previous step's axpy reduction
-                i128 ss;
-                uint64_t mw;
-                red_pull(&f.red[(rM - 1) % 4], ss, mw);
-                slot_done(lz, j, e_w_prev, ss, mw, sX, sP, s_status, s_min_bits, blockIdx.x == 0);
-            }
             if (blockIdx.x == 0) {
                 if (rM >= 2) f.red[(rM - 2) % 4] = LzRedSet{0, 0, 0, 0};
                 // the other queue counter was last taken from in step j-1 and
@@ -245,8 +246,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
                 f.taken[(j + 1) & 1] = 0;
             }
             const int e_u = sX.e - a.Fc + s_u;
-            s_coef = lz_coefs(j, s, e_u, m, sX.e, sX.m, sX.beta, sP.e, sP.m, sP.ib, s_status);
-            e_w_prev = s_coef.e_w;
+            s_coef = lz_coefs(j, s, e_u, m, sX.e, sX.m, sX.beta, sX.ib, sP.e, sP.m, sP.ib, s_status);
             if (blockIdx.x == 0) {
                 lz->s_u = s_u;
                 lz->e_u = e_u;
@@ -414,6 +414,15 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
             tma_issue_row<false>(a, S, f.inst[b0].basis + (size_t)j * f.stride, __ldg(a.rowQueue + (it - b0 * nq)),
                                  rc & 1);
         }
+        if (tid >= 32 && tid < 32 + B && j > f.j0) {
+            // slot j of instance b from the previous step's axpy reduction,
+            // while the first row copy is in flight
+            const int b = tid - 32;
+            i128 ss;
+            uint64_t mw;
+            red_pull(&f.red[((rM - 1) % 4) * B + b], ss, mw);
+            slot_done(f.inst[b].lz, j, s_ew[b], ss, mw, sX[b], sP[b], s_status[b], s_min_bits[b], blockIdx.x == 0);
+        }
         {
             i128 dot = 0;
             uint64_t mx = 0;
@@ -552,12 +561,6 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
             i128 s;
             uint64_t m;
             red_pull(&f.red[(rM % 4) * B + b], s, m);
-            if (j > f.j0) {
-                i128 ss;
-                uint64_t mw;
-                red_pull(&f.red[((rM - 1) % 4) * B + b], ss, mw);
-                slot_done(lz, j, s_ew[b], ss, mw, sX[b], sP[b], s_status[b], s_min_bits[b], blockIdx.x == 0);
-            }
             if (blockIdx.x == 0) {
                 if (rM >= 2) f.red[((rM - 2) % 4) * B + b] = LzRedSet{0, 0, 0, 0};
                 if (b == 0) f.taken[(j + 1) & 1] = 0;
@@ -566,7 +569,8 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
             const int sb = I.bq_bits + kFxBits - 62;
             const int s_u = sb > 0 ? sb : 0;
             const int e_u = sX[b].e - I.Fc + s_u;
-            s_coef[b] = lz_coefs(j, s, e_u, m, sX[b].e, sX[b].m, sX[b].beta, sP[b].e, sP[b].m, sP[b].ib, s_status[b]);
+            s_coef[b] = lz_coefs(j, s, e_u, m, sX[b].e, sX[b].m, sX[b].beta, sX[b].ib, sP[b].e, sP[b].m, sP[b].ib,
+                                 s_status[b]);
             s_ew[b] = s_coef[b].e_w;
             if (blockIdx.x == 0) {
                 lz->s_u = s_u;
