@@ -212,10 +212,11 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
             tma::fence_proxy_async_smem();
             tma_issue_row<CPLX>(a, S, xq, u0, rc & 1);
         }
-        if (tid == 32 && j > f.j0) {
+        if (tid == kTmaThreads - 32 && j > f.j0) {
             // slot j from the previous step's axpy reduction, while the first
             // row copy is in flight (read at the scalar update after the next
-            // barrier)
+            // barrier); the last warp, whose second column is past the end
+            // of a row when dim_dn < 2 * kTmaThreads - 32
             i128 ss;
             uint64_t mw;
             red_pull(&f.red[(rM - 1) % 4], ss, mw);
@@ -414,10 +415,10 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
             tma_issue_row<false>(a, S, f.inst[b0].basis + (size_t)j * f.stride, __ldg(a.rowQueue + (it - b0 * nq)),
                                  rc & 1);
         }
-        if (tid >= 32 && tid < 32 + B && j > f.j0) {
+        if (tid >= kTmaThreads - 32 && tid < kTmaThreads - 32 + B && j > f.j0) {
             // slot j of instance b from the previous step's axpy reduction,
-            // while the first row copy is in flight
-            const int b = tid - 32;
+            // while the first row copy is in flight (the last warp)
+            const int b = tid - (kTmaThreads - 32);
             i128 ss;
             uint64_t mw;
             red_pull(&f.red[((rM - 1) % 4) * B + b], ss, mw);
