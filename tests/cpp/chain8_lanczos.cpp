@@ -1,7 +1,8 @@
 // C++ caller of the C ABI through include/ed_hubbard.hpp, written the way the
 // reference drivers are (MBL_test/src/Hubbard_test.cu): build the two H_TBq,
-// the operator, run Lanczos, print E0.  Argument "--basis-only" exercises the
-// host-side part without a GPU.
+// the operator, run Lanczos, print E0; then the three lowest eigenpairs
+// (TotalSpinExcited_*) and one Krylov time step (Time_evol_test.cu).
+// Argument "--basis-only" exercises the host-side part without a GPU.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -28,6 +29,24 @@ int main(int argc, char** argv) {
         std::vector<double> evec;
         const double e0 = lanc.eigen(h, {}, evec, 100, ED_LANCZOS_FIXED, true, 0);
         std::printf("E0 %.15f steps %zu\n", e0, lanc.a.size());
+        // TotalSpinExcited_*: the lowest pairs through the Spectra-shaped solver
+        ed::SymEigsSolver eigs(h, 3, 4 * (3 + 1));
+        eigs.init();
+        const int nconv = eigs.compute(1000, 1e-10);
+        std::printf("EIGS %d %.15f %.15f %.15f\n", nconv, eigs.eigenvalues()[0], eigs.eigenvalues()[1],
+                    eigs.eigenvalues()[2]);
+        // Time_evol_test.cu: exp(-i H t) on a product state, host vectors through the C ABI
+        std::vector<double> phi0(2 * sp.rows(), 0.0), phi(2 * sp.rows());
+        phi0[0] = 1.0;
+        ed_krylov_cfg kc{200, 0, 1e-12, 0, 0};
+        ed_krylov_result kr{};
+        const double t = 0.5;
+        if (ed_krylov_evolve(h.handle(), &kc, phi0.data(), ED_MEM_HOST, 1, &t, phi.data(), ED_MEM_HOST, &kr, nullptr) !=
+            ED_OK)
+            return 3;
+        double nrm = 0.0;
+        for (double v : phi) nrm += v * v;
+        std::printf("KRYLOV steps %d norm2 %.15f\n", kr.steps, nrm);
     } catch (const ed::Error& e) {
         std::printf("error %d %s\n", (int)e.status, e.what());
         return 2;

@@ -33,6 +33,11 @@ def test_cpp_header_lanczos_on_gpu(tmp_path, edlib, golden_energies):
     e0 = float(out.split("E0 ")[1].split()[0])
     g = golden_energies["chain8_pbc_q44_U4"]["E0"]
     assert abs(e0 - g) < 1e-10 * abs(g)
+    eig = out.split("EIGS ")[1].split()
+    assert int(eig[0]) == 3 and abs(float(eig[1]) - g) < 1e-10 * abs(g)
+    assert abs(float(eig[2]) - golden_energies["chain8_pbc_q44_U4"]["E1"]) < 1e-9
+    kry = out.split("KRYLOV ")[1].split()
+    assert abs(float(kry[3]) - 1.0) < 1e-12
 
 
 def test_gather_schedule_host_check(tmp_path):
