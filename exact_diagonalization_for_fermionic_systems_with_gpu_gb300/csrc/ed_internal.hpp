@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -199,5 +200,9 @@ ed_status ee_bidiag_blocks(int device, cudaStream_t s, const double* blocks, con
                            const std::vector<int>& mm, const std::vector<int>& nn, const std::vector<int64_t>& svo,
                            std::vector<double>* sv_host, std::vector<char>* handled);
 void lanczos_basis(void* ws_slot, const int64_t** basis, int64_t* stride, const int** e_dev);
+// The vectors of the last non-stored run on a workspace, regenerated one by
+// one for visit(k, q_k) (ed_lanczos.cu).
+ed_status lanczos_replay(ed_op* op, void* ws_slot, int n,
+                         const std::function<cudaError_t(int, const int64_t*)>& visit, cudaStream_t s);
 
 }  // namespace ed

@@ -111,6 +111,36 @@ __global__ void __launch_bounds__(kKrThreads) k_krylov_combine(const int64_t* __
     }
 }
 
+// Two-pass-matvec operators (the basis is not kept): out[t][p(i)] +=
+// f * coef[t] q[i] for the regenerated real vector q in the permuted down
+// order, p(i) = u * dim_dn + perm[c] its table-order position, f = i when
+// times_i; every position is touched by one thread.
+__global__ void __launch_bounds__(kKrThreads) k_krylov_acc_perm(const int64_t* __restrict__ q, int64_t dimUP,
+                                                               int64_t dimDN, const uint32_t* __restrict__ perm,
+                                                               const double2* __restrict__ coef, int nt,
+                                                               double2* __restrict__ out, int64_t out_stride,
+                                                               int times_i) {
+    const int64_t D = dimUP * dimDN;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < D; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = i / dimDN, c = i - u * dimDN;
+        const int64_t p = u * dimDN + __ldg(perm + c);
+        const double w = (double)__ldg(q + i);
+        for (int t = 0; t < nt; ++t) {
+            const double2 cf = __ldg(coef + t);
+            double2* o = out + (size_t)t * out_stride + p;
+            double2 v = *o;
+            if (times_i) {
+                v.x -= cf.y * w;
+                v.y += cf.x * w;
+            } else {
+                v.x += cf.x * w;
+                v.y += cf.y * w;
+            }
+            *o = v;
+        }
+    }
+}
+
 }  // namespace
 }  // namespace ed
 
@@ -126,7 +156,6 @@ ed_status ed_krylov_evolve(ed_op* op, const ed_krylov_cfg* cfg, const double* ps
     if (out_mem != ED_MEM_HOST && out_mem != ED_MEM_DEVICE) return ED_ERR_ARG;
     for (int t = 0; t < n_times; ++t)
         if (!std::isfinite(times[t])) return ED_ERR_ARG;
-    if (op->striped) return ED_ERR_NOT_BUILT;
     if (cudaSetDevice(op->device) != cudaSuccess) return ED_ERR_CUDA;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const int64_t D = op->D;
@@ -191,13 +220,14 @@ ed_status ed_krylov_evolve(ed_op* op, const ed_krylov_cfg* cfg, const double* ps
         for (int p = 0; p < 2; ++p)
             if (n2[p] > 0.0) runs.push_back({tmp, p});
     }
-    if (runs.empty() && n_times > 0 && !acc) KR_CK(cudaMemsetAsync(dout, 0, vbytes * n_times, s));
+    if ((runs.empty() || op->striped) && n_times > 0 && !acc) KR_CK(cudaMemsetAsync(dout, 0, vbytes * n_times, s));
 
     ed_lanczos_cfg lc{};
     lc.max_steps = cfg->max_steps;
     lc.mode = ED_LANCZOS_FIXED;
     lc.reorth = cfg->reorth;
-    lc.ritz = ED_RITZ_STORED;
+    // the two-pass matvec's sectors keep three vectors and regenerate the basis
+    lc.ritz = op->striped ? ED_RITZ_NONE : ED_RITZ_STORED;
     lc.start = ED_START_USER;
     std::vector<double> alpha(cfg->max_steps + 2), beta(cfg->max_steps + 2);
     int max_n = 0;
@@ -242,6 +272,26 @@ ed_status ed_krylov_evolve(ed_op* op, const ed_krylov_cfg* cfg, const double* ps
             }
             const double* cl = c.data() + (size_t)2 * n * t + 2 * (n - 1);
             err = std::max(err, beta[n] * std::hypot(cl[0], cl[1]) * beta[0]);
+        }
+        if (op->striped) {
+            // coefficients time-major per vector: coefk[k][t]
+            std::vector<double2> coefk((size_t)n * n_times);
+            for (int t = 0; t < n_times; ++t)
+                for (int k = 0; k < n; ++k) coefk[(size_t)k * n_times + t] = coef[(size_t)t * n + k];
+            KR_CK(cudaMemcpyAsync(dcoef, coefk.data(), sizeof(double2) * coefk.size(), cudaMemcpyHostToDevice, s));
+            const int cg = kr_grid(D);
+            const int ti = r.part == 1 ? 1 : 0;
+            double2* o = reinterpret_cast<double2*>(dout);
+            st = lanczos_replay(op, *lanczos_ws_slot(op), n, [&](int k, const int64_t* qk) -> cudaError_t {
+                k_krylov_acc_perm<<<cg, kKrThreads, 0, s>>>(qk, op->dimUP, op->dimDN, op->d_permDN,
+                                                             dcoef + (size_t)k * n_times, n_times, o, D, ti);
+                ++launches;
+                return cudaGetLastError();
+            }, s);
+            if (st != ED_OK) { release(); return st; }
+            KR_CK(cudaStreamSynchronize(s));
+            written = true;
+            continue;
         }
         KR_CK(cudaMemcpyAsync(dcoef, coef.data(), sizeof(double2) * coef.size(), cudaMemcpyHostToDevice, s));
         const int cg = kr_grid(D);

@@ -836,6 +836,45 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
 }
 
 
+// Regenerate the vectors q_0 .. q_{n-1} of the last lanczos_run on this
+// workspace (non-stored, per-step kernels: the same start vector, still in
+// fbuf, and the same deterministic recurrence give them bit for bit) and
+// hand each to visit(k, q_k) as soon as it exists (in the two-pass matvec's
+// permuted down order for such operators).
+ed_status lanczos_replay(ed_op* op, void* ws_slot, int n, const std::function<cudaError_t(int, const int64_t*)>& visit,
+                         cudaStream_t s) {
+    Workspace* w = &reinterpret_cast<WsHolder*>(ws_slot)->ws;
+    if (n < 1 || n > w->max_steps || w->basis_slots < 3) return ED_ERR_ARG;
+    const int64_t DW = w->DW;
+    LzState* lz = w->lz;
+    auto slot = [&](int j) -> int64_t* { return w->basis + (size_t)(j % 3) * (size_t)w->stride; };
+    LZ_CK(cudaMemsetAsync(w->h.counter, 0, sizeof(unsigned int) * 4, s));
+    const double* sv = w->fbuf;
+    if (op->striped) {
+        LZ_CK(launch_permute_f64(op, w->fbuf, reinterpret_cast<double*>(w->u), 1, s));
+        sv = reinterpret_cast<const double*>(w->u);
+    }
+    LZ_CK(launch_emax(sv, DW, w->emax, w->flag, s));
+    k_lz_start<<<lz_grid(DW), kLzThreads, 0, s>>>(sv, DW, w->emax, w->flag, slot(0), lz);
+    LZ_CK(cudaGetLastError());
+    LZ_CK(visit(0, slot(0)));
+    for (int k = 0; k + 1 < n; ++k) {
+        LZ_CK(launch_matvec_lz(op, slot(k), w->u, lz, w->fxbound, k, s));
+        const int64_t* pk = k > 0 ? slot(k - 1) : slot(k);
+        k_lz_axpy<<<lz_grid(DW), kLzThreads, 0, s>>>(w->u, slot(k), pk, slot(k + 1), DW, lz, k);
+        LZ_CK(cudaGetLastError());
+        LZ_CK(visit(k + 1, slot(k + 1)));
+    }
+    int err = 0;
+    LZ_CK(cudaMemcpyAsync(&err, op->d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+    LZ_CK(cudaStreamSynchronize(s));
+    if (err) {
+        cudaMemset(op->d_err, 0, sizeof(int));
+        return ED_ERR_TIMEOUT;
+    }
+    return ED_OK;
+}
+
 // B fixed-step Lanczos runs of operators that share their hopping tables, in
 // one persistent launch (k_lz_batch), each with its own workspace (the op's)
 // and start vector; then each run's T and Ritz vector as lanczos_run forms

@@ -397,8 +397,11 @@ ed_status ed_dense_sym_eigen(int n, const double* a, double* w, double* z);
  * for each nonzero part (exp(-iHt) is linear).  psi0: 2*rows doubles
  * (complex, interleaved re, im) at psi0_mem; psi_out: n_times x 2*rows
  * doubles at out_mem, time-major, overwritten (added to with accumulate);
- * times: host.  Operators that need the two-pass matvec return
- * ED_ERR_NOT_BUILT.  Synchronous. */
+ * times: host.  Operators that need the two-pass matvec (sectors whose down
+ * rows exceed shared memory) keep three vectors and regenerate the basis in
+ * a second recurrence (as ED_RITZ_RECOMPUTE and the reference's
+ * Krylov_time_evol do), adding each vector's share as it appears.
+ * Synchronous. */
 typedef struct {
     int32_t max_steps;   /* Krylov dimension cap (the reference's loop: 1000) */
     int32_t reorth;      /* 1: full reorthogonalisation of the basis */
