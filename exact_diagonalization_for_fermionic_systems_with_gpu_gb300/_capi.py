@@ -65,6 +65,15 @@ class ed_kubo_result(C.Structure):
     _fields_ = [("drude", C.c_double), ("kinetic", C.c_double), ("vertex", C.c_double)]
 
 
+class ed_tune_cfg(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("apply", C.c_int32)]
+
+
+class ed_tune_result(C.Structure):
+    _fields_ = [("persistent", C.c_int32), ("candidates", C.c_int32), ("row_cost", C.c_double),
+                ("us_per_step", C.c_double), ("per_step_us", C.c_double), ("persistent_us", C.c_double * 3)]
+
+
 class ed_eigs_cfg(C.Structure):
     _fields_ = [("nev", C.c_int32), ("ncv", C.c_int32), ("max_restarts", C.c_int32), ("start", C.c_int32),
                 ("tol", C.c_double), ("seed", C.c_uint64)]
@@ -109,6 +118,8 @@ SIGNATURES = {
                                  C.c_int, C.c_void_p, C.c_void_p, C.POINTER(ed_lanczos_result), C.c_void_p]),
     "ed_lanczos_batch": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(ed_lanczos_cfg), C.c_void_p, C.c_int, C.c_void_p,
                                    C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ed_op_autotune": (C.c_int, [C.c_void_p, C.POINTER(ed_tune_cfg), C.POINTER(ed_tune_result), C.c_void_p]),
+    "ed_op_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(ed_tune_result)]),
     "ed_random_vector": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p]),
     "ed_random_vector_device": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p, C.c_void_p]),
     "ed_tridiag_lowest": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

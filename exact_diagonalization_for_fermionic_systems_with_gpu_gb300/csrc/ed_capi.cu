@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -561,6 +562,87 @@ ed_status ed_lanczos_batch(ed_op* const* ops, int n_ops, const ed_lanczos_cfg* c
     if (cudaSetDevice(ops[0]->device) != cudaSuccess) return ED_ERR_CUDA;
     return ed::lanczos_batch_run(ops, n_ops, cfg, starts, start_mem, evecs, evec_mem, alpha, beta, res,
                                  reinterpret_cast<cudaStream_t>(stream));
+}
+
+// Rebuild and upload the persistent kernel's row plan with row-cost weight w.
+static ed_status set_row_plan(ed_op* op, double w) {
+    std::vector<uint32_t> rs, rl, rq;
+    ed::row_plan(op->tup, op->tma_grid, &rs, &rl, &rq, w);
+    if (cudaMemcpy(op->d_rowStart, rs.data(), sizeof(uint32_t) * rs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(op->d_rowList, rl.data(), sizeof(uint32_t) * rl.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(op->d_rowQueue, rq.data(), sizeof(uint32_t) * rq.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        return ED_ERR_CUDA;
+    op->row_cost = w;
+    return ED_OK;
+}
+
+ed_status ed_op_autotune(ed_op* op, const ed_tune_cfg* cfg, ed_tune_result* res, void* stream) {
+    if (!op || !cfg || cfg->steps < 2 || cfg->steps > 10000) return ED_ERR_ARG;
+    if (cudaSetDevice(op->device) != cudaSuccess) return ED_ERR_CUDA;
+    ed_tune_result r{};
+    ed_lanczos_cfg lc{};
+    lc.max_steps = cfg->steps;
+    lc.mode = ED_LANCZOS_FIXED;
+    lc.ritz = ED_RITZ_NONE;
+    lc.start = ED_START_RANDOM;
+    const int saved_mode = op->lz_mode;
+    const double saved_w = op->row_cost;
+    // one candidate: a warm-up run, then the best of two timed runs
+    auto time_run = [&](double* us) -> ed_status {
+        ed_status st = ed_lanczos_run(op, &lc, nullptr, ED_MEM_DEVICE, nullptr, ED_MEM_DEVICE, nullptr, nullptr,
+                                      nullptr, stream);
+        double best = 1e300;
+        for (int rep = 0; st == ED_OK && rep < 2; ++rep) {
+            const auto t0 = std::chrono::steady_clock::now();
+            st = ed_lanczos_run(op, &lc, nullptr, ED_MEM_DEVICE, nullptr, ED_MEM_DEVICE, nullptr, nullptr, nullptr,
+                                stream);
+            const double dt = std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now() - t0).count();
+            best = std::min(best, dt);
+        }
+        *us = best / cfg->steps;
+        return st;
+    };
+    ed_status st = ED_OK;
+    op->lz_mode = 1;
+    st = time_run(&r.per_step_us);
+    ++r.candidates;
+    r.persistent = 0;
+    r.us_per_step = r.per_step_us;
+    r.row_cost = saved_w;
+    const double weights[3] = {0.4, 0.8, 1.2};
+    if (st == ED_OK && op->tma_smem > 0) {
+        op->lz_mode = 2;
+        for (int k = 0; k < 3 && st == ED_OK; ++k) {
+            st = set_row_plan(op, weights[k]);
+            if (st == ED_OK) st = time_run(&r.persistent_us[k]);
+            ++r.candidates;
+            if (st == ED_OK && r.persistent_us[k] < r.us_per_step) {
+                r.us_per_step = r.persistent_us[k];
+                r.persistent = 1;
+                r.row_cost = weights[k];
+            }
+        }
+    }
+    if (st == ED_OK && cfg->apply) {
+        op->lz_mode = r.persistent ? 2 : 1;
+        if (op->tma_smem > 0) st = set_row_plan(op, r.persistent ? r.row_cost : saved_w);
+    } else {
+        op->lz_mode = saved_mode;
+        if (op->tma_smem > 0) {
+            const ed_status s2 = set_row_plan(op, saved_w);
+            if (st == ED_OK) st = s2;
+        }
+    }
+    if (res) *res = r;
+    return st;
+}
+
+ed_status ed_op_set_tuning(ed_op* op, const ed_tune_result* tuned) {
+    if (!op || !tuned) return ED_ERR_ARG;
+    if (cudaSetDevice(op->device) != cudaSuccess) return ED_ERR_CUDA;
+    op->lz_mode = tuned->persistent ? 2 : 1;
+    if (op->tma_smem > 0 && tuned->persistent) return set_row_plan(op, tuned->row_cost);
+    return ED_OK;
 }
 
 ed_status ed_random_vector(int64_t n, uint64_t seed, double* out_host) {

@@ -139,6 +139,10 @@ struct ed_op {
     // two-pass matvec (striped): down index permuted by perm (new -> old)
     bool striped = false;
     int st_grid = 0, st_win = 0, st_chunk = 0;
+    // tuning (ed_op_autotune): Lanczos kernels 0 by the default rule, 1 per
+    // step, 2 persistent; weight of the persistent kernel's row queue
+    int lz_mode = 0;
+    double row_cost = -1.0;
     int64_t st_bw = 0, st_cpad = 0;
     uint32_t* d_permDN = nullptr;
     uint32_t* d_sched32 = nullptr;
@@ -168,8 +172,9 @@ int tma_grid(const ed_op* op);
 // Rows of each of the G CTAs: longest-processing-time-first under the cost
 // model 1 + w * len_up(u) / mean len_up (w from ED_ROW_COST_UP, default kRowCostUp).
 // queue: all rows in decreasing order of that cost.
+// w < 0: ED_ROW_COST_UP or kRowCostUp.
 void row_plan(const SpinTable& up, int G, std::vector<uint32_t>* start, std::vector<uint32_t>* list,
-              std::vector<uint32_t>* queue);
+              std::vector<uint32_t>* queue, double w = -1.0);
 cudaError_t launch_matvec_tma(const ed_op* op, const MvArgs& a, int out, cudaStream_t s);
 cudaError_t launch_striped_down(const ed_op* op, const StripedArgs& g, cudaStream_t s);
 cudaError_t launch_striped_up(const ed_op* op, const MvArgs& a, const StripedArgs& g, int out, cudaStream_t s);

@@ -527,7 +527,10 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     // classes), where the per-step kernels measured faster.
     const char* fz = std::getenv("ED_LZ_FUSED");
     const bool force = fz && fz[0] == '1', never = fz && fz[0] == '0';
-    bool fused = op->tma_smem > 0 && !cfg->reorth && !prof && !never && (force || op->mv.dnSched != nullptr);
+    // ed_op_autotune's choice, when made, replaces the default rule
+    const bool rule = fz ? (force || op->mv.dnSched != nullptr)
+                         : (op->lz_mode == 2 || (op->lz_mode == 0 && op->mv.dnSched != nullptr));
+    bool fused = op->tma_smem > 0 && !cfg->reorth && !prof && !never && rule;
     int steps_run = 0;
     int n_fused = 0;  // persistent launches
     int j = 0;

@@ -150,10 +150,12 @@ int tma_grid(const ed_op* op) {
 }
 
 void row_plan(const SpinTable& up, int G, std::vector<uint32_t>* start, std::vector<uint32_t>* list,
-              std::vector<uint32_t>* queue) {
+              std::vector<uint32_t>* queue, double w) {
     const int64_t n = up.count;
-    double w = kRowCostUp;
-    if (const char* e = std::getenv("ED_ROW_COST_UP")) w = std::atof(e);
+    if (w < 0.0) {
+        w = kRowCostUp;
+        if (const char* e = std::getenv("ED_ROW_COST_UP")) w = std::atof(e);
+    }
     double mean = 0.0;
     for (int64_t u = 0; u < n; ++u) mean += up.len[u];
     mean = n ? mean / (double)n : 0.0;

@@ -217,6 +217,20 @@ class Hubbard:
         check(self._lib.ed_op_perform(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
                                       _capi.ED_MEM_DEVICE, C.c_void_p(s.cuda_stream)), "ed_op_perform")
 
+    def autotune(self, steps: int = 30, apply: bool = True) -> dict:
+        """ed_op_autotune: time the Lanczos step's kernel choices on this
+        operator and (apply) keep the fastest.  Returns the timings and the
+        result structure (for set_tuning on operators of the same shape)."""
+        cfg = _capi.ed_tune_cfg(int(steps), 1 if apply else 0)
+        res = _capi.ed_tune_result()
+        check(_capi.load().ed_op_autotune(self.handle, C.byref(cfg), C.byref(res), None), "ed_op_autotune")
+        return {"persistent": bool(res.persistent), "row_cost": res.row_cost, "us_per_step": res.us_per_step,
+                "per_step_us": res.per_step_us, "persistent_us": list(res.persistent_us), "result": res}
+
+    def set_tuning(self, result) -> None:
+        """ed_op_set_tuning: apply another operator's autotune result."""
+        check(_capi.load().ed_op_set_tuning(self.handle, C.byref(result)), "ed_op_set_tuning")
+
     def close(self) -> None:
         if getattr(self, "_h", None):
             self._lib.ed_op_destroy(self._h)

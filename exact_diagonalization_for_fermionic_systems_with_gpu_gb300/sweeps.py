@@ -105,18 +105,27 @@ def flux_phis(n_phi: int = 16) -> np.ndarray:
 
 def flux_sweep(phis: Optional[Sequence[float]] = None, n_up: int = 6, n_dn: int = 6, U: float = 4.0,
                steps: int = 300, mode: str = "fixed", response_steps: int = 200, seed: int = 0,
-               rand: Optional[Sequence[float]] = None, timing: Optional[SweepTiming] = None) -> List[FluxPoint]:
+               rand: Optional[Sequence[float]] = None, timing: Optional[SweepTiming] = None,
+               autotune: bool = False) -> List[FluxPoint]:
     """E0(Phi), dE0/dPhi, d2E0/dPhi2 of Kagome12 (complex operator at every
-    Phi, Phi = 0 included, so the second-order response sees the current)."""
+    Phi, Phi = 0 included, so the second-order response sees the current).
+    autotune: time the Lanczos kernel choices on the first twist's operator
+    and apply the fastest to every twist (same shape, same tables)."""
     phis = flux_phis() if phis is None else phis
     t = timing if timing is not None else SweepTiming()
     out: List[FluxPoint] = []
+    tuned = None
     t0 = time.perf_counter()
     for k, phi in enumerate(phis):
         ti = time.perf_counter()
         terms = L.kagome12(rand, flux=float(phi), peierls=True)
         d1t, d2t = L.kagome12_flux_derivatives(float(phi), rand)
         H = Hubbard(H_TBq(12, n_up).extend(terms), H_TBq(12, n_dn).extend(terms), U)
+        if autotune:
+            if tuned is None:
+                tuned = H.autotune(steps=30)["result"]
+            else:
+                H.set_tuning(tuned)
         dH = Hubbard(H_TBq(12, n_up).extend(d1t), H_TBq(12, n_dn).extend(d1t), 0.0)
         d2H = Hubbard(H_TBq(12, n_up).extend(d2t), H_TBq(12, n_dn).extend(d2t), 0.0)
         _sync()
@@ -285,9 +294,10 @@ def _run(a, n, form: str):
     try:
         tm = SweepTiming()
         if a.what == "flux":
+            tune = form == "tuned"
             if a.warmup:
-                flux_sweep(flux_phis(n)[: a.warmup], steps=a.steps, mode=a.mode, seed=a.seed)
-            pts = flux_sweep(flux_phis(n), steps=a.steps, mode=a.mode, seed=a.seed, timing=tm)
+                flux_sweep(flux_phis(n)[: a.warmup], steps=a.steps, mode=a.mode, seed=a.seed, autotune=tune)
+            pts = flux_sweep(flux_phis(n), steps=a.steps, mode=a.mode, seed=a.seed, timing=tm, autotune=tune)
         else:
             bt = a.batch if form == "tuned" else 1
             if a.warmup:

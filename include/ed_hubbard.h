@@ -234,6 +234,34 @@ ed_status ed_lanczos_batch(ed_op* const* ops, int n_ops, const ed_lanczos_cfg* c
                            int start_mem, double* evecs, int evec_mem, double* alpha, double* beta,
                            ed_lanczos_result* res, void* stream);
 
+/* Autotuning of the Lanczos step for one operator: the per-step kernels and
+ * the persistent kernel with three row-cost weights of its work queue
+ * (the cost of a row taken as 1 + w len_up(u) / mean len_up, w = 0.4, 0.8,
+ * 1.2) each run `steps` fixed Lanczos steps (one warm-up run, best of two
+ * timed runs); with apply, the fastest becomes the operator's choice for
+ * ed_lanczos_run and its users (the environment variable ED_LZ_FUSED still
+ * overrides).  Every candidate computes the same coefficients bit for bit;
+ * only the time differs.  Synchronous. */
+typedef struct {
+    int32_t steps;           /* Lanczos steps per timed run (e.g. 30) */
+    int32_t apply;           /* 1: keep the fastest on the operator */
+} ed_tune_cfg;
+
+typedef struct {
+    int32_t persistent;      /* the choice: 1 persistent kernel, 0 per-step kernels */
+    int32_t candidates;      /* configurations timed */
+    double row_cost;         /* the choice's row-cost weight (persistent) */
+    double us_per_step;      /* the choice's time per step, host clock */
+    double per_step_us;      /* per-step kernels */
+    double persistent_us[3]; /* persistent kernel, w = 0.4, 0.8, 1.2 (0: no shared-memory plan) */
+} ed_tune_result;
+
+ed_status ed_op_autotune(ed_op* op, const ed_tune_cfg* cfg, ed_tune_result* res, void* stream);
+
+/* Apply an ed_op_autotune result to another operator of the same shape
+ * (e.g. the next twist or disorder sample of a sweep). */
+ed_status ed_op_set_tuning(ed_op* op, const ed_tune_result* tuned);
+
 /* Same generator on the device: out (device, n doubles), async on stream. */
 ed_status ed_random_vector_device(int64_t n, uint64_t seed, double* out_device, void* stream);
 

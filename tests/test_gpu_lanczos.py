@@ -281,3 +281,33 @@ def test_lanczos_batch_rejects_other_tables(ed):
     b = ed.Hubbard(ed.H_TBq(12, 6).extend(L.chain(12)), ed.H_TBq(12, 6).extend(L.chain(12)), 1.0)
     with pytest.raises(ed.EdError):
         ed.lanczos_batch([a, b], 10)
+
+
+@pytest.mark.parametrize("case", ["chain12_66", "kagome12_flux"])
+def test_autotune_keeps_results(ed, case):
+    """ed_op_autotune times the per-step and persistent kernels (three queue
+    weights) and applies the fastest; the Lanczos coefficients afterwards are
+    the same bit for bit, and set_tuning carries the choice to a second
+    operator of the same shape."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, sweeps
+    if case == "chain12_66":
+        eu, edn = sweeps.mbl_disorder(0, 12, 6.0)
+        make = lambda: ed.Hubbard(ed.H_TBq(12, 6).extend(sweeps.mbl_chain_terms(eu)),
+                                  ed.H_TBq(12, 6).extend(sweeps.mbl_chain_terms(edn)), 1.0)
+    else:
+        t = L.kagome12(flux=0.3)
+        make = lambda: ed.Hubbard(ed.H_TBq(12, 6).extend(t), ed.H_TBq(12, 6).extend(t), 4.0)
+    op = make()
+    lz0 = ed.Lanczos()
+    lz0.eigen(op, max_steps=40, mode="fixed", ritz="none", seed=3)
+    info = op.autotune(steps=20)
+    assert info["per_step_us"] > 0 and all(v > 0 for v in info["persistent_us"])
+    assert info["us_per_step"] == min([info["per_step_us"]] + info["persistent_us"])
+    lz1 = ed.Lanczos()
+    lz1.eigen(op, max_steps=40, mode="fixed", ritz="none", seed=3)
+    assert lz1.a == lz0.a and lz1.b == lz0.b
+    op2 = make()
+    op2.set_tuning(info["result"])
+    lz2 = ed.Lanczos()
+    lz2.eigen(op2, max_steps=40, mode="fixed", ritz="none", seed=3)
+    assert lz2.a == lz0.a and lz2.b == lz0.b
