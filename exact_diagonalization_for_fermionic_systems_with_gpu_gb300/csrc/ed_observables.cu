@@ -4,7 +4,8 @@
 // Kubo Drude weight (HubMatrix_GPU.cuh:820-849,
 // drude_v2_cal_Kagome_randomHop.cu:183-220), the second-order flux response
 // by a Lanczos solve of the linear-response equation, and the half-system
-// entanglement entropy (entangle_entropy.h:22-44,177-197 + cusolverDnDgesvd).
+// entanglement entropy (entangle_entropy.h:22-44,177-197; block singular
+// values in ed_ee_bidiag.cu, cusolverDnDgesvd for blocks beyond it).
 #include <cuda_runtime.h>
 #include <cusolverDn.h>
 
@@ -242,9 +243,10 @@ namespace {
 using ed::kObBlocks;
 using ed::kObThreads;
 
-// Block SVDs of the entanglement matrix.  cusolverDnDgesvd on a block of a
-// few hundred rows is latency-bound (one SM's worth of work per call), so
-// the blocks run concurrently: a per-device pool of workers, each a host
+// Block SVDs by cusolverDnDgesvd, for the blocks the cluster kernel leaves
+// (or every block with ED_EE_METHOD=gesvd).  One call runs a block at one
+// SM's FP64 rate, so the blocks run concurrently: a per-device pool of
+// workers, each a host
 // thread with its own stream, cuSOLVER handle and workspace (created on
 // first use, kept for the life of the process), takes the blocks
 // largest-first to the least-loaded worker.
@@ -806,9 +808,9 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
     m.blk_off = doff;
     m.nqd = nqd;
     ed::k_ee_scatter<<<ob_grid(op->D), kObThreads, 0, s>>>(dpsi, op->dimUP, op->dimDN, m, blocks);
-    // singular values of every block (cusolverDnDgesvd, jobu = jobvt = 'N',
-    // as entangle_entropy.h:231-291), the blocks spread over the device's
-    // worker streams; all singular values land in one device array
+    // singular values of every block; cusolverDnDgesvd (jobu = jobvt = 'N',
+    // as entangle_entropy.h:231-291) on the device's worker streams for the
+    // blocks the cluster bidiagonalisation does not take
     std::vector<int> mmv(off.size()), nnv(off.size());
     std::vector<int64_t> svo(off.size() + 1, 0);
     for (size_t k = 0; k < off.size(); ++k) {

@@ -366,8 +366,11 @@ ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double
                       double* second, void* stream);
 /* Entanglement entropy of psi for the sites in a_mask: the matrix
  * psi[(a_up a_dn), (b_up b_dn)] (entangle_entropy.h:177-197) is block-diagonal
- * in the particle numbers of A; singular values s of every block by
- * cusolverDnDgesvd.  s_vn = -sum s^2 ln s^2 (von Neumann entropy of the
+ * in the particle numbers of A; singular values s of every block from a
+ * Householder bidiagonalisation on a thread-block cluster and Golub-Kahan
+ * SVD steps on the host (blocks too large for a cluster's shared memory:
+ * cusolverDnDgesvd, as entangle_entropy.h:231-291; ED_EE_METHOD=gesvd for
+ * every block).  s_vn = -sum s^2 ln s^2 (von Neumann entropy of the
  * reduced density matrix), s_ref = -sum s ln s (the sum the reference
  * drivers print, Hubbard_EE_test.cu:80-83).  Real operators. */
 ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_t a_mask, double* s_vn,
