@@ -246,10 +246,9 @@ using ed::kObThreads;
 // Block SVDs by cusolverDnDgesvd, for the blocks the cluster kernel leaves
 // (or every block with ED_EE_METHOD=gesvd).  One call runs a block at one
 // SM's FP64 rate, so the blocks run concurrently: a per-device pool of
-// workers, each a host
-// thread with its own stream, cuSOLVER handle and workspace (created on
-// first use, kept for the life of the process), takes the blocks
-// largest-first to the least-loaded worker.
+// workers, each a host thread with its own stream, cuSOLVER handle and
+// workspace (created on first use, kept for the life of the process), takes
+// the blocks largest-first to the least-loaded worker.
 struct EeWorker {
     cudaStream_t st = nullptr;
     cusolverDnHandle_t h = nullptr;
