@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIBNAME = "libedgb300.so"
 
 SOURCES = ["ed_tables.cpp", "ed_matvec.cu", "ed_matvec_tma.cu", "ed_matvec_striped.cu", "ed_lanczos.cu", "ed_lanczos_fused.cu", "ed_tridiag.cpp", "ed_capi.cu",
-           "ed_observables.cu", "ed_noalloc.cu", "ed_krylov.cu", "ed_eigs.cu", "ed_ee_bidiag.cu"]
+           "ed_observables.cu", "ed_noalloc.cu", "ed_krylov.cu", "ed_eigs.cu", "ed_ee_bidiag.cu", "ed_dense.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", str(ROOT / "include")]

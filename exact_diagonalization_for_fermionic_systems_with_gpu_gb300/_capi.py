@@ -120,6 +120,7 @@ SIGNATURES = {
                                    C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_op_autotune": (C.c_int, [C.c_void_p, C.POINTER(ed_tune_cfg), C.POINTER(ed_tune_result), C.c_void_p]),
     "ed_op_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(ed_tune_result)]),
+    "ed_op_write_dense": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "ed_random_vector": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p]),
     "ed_random_vector_device": (C.c_int, [C.c_int64, C.c_uint64, C.c_void_p, C.c_void_p]),
     "ed_tridiag_lowest": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

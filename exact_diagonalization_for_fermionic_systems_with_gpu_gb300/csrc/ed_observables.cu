@@ -288,7 +288,9 @@ ed_status ee_block_svd(int device, cudaStream_t s, double* blocks, const std::ve
     const int K = ee_workers();
     while ((int)pool->w.size() < K) {
         EeWorker w;
-        if (cudaStreamCreateWithFlags(&w.st, cudaStreamNonBlocking) != cudaSuccess) return ED_ERR_CUDA;
+        // a blocking stream: it orders itself with the legacy default stream,
+        // which cuSOLVER may use inside a call
+        if (cudaStreamCreate(&w.st) != cudaSuccess) return ED_ERR_CUDA;
         if (cusolverDnCreate(&w.h) != CUSOLVER_STATUS_SUCCESS) return ED_ERR_CUDA;
         cusolverDnSetStream(w.h, w.st);
         if (cudaMalloc(&w.info, sizeof(int)) != cudaSuccess) return ED_ERR_ALLOC;
@@ -316,27 +318,39 @@ ed_status ee_block_svd(int device, cudaStream_t s, double* blocks, const std::ve
     std::vector<ed_status> res(K, ED_OK);
     auto run = [&](int q) {
         EeWorker& w = pool->w[q];
-        if (cudaSetDevice(device) != cudaSuccess || cudaStreamWaitEvent(w.st, ready, 0) != cudaSuccess) {
+        if (cudaSetDevice(device) != cudaSuccess) {
+            res[q] = ED_ERR_CUDA;
+            return;
+        }
+        // workspace for the largest of this worker's blocks, sized before any
+        // of them is queued (the stream is idle: its last call was waited for)
+        int lw_max = 0, n_max = 0;
+        for (int k : part[q]) {
+            int lw = 0;
+            if (cusolverDnDgesvd_bufferSize(w.h, mm[k], nn[k], &lw) != CUSOLVER_STATUS_SUCCESS) { res[q] = ED_ERR_CUDA; return; }
+            lw_max = std::max(lw_max, lw);
+            n_max = std::max(n_max, nn[k]);
+        }
+        if (cudaStreamSynchronize(w.st) != cudaSuccess) { res[q] = ED_ERR_CUDA; return; }
+        if (lw_max > w.lwork) {
+            cudaFree(w.work);
+            w.work = nullptr;
+            w.lwork = 0;
+            if (cudaMalloc(&w.work, sizeof(double) * lw_max) != cudaSuccess) { res[q] = ED_ERR_ALLOC; return; }
+            w.lwork = lw_max;
+        }
+        if (n_max > w.rwork_n) {
+            cudaFree(w.rwork);
+            w.rwork = nullptr;
+            w.rwork_n = 0;
+            if (cudaMalloc(&w.rwork, sizeof(double) * n_max) != cudaSuccess) { res[q] = ED_ERR_ALLOC; return; }
+            w.rwork_n = n_max;
+        }
+        if (cudaStreamWaitEvent(w.st, ready, 0) != cudaSuccess) {
             res[q] = ED_ERR_CUDA;
             return;
         }
         for (int k : part[q]) {
-            int lw = 0;
-            if (cusolverDnDgesvd_bufferSize(w.h, mm[k], nn[k], &lw) != CUSOLVER_STATUS_SUCCESS) { res[q] = ED_ERR_CUDA; return; }
-            if (lw > w.lwork) {
-                cudaFree(w.work);
-                w.work = nullptr;
-                w.lwork = 0;
-                if (cudaMalloc(&w.work, sizeof(double) * lw) != cudaSuccess) { res[q] = ED_ERR_ALLOC; return; }
-                w.lwork = lw;
-            }
-            if (nn[k] > w.rwork_n) {
-                cudaFree(w.rwork);
-                w.rwork = nullptr;
-                w.rwork_n = 0;
-                if (cudaMalloc(&w.rwork, sizeof(double) * nn[k]) != cudaSuccess) { res[q] = ED_ERR_ALLOC; return; }
-                w.rwork_n = nn[k];
-            }
             if (cusolverDnDgesvd(w.h, 'N', 'N', mm[k], nn[k], blocks + off[k], mm[k], sv_all + svo[k], nullptr,
                                  mm[k], nullptr, nn[k], w.work, w.lwork, w.rwork, w.info) != CUSOLVER_STATUS_SUCCESS) {
                 res[q] = ED_ERR_CUDA;

@@ -217,6 +217,14 @@ class Hubbard:
         check(self._lib.ed_op_perform(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()),
                                       _capi.ED_MEM_DEVICE, C.c_void_p(s.cuda_stream)), "ed_op_perform")
 
+    def Write(self) -> np.ndarray:
+        """The dense matrix (rows x rows, complex for complex operators)
+        (Hubbard::Write, HubMatrix_GPU.cuh:224-240)."""
+        n = self.rows()
+        H = np.empty((n, 2 * n) if self.is_complex else (n, n))
+        check(_capi.load().ed_op_write_dense(self.handle, _ptr(H), _capi.ED_MEM_HOST, None), "ed_op_write_dense")
+        return H.view(np.complex128) if self.is_complex else H
+
     def autotune(self, steps: int = 30, apply: bool = True) -> dict:
         """ed_op_autotune: time the Lanczos step's kernel choices on this
         operator and (apply) keep the fastest.  Returns the timings and the

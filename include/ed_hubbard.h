@@ -217,6 +217,13 @@ ed_status ed_lanczos_run(ed_op* op, const ed_lanczos_cfg* cfg,
                          double* alpha, double* beta,
                          ed_lanczos_result* res, void* stream);
 
+/* The operator as a dense rows x rows matrix, row-major (Hubbard::Write,
+ * MBL_test/include/HubMatrix_GPU.cuh:184-240, for the dense-ED drivers
+ * TotalSpinFull_* and tED): FP64 entries from the coefficients (interleaved
+ * re, im pairs for complex operators), overwritten (the reference adds into a
+ * zeroed matrix).  rows <= 65536.  H at mem; synchronous. */
+ed_status ed_op_write_dense(ed_op* op, double* H, int mem, void* stream);
+
 /* n_ops (1..8) fixed-step Lanczos runs in one persistent launch, for
  * operators that share their hopping tables (same sector and lattice terms;
  * the on-site terms, U and so the folded diagonals may differ): the

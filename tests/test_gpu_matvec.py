@@ -265,3 +265,25 @@ def test_lieb18_two_pass_lanczos_matches_generic(ed, monkeypatch):
         op.close()
         monkeypatch.delenv("ED_MATVEC", raising=False)
     assert runs["auto"] == runs["generic"]
+
+
+@pytest.mark.parametrize("case", ["chain8_35_disorder", "kagome12_22_flux", "chain8_44_U_dilute"])
+def test_write_dense_matches_oracle(ed, orc, case):
+    """Hubbard::Write: the dense matrix against the oracle's sparse
+    Hamiltonian (real, complex Peierls, U on a subset of sites)."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    if case == "chain8_35_disorder":
+        N, qu, qd, U, t, mask = 8, 3, 5, 2.0, L.chain(8, eps=list(philox_uniform(4, 8, 1.5))), None
+    elif case == "kagome12_22_flux":
+        N, qu, qd, U, t, mask = 12, 2, 2, 4.0, L.kagome12(flux=0.4), None
+    else:
+        N, qu, qd, U, t, mask = 8, 4, 4, 3.0, L.chain(8), 0b10110101
+    op = make_op(ed, N, qu, qd, t, t, U, dilution=mask)
+    H = op.Write()
+    ref = orc.hamiltonian(N, qu, qd, t, t, U, mask=mask).toarray()
+    assert H.shape == ref.shape
+    assert np.max(np.abs(H - ref)) < 1e-14 * max(1.0, np.max(np.abs(ref)))
+    x = philox_uniform(9, op.rows())
+    if op.is_complex:
+        x = x + 0j
+    assert np.max(np.abs(H @ x - op.matvec(x))) < 1e-12 * np.max(np.abs(ref)) * np.sqrt(op.rows())
