@@ -192,8 +192,10 @@ __global__ void __launch_bounds__(kLzThreads) k_lz_reorth(int64_t* __restrict__ 
 
 // evec = sum_k (rt_k q_k >> rs_k) * 2^-F as FP64, plus |evec|^2 partials.
 // A thread forms two adjacent elements from 16-byte loads of every slot
-// (slots are 256-byte aligned), four slots per iteration so that eight loads
-// are in flight; the basis is read once, at HBM rate.
+// (slots are 256-byte aligned), kRitzSlots slots per iteration with all their
+// loads issued before the sums; the basis is read once.
+constexpr int kRitzSlots = 16;
+
 __global__ void __launch_bounds__(kLzThreads) k_ritz(const int64_t* __restrict__ basis, int64_t n, int64_t stride,
                                                      int nk, const int64_t* __restrict__ rt,
                                                      const int* __restrict__ rs, int F, double* __restrict__ out,
@@ -206,15 +208,17 @@ __global__ void __launch_bounds__(kLzThreads) k_ritz(const int64_t* __restrict__
         const int64_t s2 = stride >> 1;
         i128 a0 = 0, a1 = 0;
         int k = 0;
-        for (; k + 4 <= nk; k += 4) {
-            const longlong2 v0 = __ldg(q + (k + 0) * s2), v1 = __ldg(q + (k + 1) * s2);
-            const longlong2 v2 = __ldg(q + (k + 2) * s2), v3 = __ldg(q + (k + 3) * s2);
-            const int64_t c0 = __ldg(rt + k), c1 = __ldg(rt + k + 1), c2 = __ldg(rt + k + 2), c3 = __ldg(rt + k + 3);
-            const int r0 = __ldg(rs + k), r1 = __ldg(rs + k + 1), r2 = __ldg(rs + k + 2), r3 = __ldg(rs + k + 3);
-            a0 += (mul_wide(c0, v0.x) >> r0) + (mul_wide(c1, v1.x) >> r1) + (mul_wide(c2, v2.x) >> r2) +
-                  (mul_wide(c3, v3.x) >> r3);
-            a1 += (mul_wide(c0, v0.y) >> r0) + (mul_wide(c1, v1.y) >> r1) + (mul_wide(c2, v2.y) >> r2) +
-                  (mul_wide(c3, v3.y) >> r3);
+        for (; k + kRitzSlots <= nk; k += kRitzSlots) {
+            longlong2 v[kRitzSlots];
+#pragma unroll
+            for (int t = 0; t < kRitzSlots; ++t) v[t] = __ldg(q + (k + t) * s2);
+#pragma unroll
+            for (int t = 0; t < kRitzSlots; ++t) {
+                const int64_t c = __ldg(rt + k + t);
+                const int r = __ldg(rs + k + t);
+                a0 += mul_wide(c, v[t].x) >> r;
+                a1 += mul_wide(c, v[t].y) >> r;
+            }
         }
         for (; k < nk; ++k) {
             const longlong2 v = __ldg(q + k * s2);
