@@ -19,6 +19,7 @@ STATUS_NAMES = {
 
 ED_TERM_HOP, ED_TERM_CURRENT, ED_TERM_DENSITY, ED_TERM_PEIERLS = 0, 1, 2, 3
 ED_OP_REAL, ED_OP_COMPLEX = 0, 1
+ED_MV_GENERIC, ED_MV_ROWS, ED_MV_TWO_PASS = 0, 1, 2
 ED_MEM_HOST, ED_MEM_DEVICE = 0, 1
 ED_LANCZOS_REFERENCE, ED_LANCZOS_FIXED = 0, 1
 ED_RITZ_NONE, ED_RITZ_STORED, ED_RITZ_RECOMPUTE = 0, 1, 2
@@ -112,6 +113,7 @@ SIGNATURES = {
     "ed_op_dim_up": (C.c_int64, [C.c_void_p]),
     "ed_op_dim_dn": (C.c_int64, [C.c_void_p]),
     "ed_op_is_complex": (C.c_int, [C.c_void_p]),
+    "ed_op_matvec_kind": (C.c_int, [C.c_void_p]),
     "ed_op_perform": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
     "ed_op_perform_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_lanczos_run": (C.c_int, [C.c_void_p, C.POINTER(ed_lanczos_cfg), C.c_void_p, C.c_int, C.c_void_p,

@@ -93,10 +93,15 @@ cudaError_t upload(T** dst, const T* src, size_t n) {
 
 // Plans and uploads the two-pass matvec when the down index's bandwidth
 // leaves a useful window in shared memory; leaves op->striped false otherwise.
+constexpr int kDegreeBlock = 256;  // columns reordered by hop count within each block
+
 static ed_status plan_striped(ed_op* op, bool forced) {
     std::vector<uint32_t> perm, inv;
     int64_t bw = 0;
     ed::rcm_order(op->tdn, &perm, &inv, &bw);
+    // lanes of a warp with similar hop counts: pass D's steps follow the
+    // largest count among a warp's columns
+    ed::sort_blocks_by_degree(op->tdn, kDegreeBlock, &perm, &inv, &bw);
     // window of chunk + 2 bw columns (+ alignment) in at most ~220 KB
     const int64_t max_win = 220 * 1024 / 8;
     int64_t chunk = (max_win - 2 * bw - 64) / 1024 * 1024;
@@ -105,9 +110,42 @@ static ed_status plan_striped(ed_op* op, bool forced) {
     if (chunk > dn_pad) chunk = dn_pad;
     if (chunk < 1024) return ED_OK;  // too wide: the generic kernel stays
     if (!forced && op->dimDN * 8 <= 160 * 1024) return ED_OK;
+    // Pass D's schedule: one step per hop of a column, at most two targets
+    // per bank pair in a step (a two-way conflict at worst), stored step by
+    // step as 16-bit offsets into the chunk's window | sign << 15.  A window
+    // starts on a multiple of 16 columns, so an offset keeps its column's
+    // residue mod 16; idle lanes of a step read one zero slot (a broadcast) at
+    // a residue no busy lane of their half-warp uses in that step, from the
+    // 16 zero slots [zbase, zbase + 16) past every window.
     ed::GatherSchedule32 g;
     std::string err;
-    if (!ed::build_gather_schedule32(op->tdn, perm, inv, &g, &err)) return ED_OK;
+    if (!ed::build_gather_schedule32(op->tdn, perm, inv, &g, &err, -1, 2)) return ED_OK;
+    const int64_t zbase = (chunk + 2 * bw + 16 + 15) / 16 * 16;
+    if (zbase + 16 > 32768) return ED_OK;
+    const int64_t cpad = g.count_pad, nsteps = std::max(g.steps, 1);
+    std::vector<uint16_t> s16((size_t)nsteps * cpad, 0);
+    for (int64_t cg = 0; cg < cpad; cg += 16) {
+        const int64_t k = cg / chunk;  // a chunk is a multiple of 1024 columns: one chunk per group
+        const int64_t w0 = std::max<int64_t>(0, k * chunk - bw) & ~(int64_t)15;
+        int64_t w1 = std::min<int64_t>(op->dimDN, (k + 1) * chunk + bw);
+        w1 = (w1 + 1) & ~(int64_t)1;
+        for (int64_t st = 0; st < nsteps; ++st) {
+            auto word = [&](int l) { return st < g.steps ? g.ent[(size_t)st * cpad + cg + l] : ed::kSched32None; };
+            uint32_t used = 0;
+            for (int l = 0; l < 16; ++l) {
+                const uint32_t e = word(l);
+                if (e == ed::kSched32None) continue;
+                const int64_t off = (int64_t)(e & 0x7FFFFFFFu) - w0;
+                if (off < 0 || off >= w1 - w0) return ED_OK;  // not within the chunk's window
+                used |= 1u << (off & 15);
+                s16[(size_t)st * cpad + cg + l] = (uint16_t)(off | ((e & 0x80000000u) ? 0x8000 : 0));
+            }
+            int z = 0;
+            while (z < 16 && ((used >> z) & 1u)) ++z;  // a step with an idle lane leaves a residue free
+            for (int l = 0; l < 16; ++l)
+                if (word(l) == ed::kSched32None) s16[(size_t)st * cpad + cg + l] = (uint16_t)(zbase + (z & 15));
+        }
+    }
     const int Fc = op->mv.Fc;
     std::vector<int64_t> dq((size_t)op->dimDN);
     std::vector<uint64_t> st((size_t)op->dimDN);
@@ -116,7 +154,7 @@ static ed_status plan_striped(ed_op* op, bool forced) {
         st[c] = op->bdn.state[perm[c]];
     }
     if (upload(&op->d_permDN, perm.data(), perm.size()) != cudaSuccess ||
-        upload(&op->d_sched32, g.ent.data(), g.ent.size()) != cudaSuccess ||
+        upload(&op->d_sched16, s16.data(), s16.size()) != cudaSuccess ||
         upload(&op->d_steps32, g.steps32.data(), g.steps32.size()) != cudaSuccess ||
         upload(&op->d_dDNqP, dq.data(), dq.size()) != cudaSuccess ||
         upload(&op->d_stDNp, st.data(), st.size()) != cudaSuccess)
@@ -127,8 +165,9 @@ static ed_status plan_striped(ed_op* op, bool forced) {
     op->st_grid = sms;
     op->st_bw = bw;
     op->st_chunk = (int)chunk;
-    op->st_win = (int)(chunk + 2 * bw + 32);
-    op->st_cpad = g.count_pad;
+    op->st_win = (int)(zbase + 16);
+    op->st_zbase = (int)zbase;
+    op->st_cpad = cpad;
     return ED_OK;
 }
 
@@ -485,7 +524,7 @@ ed_status ed_op_destroy(ed_op* op) {
     cudaFree(op->d_upPtr); cudaFree(op->d_upEntC); cudaFree(op->d_dnPtr); cudaFree(op->d_dnEntC);
     cudaFree(op->d_dnSched); cudaFree(op->d_dnSteps); cudaFree(op->d_rowStart); cudaFree(op->d_rowList); cudaFree(op->d_rowQueue);
     cudaFree(op->d_upSegE); cudaFree(op->d_upSegP); cudaFree(op->d_dnSegE); cudaFree(op->d_dnSegP);
-    cudaFree(op->d_permDN); cudaFree(op->d_sched32); cudaFree(op->d_steps32); cudaFree(op->d_dDNqP);
+    cudaFree(op->d_permDN); cudaFree(op->d_sched16); cudaFree(op->d_steps32); cudaFree(op->d_dDNqP);
     cudaFree(op->d_stDNp); cudaFree(op->d_sdn);
     cudaFree(op->d_err);
     cudaFree(op->d_dUPq); cudaFree(op->d_dDNq); cudaFree(op->d_stUP); cudaFree(op->d_stDN);
@@ -500,6 +539,11 @@ int64_t ed_op_cols(const ed_op* op) { return op ? op->D : 0; }
 int64_t ed_op_dim_up(const ed_op* op) { return op ? op->dimUP : 0; }
 int64_t ed_op_dim_dn(const ed_op* op) { return op ? op->dimDN : 0; }
 int ed_op_is_complex(const ed_op* op) { return op && op->cplx ? 1 : 0; }
+
+int ed_op_matvec_kind(const ed_op* op) {
+    if (!op) return -1;
+    return op->striped ? ED_MV_TWO_PASS : (op->tma_smem > 0 ? ED_MV_ROWS : ED_MV_GENERIC);
+}
 
 ed_status ed_op_perform(ed_op* op, const double* x, double* y, int mem, void* stream) {
     if (!op || !x || !y || (mem != ED_MEM_HOST && mem != ED_MEM_DEVICE)) return ED_ERR_ARG;

@@ -88,11 +88,12 @@ struct StripedArgs {
     const int64_t* xq;        // FX input, permuted order
     int64_t* sdn;             // int64 down sums (pass D out, pass U in / FP64 out)
     int64_t dimUP, dimDN;
-    const uint32_t* sched32;  // [steps][cpad] permuted column | sign, kSched32None idle
-    const uint8_t* steps32;
+    const uint16_t* sched16;  // [steps][cpad] offset in the chunk's window | sign << 15; idle: a zero slot
+    const uint8_t* steps32;   // steps the warp of 32-column block k runs
     int64_t cpad;
     int64_t bw;               // bandwidth of the permuted down index
     int chunk;                // columns per pass-D item
+    int zbase;                // first of the 16 zero slots after the window
     const int64_t* dDNq;      // folded down diagonal, permuted
     const uint64_t* stDN;     // down bitstrings, permuted
     int* err;
@@ -138,14 +139,14 @@ struct ed_op {
     int tma_grid = 0;
     // two-pass matvec (striped): down index permuted by perm (new -> old)
     bool striped = false;
-    int st_grid = 0, st_win = 0, st_chunk = 0;
+    int st_grid = 0, st_win = 0, st_chunk = 0, st_zbase = 0;
     // tuning (ed_op_autotune): Lanczos kernels 0 by the default rule, 1 per
     // step, 2 persistent; weight of the persistent kernel's row queue
     int lz_mode = 0;
     double row_cost = -1.0;
     int64_t st_bw = 0, st_cpad = 0;
     uint32_t* d_permDN = nullptr;
-    uint32_t* d_sched32 = nullptr;
+    uint16_t* d_sched16 = nullptr;
     uint8_t* d_steps32 = nullptr;
     int64_t* d_dDNqP = nullptr;
     uint64_t* d_stDNp = nullptr;

@@ -287,11 +287,13 @@ cudaError_t striped_args(ed_op* op, const int64_t* xq, StripedArgs* g) {
     g->sdn = op->d_sdn;
     g->dimUP = op->dimUP;
     g->dimDN = op->dimDN;
-    g->sched32 = op->d_sched32;
+    g->sched16 = op->d_sched16;
     g->steps32 = op->d_steps32;
     g->cpad = op->st_cpad;
     g->bw = op->st_bw;
     g->chunk = op->st_chunk;
+    g->zbase = op->st_zbase;
+
     g->dDNq = op->d_dDNqP;
     g->stDN = op->d_stDNp;
     g->err = op->d_err;

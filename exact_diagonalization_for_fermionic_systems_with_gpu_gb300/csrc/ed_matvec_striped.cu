@@ -10,8 +10,12 @@
 //   the CTA copies the window x[u, c0-B .. c0+C+B) of the row into shared
 //   memory with one bulk copy (consecutive chunks overlap, so most of it
 //   comes from L2) and every column of the chunk sums its down-hop entries
-//   from the window through a conflict-free gather schedule (32-bit words:
-//   permuted column | sign).  Output: the exact int64 down sums S_dn.
+//   from the window through a gather schedule (16-bit words: offset in the
+//   chunk's window | sign << 15; at most two targets per bank pair in a
+//   step, idle lanes on a zero slot; the columns are ordered by hop count
+//   within blocks of 256 so that a warp's lanes have similar step counts; the
+//   schedule is the same for every row and is read from L2, eight steps'
+//   words in flight per thread).  Output: the exact int64 down sums S_dn.
 // Pass U (k_mv_up): column stripes of kStripe columns, stripe-major over all
 //   rows so that the stripe of x (dim_up x kStripe x 8 B) stays in L2 while
 //   every row's up neighbours gather from it; a warp computes one row of a
@@ -37,6 +41,7 @@ using namespace dev;
 constexpr int kStripe = 64;        // columns of a pass-U stripe (32 lanes x 2)
 constexpr int kDownThreads = 1024;
 constexpr int kUpThreads = 1024;   // 32 warps: 32 rows of a stripe per item
+constexpr int kDownBatch = 8;      // pass-D schedule words loaded before their sums
 
 // ---------------------------------------------------------------- pass D --
 __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g) {
@@ -53,6 +58,7 @@ __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g
         tma::fence_mbar_init();
         give_up = 0;
     }
+    if (tid < 16) win[g.zbase + tid] = 0;  // never written by a window copy
     __syncthreads();
     uint32_t phase = 0;
     for (int64_t it = blockIdx.x; it < nitems; it += gridDim.x, phase ^= 1) {
@@ -75,15 +81,23 @@ __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g
         if (give_up) return;  // the copy this CTA waited for has given up; none other is in flight
         for (int64_t c = c0 + tid; c < c1; c += kDownThreads) {
             const int n = __ldg(g.steps32 + (c >> 5));
-            const uint32_t* sc = g.sched32 + c;
+            const uint16_t* sc = g.sched16 + c;
             int64_t acc = 0;
-#pragma unroll 4
-            for (int s = 0; s < n; ++s) {
-                const uint32_t e = __ldg(sc + (size_t)s * g.cpad);
-                if (e != kSched32None) {
-                    const int64_t v = win[(int64_t)(e & 0x7FFFFFFFu) - w0];
-                    acc += (e & 0x80000000u) ? -v : v;
+            int s = 0;
+            for (; s + kDownBatch <= n; s += kDownBatch) {
+                uint32_t e[kDownBatch];
+#pragma unroll
+                for (int t = 0; t < kDownBatch; ++t) e[t] = __ldg(sc + (size_t)(s + t) * g.cpad);
+#pragma unroll
+                for (int t = 0; t < kDownBatch; ++t) {
+                    const int64_t v = win[e[t] & 0x7FFFu];
+                    acc += (e[t] & 0x8000u) ? -v : v;
                 }
+            }
+            for (; s < n; ++s) {
+                const uint32_t e = __ldg(sc + (size_t)s * g.cpad);
+                const int64_t v = win[e & 0x7FFFu];
+                acc += (e & 0x8000u) ? -v : v;
             }
             g.sdn[u * dimDN + c] = acc;
         }

@@ -263,13 +263,15 @@ struct GroupEdge {
     uint32_t word;
 };
 
-// Proper edge colouring of one 16-column group (lanes x bank pairs) with as
-// many colours as the largest degree; pick[c * 16 + l] = edge of lane l in
-// colour c or -1, *free_banks[c] = bank pairs no edge of colour c uses.
+// Proper edge colouring of one 16-column group (lanes x nbanks banks,
+// nbanks <= 32) with as many colours as the largest degree;
+// pick[c * 16 + l] = edge of lane l in colour c or -1, *free_banks[c] = the
+// banks no edge of colour c uses (bit mask).
 bool colour_group(const std::vector<GroupEdge>& edges, int* Dout, std::vector<int>* pick,
-                  std::vector<int>* free_banks, std::string* err) {
-    constexpr int kL = 16, kB = 16;
-    int degL[kL] = {0}, degB[kB] = {0};
+                  std::vector<int>* free_banks, std::string* err, int nbanks = 16) {
+    constexpr int kL = 16;
+    const int kB = nbanks;
+    int degL[kL] = {0}, degB[32] = {0};
     for (const GroupEdge& e : edges) {
         ++degL[e.lane];
         ++degB[e.bank];
@@ -314,11 +316,11 @@ bool colour_group(const std::vector<GroupEdge>& edges, int* Dout, std::vector<in
     pick->assign((size_t)D * kL, -1);
     free_banks->assign(D, 0);
     for (int c = 0; c < D; ++c) {
-        int seen = 0;
+        uint32_t seen = 0;
         for (int l = 0; l < kL; ++l) {
             const int e = cL[(size_t)l * D + c];
             if (e < 0) continue;
-            const int bit = 1 << edges[e].bank;
+            const uint32_t bit = 1u << edges[e].bank;
             if (seen & bit || color[e] != c) {
                 if (err) *err = "gather schedule: colouring check failed";
                 return false;
@@ -326,7 +328,7 @@ bool colour_group(const std::vector<GroupEdge>& edges, int* Dout, std::vector<in
             seen |= bit;
             (*pick)[(size_t)c * kL + l] = e;
         }
-        (*free_banks)[c] = ~seen & 0xFFFF;
+        (*free_banks)[c] = (int)(~seen & (kB == 32 ? 0xFFFFFFFFu : ((1u << kB) - 1u)));
     }
     for (int e = 0; e < (int)edges.size(); ++e)
         if (color[e] < 0) {
@@ -496,8 +498,23 @@ void rcm_order(const SpinTable& t, std::vector<uint32_t>* perm, std::vector<uint
     *bandwidth = bw;
 }
 
+void sort_blocks_by_degree(const SpinTable& t, int block, std::vector<uint32_t>* perm, std::vector<uint32_t>* inv,
+                           int64_t* bandwidth) {
+    for (size_t s = 0; s < perm->size(); s += (size_t)block) {
+        const size_t e = std::min(perm->size(), s + (size_t)block);
+        std::stable_sort(perm->begin() + s, perm->begin() + e,
+                         [&](uint32_t a, uint32_t b) { return t.len[a] > t.len[b]; });
+    }
+    for (size_t k = 0; k < perm->size(); ++k) (*inv)[(*perm)[k]] = (uint32_t)k;
+    int64_t bw = 0;
+    for (int64_t a = 0; a < t.count; ++a)
+        for (int k = 0; k < t.len[a]; ++k)
+            bw = std::max<int64_t>(bw, std::llabs((int64_t)(*inv)[a] - (int64_t)(*inv)[t.ent[(size_t)k * t.count + a] & kColMask]));
+    *bandwidth = bw;
+}
+
 bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
-                             GatherSchedule32* g, std::string* err) {
+                             GatherSchedule32* g, std::string* err, int sign_filter, int bank_cap) {
     if (t.complex_coef || t.coef.size() > 1) {
         if (err) *err = "gather schedule: needs a real single-class table";
         return false;
@@ -511,19 +528,25 @@ bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& pe
     int smax = 0;
     for (int64_t gi = 0; gi < ngroups; ++gi) {
         std::vector<GroupEdge> edges;
+        int seen_res[16] = {0};
         for (int l = 0; l < kL; ++l) {
             const int64_t c = gi * 16 + l;  // permuted column
             if (c >= count) continue;
             const int64_t d = perm[c];      // its state in table order
             for (int k = 0; k < t.len[d]; ++k) {
                 const uint32_t e = t.ent[(size_t)k * count + d];
+                if (sign_filter >= 0 && ((e & kSignBit) != 0) != (sign_filter == 1)) continue;
                 const uint32_t tc = inv[e & kColMask];
-                edges.push_back({l, (int)(tc % 16), tc | (e & kSignBit)});
+                // bank_cap 2: the targets of a residue alternate between two
+                // virtual banks, so a step holds at most two of them
+                const int r = (int)(tc % 16);
+                const int bank = bank_cap == 2 ? 2 * r + (seen_res[r]++ & 1) : r;
+                edges.push_back({l, bank, tc | (e & kSignBit)});
             }
         }
         int D = 0;
         std::vector<int> pick, freeb;
-        if (!colour_group(edges, &D, &pick, &freeb, err)) return false;
+        if (!colour_group(edges, &D, &pick, &freeb, err, bank_cap == 2 ? 32 : 16)) return false;
         std::vector<uint32_t> words((size_t)D * kL, kSched32None);
         for (int c = 0; c < D; ++c)
             for (int l = 0; l < kL; ++l) {

@@ -110,6 +110,12 @@ bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* e
 // the hops of a state stay within +-bandwidth of it.
 void rcm_order(const SpinTable& t, std::vector<uint32_t>* perm, std::vector<uint32_t>* inv, int64_t* bandwidth);
 
+// Reorders each aligned block of `block` consecutive entries of perm by
+// decreasing row length (stable), so that the lanes of a warp have similar
+// entry counts; updates inv and the bandwidth (which grows by < block).
+void sort_blocks_by_degree(const SpinTable& t, int block, std::vector<uint32_t>* perm, std::vector<uint32_t>* inv,
+                           int64_t* bandwidth);
+
 // Conflict-free gather schedule over permuted columns for the two-pass
 // matvec: column c' = inv[d] of the permuted table reads its entries
 // (targets inv[col]) one per step, 32-bit words col' | sign << 31, idle
@@ -124,8 +130,11 @@ struct GatherSchedule32 {
     std::vector<uint8_t> steps32;  // steps the warp of 32-column block k runs
 };
 
+// sign_filter: -1 every entry, 0 only the + entries, 1 only the - entries.
+// bank_cap: 1 conflict-free steps; 2 at most two targets per bank pair in a
+// step (a two-way conflict), which lets a step carry more lanes.
 bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
-                             GatherSchedule32* g, std::string* err);
+                             GatherSchedule32* g, std::string* err, int sign_filter = -1, int bank_cap = 1);
 
 // Build both layouts for one spin from a term list.  Returns ED_OK or an
 // error (bad site, table overflow, complex term in a real operator when

@@ -176,6 +176,7 @@ class Hubbard:
         self.dimUP = int(lib.ed_op_dim_up(h))
         self.dimDN = int(lib.ed_op_dim_dn(h))
         self.is_complex = bool(lib.ed_op_is_complex(h))
+        self.matvec_kind = ("generic", "rows", "two_pass")[lib.ed_op_matvec_kind(h)]
 
     # -- Spectra concept (TotalSpin/include/HubMatrix_TotalSpin.cuh:279-311) --
     def rows(self) -> int:

@@ -12,7 +12,9 @@ Cases: kagome12 (6+6, dim 853,776, L2-resident vectors), kagome12_flux
 (complex, Peierls phases), chain12_66 / chain12_75 / chain12_84 (open L=12
 chain, W=6 disorder, the three sectors of the MBL sweep), chain14 (7+7 open
 chain with disorder, dim 11,778,624, vectors larger than L2), lieb18 (9+9,
-dim 2.36e9, ~100 GB of device memory for a Lanczos run).
+dim 2.36e9, ~100 GB of device memory for a Lanczos run), lieb18_49 (4+9:
+Lieb18's down rows under 3,060 up rows, dim 1.49e8, for profiling the
+two-pass matvec on a small case).
 """
 from __future__ import annotations
 
@@ -38,6 +40,9 @@ def build_case(name: str):
     if name == "lieb18":
         t = L.lieb18()
         return Hubbard(H_TBq(18, 9).extend(t), H_TBq(18, 9).extend(t), 4.0)
+    if name == "lieb18_49":  # Lieb18's down rows (48,620 columns) under 3,060 up rows: 1.2 GB vectors
+        t = L.lieb18()
+        return Hubbard(H_TBq(18, 4).extend(t), H_TBq(18, 9).extend(t), 4.0)
     if name == "kagome12_flux":
         t = L.kagome12(flux=0.3)
         return Hubbard(H_TBq(12, 6).extend(t), H_TBq(12, 6).extend(t), 4.0)

@@ -133,6 +133,14 @@ int64_t ed_op_dim_up(const ed_op* op);
 int64_t ed_op_dim_dn(const ed_op* op);
 int ed_op_is_complex(const ed_op* op);
 
+/* The matvec kernel of the operator's Lanczos steps: ED_MV_GENERIC (one
+ * thread per element), ED_MV_ROWS (rows staged in shared memory by bulk
+ * copies) or ED_MV_TWO_PASS (down sums over a bandwidth-reduced down index,
+ * then the up term over L2-resident column stripes); -1 for a null op.
+ * Chosen at ed_op_create from the sector's shape (ED_MATVEC overrides). */
+enum { ED_MV_GENERIC = 0, ED_MV_ROWS = 1, ED_MV_TWO_PASS = 2 };
+int ed_op_matvec_kind(const ed_op* op);
+
 /* y = H x.  mem = ED_MEM_HOST: x, y are host pointers and the call is
  * synchronous — the cuSpectra::Hubbard::perform_op semantics
  * (HubMatrix_TotalSpin.cuh:282-311).  mem = ED_MEM_DEVICE: device pointers,

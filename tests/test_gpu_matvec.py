@@ -195,6 +195,11 @@ def test_matvec_kernels_agree_bit_for_bit(ed, monkeypatch, case):
         ops[kind] = make_op(ed, N, qu, qd, ut, dt, U)
         for k in env:
             monkeypatch.delenv(k, raising=False)
+    # the two-pass kernel takes real single-class operators with an even
+    # down dimension; the others fall through
+    if not ops["auto"].is_complex and "classes" not in name and ops["auto"].dimDN % 2 == 0:
+        assert ops["striped"].matvec_kind == "two_pass", name
+    assert ops["generic"].matvec_kind == "generic"
     rng = np.random.default_rng(11)
     n = ops["auto"].rows()
     cplx = ops["auto"].is_complex
@@ -259,6 +264,7 @@ def test_lieb18_two_pass_lanczos_matches_generic(ed, monkeypatch):
         if kind:
             monkeypatch.setenv("ED_MATVEC", kind)
         op = make_op(ed, 18, 9, 9, t, t, 4.0)
+        assert op.matvec_kind == (kind or "two_pass")
         lz = ed.Lanczos()
         lz.eigen(op, max_steps=4, mode="fixed", ritz="none", seed=1)
         runs[kind or "auto"] = (lz.a, lz.b)
