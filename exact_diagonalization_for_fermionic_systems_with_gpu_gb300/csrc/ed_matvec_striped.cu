@@ -19,7 +19,7 @@
 // Pass U (k_mv_up): column stripes of kStripe columns, stripe-major over all
 //   rows so that the stripe of x (dim_up x kStripe x 8 B) stays in L2 while
 //   every row's up neighbours gather from it; a warp computes one row of a
-//   stripe (2 columns per lane, 16-byte loads), adds S_dn and the diagonal,
+//   stripe (two column pairs per lane, 16-byte loads), adds S_dn and the diagonal,
 //   rounds once, and writes u (FX, Lanczos) or y (FP64, permuted order; the
 //   operator apply keeps the table-order kernels).
 // HBM traffic per matvec: pass D reads x and writes S_dn, pass U reads x,
@@ -38,9 +38,9 @@
 namespace ed {
 using namespace dev;
 
-constexpr int kStripe = 64;        // columns of a pass-U stripe (32 lanes x 2)
+constexpr int kStripe = 128;       // columns of a pass-U stripe (32 lanes x 4)
 constexpr int kDownThreads = 1024;
-constexpr int kUpThreads = 1024;   // 32 warps: 32 rows of a stripe per item
+constexpr int kUpThreads = 768;    // 24 warps (80 registers a thread): 24 rows of a stripe per item
 constexpr int kDownBatch = 8;      // pass-D schedule words loaded before their sums
 
 // ---------------------------------------------------------------- pass D --
@@ -107,10 +107,15 @@ __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g
 
 // ---------------------------------------------------------------- pass U --
 // Column-stripe-major items: item = stripe * dim_up + row, one warp each;
-// warp w of CTA b takes items b * 32 + w, + 32 * gridDim.x, ...
+// warp w of CTA b takes items b * 24 + w, + 24 * gridDim.x, ...  A lane
+// holds two column pairs 64 columns apart (c, c + 1 and c + 64, c + 65), so
+// each 16-byte load instruction of the warp reads one contiguous 512-byte
+// segment; the second pair is absent past the end of the row.  Row offsets
+// are 32-bit element offsets (a vector has < 2^32 elements).
 template <int OUT>
 __global__ void __launch_bounds__(kUpThreads, 1) k_mv_up(const MvArgs a, const StripedArgs g) {
     const int64_t dimUP = g.dimUP, dimDN = g.dimDN;
+    const uint32_t dn32 = (uint32_t)dimDN;
     const int64_t nstripe = (dimDN + kStripe - 1) / kStripe;
     const int64_t nitems = nstripe * dimUP;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -130,61 +135,83 @@ __global__ void __launch_bounds__(kUpThreads, 1) k_mv_up(const MvArgs a, const S
     uint64_t mx = 0;
     for (int64_t it = (int64_t)blockIdx.x * (kUpThreads / 32) + warp; it < nitems; it += nwarps) {
         const int64_t st = it / dimUP, u = it - st * dimUP;
-        const int64_t c = st * kStripe + lane * 2;  // dim_dn is even: both columns exist
-        if (c >= dimDN) continue;
+        const uint32_t c = (uint32_t)(st * kStripe) + 2u * (uint32_t)lane;  // dim_dn is even
+        if (c >= dn32) continue;
+        const bool two = c + 64u < dn32;  // the second pair of columns exists
+        const uint32_t rowu = (uint32_t)u * dn32 + c;
         // the row's own values and down sums first: their HBM latency overlaps the gathers
-        const longlong2 dsv = __ldcs(reinterpret_cast<const longlong2*>(g.sdn + u * dimDN + c));
-        const longlong2 xs = __ldcg(reinterpret_cast<const longlong2*>(xq + u * dimDN + c));
+        longlong2 dsv[2], xs[2];
+        dsv[0] = __ldcs(reinterpret_cast<const longlong2*>(g.sdn + rowu));
+        xs[0] = __ldcg(reinterpret_cast<const longlong2*>(xq + rowu));
+        if (two) {
+            dsv[1] = __ldcs(reinterpret_cast<const longlong2*>(g.sdn + rowu + 64u));
+            xs[1] = __ldcg(reinterpret_cast<const longlong2*>(xq + rowu + 64u));
+        } else {
+            dsv[1] = make_longlong2(0, 0);
+            xs[1] = dsv[1];
+        }
         const uint32_t p0 = __ldg(a.upPtr + u), len = __ldg(a.upPtr + u + 1) - p0;
         const int npos = (int)__ldg(a.upNpos + u);
-        int64_t sp0 = 0, sp1 = 0, sn0 = 0, sn1 = 0;
+        int64_t sp[4] = {0, 0, 0, 0};  // + neighbours added, - neighbours subtracted
         int k = 0;
 #pragma unroll 4
         for (; k < npos; ++k) {
-            const int64_t j = __ldg(a.upEntC + p0 + k) & kColMask;
-            const longlong2 v = __ldcg(reinterpret_cast<const longlong2*>(xq + j * dimDN + c));
-            sp0 += v.x;
-            sp1 += v.y;
+            const uint32_t o = (__ldg(a.upEntC + p0 + k) & kColMask) * dn32 + c;
+            const longlong2 v0 = __ldcg(reinterpret_cast<const longlong2*>(xq + o));
+            const longlong2 v1 = two ? __ldcg(reinterpret_cast<const longlong2*>(xq + o + 64u)) : make_longlong2(0, 0);
+            sp[0] += v0.x;
+            sp[1] += v0.y;
+            sp[2] += v1.x;
+            sp[3] += v1.y;
         }
 #pragma unroll 4
         for (; k < (int)len; ++k) {
-            const int64_t j = __ldg(a.upEntC + p0 + k) & kColMask;
-            const longlong2 v = __ldcg(reinterpret_cast<const longlong2*>(xq + j * dimDN + c));
-            sn0 += v.x;
-            sn1 += v.y;
+            const uint32_t o = (__ldg(a.upEntC + p0 + k) & kColMask) * dn32 + c;
+            const longlong2 v0 = __ldcg(reinterpret_cast<const longlong2*>(xq + o));
+            const longlong2 v1 = two ? __ldcg(reinterpret_cast<const longlong2*>(xq + o + 64u)) : make_longlong2(0, 0);
+            sp[0] -= v0.x;
+            sp[1] -= v0.y;
+            sp[2] -= v1.x;
+            sp[3] -= v1.y;
         }
         const uint64_t stu = __ldg(a.stUP + u);
         const int64_t du = __ldg(a.dUPq + u);
-        int64_t oq[2];
-        double of[2];
+        // the two column pairs one after the other, each stored at once
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            const int64_t up_sum = q ? sp1 - sn1 : sp0 - sn0;
-            const int64_t dn_sum = q ? dsv.y : dsv.x;
-            const int64_t xv = q ? xs.y : xs.x;
-            i128 ar = 0, ai = 0;
-            if (merge) {
-                apply_class<false>(ar, ai, up_sum + dn_sum, 0, a.coefUP, 0, unitU, a.Fc);
-            } else {
-                if (len) apply_class<false>(ar, ai, up_sum, 0, a.coefUP, 0, unitU, a.Fc);
-                if (a.nclsDN) apply_class<false>(ar, ai, dn_sum, 0, a.coefDN, 0, unitD, a.Fc);
+        for (int h = 0; h < 2; ++h) {
+            if (h == 1 && !two) break;
+            int64_t oq[2];
+            double of[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int q = 2 * h + e;
+                const int64_t dn_sum = e ? dsv[h].y : dsv[h].x;
+                const int64_t xv = e ? xs[h].y : xs[h].x;
+                i128 ar = 0, ai = 0;
+                if (merge) {
+                    apply_class<false>(ar, ai, sp[q] + dn_sum, 0, a.coefUP, 0, unitU, a.Fc);
+                } else {
+                    if (len) apply_class<false>(ar, ai, sp[q], 0, a.coefUP, 0, unitU, a.Fc);
+                    if (a.nclsDN) apply_class<false>(ar, ai, dn_sum, 0, a.coefDN, 0, unitD, a.Fc);
+                }
+                const uint32_t cq = c + 64u * h + e;
+                const int64_t dq = du + __ldg(g.dDNq + cq) + a.Uq * (int64_t)__popcll(stu & __ldg(g.stDN + cq) & a.mask);
+                ar += mul_wide(dq, xv);
+                if (OUT == 0) {
+                    of[e] = i128_to_f64(ar, E_out);
+                } else {
+                    oq[e] = shr_round_i64(ar, s_u);
+                    dot += mul_wide(xv, oq[e]) >> 24;
+                    const uint64_t aq = (uint64_t)(oq[e] < 0 ? -oq[e] : oq[e]);
+                    mx = aq > mx ? aq : mx;
+                }
             }
-            const int64_t dq = du + __ldg(g.dDNq + c + q) + a.Uq * (int64_t)__popcll(stu & __ldg(g.stDN + c + q) & a.mask);
-            ar += mul_wide(dq, xv);
             if (OUT == 0) {
-                of[q] = i128_to_f64(ar, E_out);
+                // the FP64 result overwrites S_dn in place (permuted order)
+                *reinterpret_cast<double2*>(g.sdn + rowu + 64u * h) = make_double2(of[0], of[1]);
             } else {
-                oq[q] = shr_round_i64(ar, s_u);
-                dot += mul_wide(xv, oq[q]) >> 24;
-                const uint64_t aq = (uint64_t)(oq[q] < 0 ? -oq[q] : oq[q]);
-                mx = aq > mx ? aq : mx;
+                __stcs(reinterpret_cast<longlong2*>(a.uq + rowu + 64u * h), make_longlong2(oq[0], oq[1]));
             }
-        }
-        if (OUT == 0) {
-            // the FP64 result overwrites S_dn in place (permuted order)
-            *reinterpret_cast<double2*>(g.sdn + u * dimDN + c) = make_double2(of[0], of[1]);
-        } else {
-            __stcs(reinterpret_cast<longlong2*>(a.uq + u * dimDN + c), make_longlong2(oq[0], oq[1]));
         }
     }
     if (OUT == 1) mv_lanczos_epilogue(a, dot, mx, s_u);
