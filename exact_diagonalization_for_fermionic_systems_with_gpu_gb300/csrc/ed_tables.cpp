@@ -341,7 +341,7 @@ bool colour_group(const std::vector<GroupEdge>& edges, int* Dout, std::vector<in
 
 }  // namespace
 
-bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* err) {
+bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* err, int bank_cap) {
     if (t.complex_coef || t.coef.size() > 1) {
         if (err) *err = "gather schedule: needs a real single-class table";
         return false;
@@ -361,22 +361,34 @@ bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* e
     int smax = 0;
     for (int64_t gi = 0; gi < ngroups; ++gi) {
         std::vector<GroupEdge> edges;
+        int seen_res[16] = {0};
         for (int l = 0; l < kL; ++l) {
             const int64_t d = gi * 16 + l;
             if (d >= count) continue;
             for (int k = 0; k < t.len[d]; ++k) {
                 const uint32_t e = t.ent[(size_t)k * count + d];
                 const uint32_t col = e & kColMask;
-                edges.push_back({l, (int)(col % 16), (uint32_t)(col + ((e & kSignBit) ? neg_base : 0))});
+                // bank_cap 2: a residue's targets alternate between two
+                // virtual banks, so a step holds at most two of them
+                const int r = (int)(col % 16);
+                const int bank = bank_cap == 2 ? 2 * r + (seen_res[r]++ & 1) : r;
+                edges.push_back({l, bank, (uint32_t)(col + ((e & kSignBit) ? neg_base : 0))});
             }
         }
         int D = 0;
         std::vector<int> pick, freeb;
-        if (!colour_group(edges, &D, &pick, &freeb, err)) return false;
-        // idle lanes take the zeros of the bank pairs left free
+        if (!colour_group(edges, &D, &pick, &freeb, err, bank_cap == 2 ? 32 : 16)) return false;
+        // idle lanes take the zeros of the bank pairs left free (a step with
+        // k idle lanes has at most 16 - k busy lanes, so k residues are free)
         std::vector<uint16_t> words((size_t)D * kL, 0);
         for (int c = 0; c < D; ++c) {
             int fb = freeb[c];
+            if (bank_cap == 2) {
+                int fr = 0;
+                for (int r = 0; r < 16; ++r)
+                    if (((freeb[c] >> (2 * r)) & 3) == 3) fr |= 1 << r;
+                fb = fr;
+            }
             for (int l = 0; l < kL; ++l) {
                 const int e = pick[(size_t)c * kL + l];
                 if (e >= 0) {

@@ -101,7 +101,8 @@ struct GatherSchedule {
 
 // False (with *err) when the table is not eligible: complex or several
 // classes, more than kSchedMaxCount states, or more than 255 steps.
-bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* err);
+// bank_cap as in build_gather_schedule32.
+bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* err, int bank_cap = 1);
 
 // Reverse Cuthill-McKee order of a table's hop graph (breadth-first from a
 // pseudo-peripheral state, neighbours by increasing degree, reversed; every
