@@ -141,6 +141,8 @@ SIGNATURES = {
                               C.c_void_p, C.c_void_p]),
     "ed_entanglement_entropy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),
+    "ed_entanglement_entropy_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_uint64, C.c_void_p,
+                                                C.c_void_p, C.c_void_p]),
     "ed_tridiag_eigen": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_bidiag_singular_values": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_tridiag_expm": (C.c_int, [C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]),

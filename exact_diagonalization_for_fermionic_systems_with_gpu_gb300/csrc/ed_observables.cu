@@ -265,9 +265,14 @@ struct EePool {
     std::vector<EeWorker> w;
 };
 
+// One worker by default: with several concurrent workers the gesvd results
+// differed (1e-9 .. 3e-6 in the entropy) in rare runs after earlier calls
+// had used the pool, a cause not found; the cluster bidiagonalisation takes
+// every block of the sectors run here, so this path is a fallback.
+// ED_EE_STREAMS=k (<= 32) sets k workers.
 int ee_workers() {
     const char* e = std::getenv("ED_EE_STREAMS");
-    const int k = e ? std::atoi(e) : 8;
+    const int k = e ? std::atoi(e) : 1;
     return std::max(1, std::min(k, 32));
 }
 
@@ -741,9 +746,14 @@ ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double
     return st;
 }
 
-ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_t a_mask, double* s_vn, double* s_ref,
-                                  void* stream) {
-    if (!op || !psi) return ED_ERR_ARG;
+// The entropies of n_states states of op's sector (psi: n_states x rows,
+// row-major): every state's blocks go through the same bidiagonalisation
+// launches and host SVD pool, so a batch fills the GPU where one state's
+// blocks leave SMs idle.  Each state's result equals its own one-state call
+// bit for bit (the same blocks, cluster sizes and summation order).
+static ed_status ee_states(ed_op* op, int n_states, const double* psi, int mem, uint64_t a_mask, double* s_vn,
+                           double* s_ref, void* stream) {
+    if (!op || !psi || n_states < 1) return ED_ERR_ARG;
     if (op->cplx) return ED_ERR_NOT_BUILT;
     const int N = op->n_sites;
     const uint64_t all = (N >= 64) ? ~0ULL : ((1ULL << N) - 1ULL);
@@ -770,8 +780,9 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
     labels(op->bup, &nau, &iau, &ibu);
     labels(op->bdn, &nad, &iad, &ibd);
     const int nqu = std::min(Qu, nA) + 1, nqd = std::min(Qd, nA) + 1;
-    std::vector<int64_t> off(nqu * nqd, 0);
-    std::vector<int32_t> rA(nqu * nqd, 0), cB(nqu * nqd, 0), dimA_dn(nqd), dimB_dn(nqd);
+    const int nblk = nqu * nqd;
+    std::vector<int64_t> off(nblk, 0);
+    std::vector<int32_t> rA(nblk, 0), cB(nblk, 0), dimA_dn(nqd), dimB_dn(nqd);
     int64_t total = 0;
     for (int kd = 0; kd < nqd; ++kd) {
         dimA_dn[kd] = (int32_t)binom_i(nA, kd);
@@ -788,7 +799,7 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
     // device copies
     const double* dpsi;
     double* owned;
-    ed_status st = to_device(psi, op->D, mem, &dpsi, &owned, s);
+    ed_status st = to_device(psi, op->D * n_states, mem, &dpsi, &owned, s);
     if (st != ED_OK) return st;
     std::vector<int32_t> meta_i;
     auto push = [&](const std::vector<int32_t>& v) { meta_i.insert(meta_i.end(), v.begin(), v.end()); };
@@ -796,16 +807,17 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
     int32_t* dmi = nullptr;
     int64_t* doff = nullptr;
     double* blocks = nullptr;
+    const int64_t nall = std::max<int64_t>(total * n_states, 1);
     if (cudaMalloc(&dmi, sizeof(int32_t) * meta_i.size()) != cudaSuccess ||
         cudaMalloc(&doff, sizeof(int64_t) * off.size()) != cudaSuccess ||
-        cudaMalloc(&blocks, sizeof(double) * std::max<int64_t>(total, 1)) != cudaSuccess) {
+        cudaMalloc(&blocks, sizeof(double) * nall) != cudaSuccess) {
         cudaFree(dmi); cudaFree(doff);
         if (owned) cudaFreeAsync(owned, s);
         return ED_ERR_ALLOC;
     }
     cudaMemcpyAsync(dmi, meta_i.data(), sizeof(int32_t) * meta_i.size(), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice, s);
-    cudaMemsetAsync(blocks, 0, sizeof(double) * std::max<int64_t>(total, 1), s);
+    cudaMemsetAsync(blocks, 0, sizeof(double) * nall, s);
     ed::EeMeta m;
     size_t p = 0;
     m.nA_up = dmi + p; p += nau.size();
@@ -820,40 +832,47 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
     m.dimB_dn = dmi + p; p += dimB_dn.size();
     m.blk_off = doff;
     m.nqd = nqd;
-    ed::k_ee_scatter<<<ob_grid(op->D), kObThreads, 0, s>>>(dpsi, op->dimUP, op->dimDN, m, blocks);
-    // singular values of every block; cusolverDnDgesvd (jobu = jobvt = 'N',
-    // as entangle_entropy.h:231-291) on the device's worker streams for the
-    // blocks the cluster bidiagonalisation does not take
-    std::vector<int> mmv(off.size()), nnv(off.size());
-    std::vector<int64_t> svo(off.size() + 1, 0);
-    for (size_t k = 0; k < off.size(); ++k) {
-        mmv[k] = std::max(rA[k], cB[k]);
-        nnv[k] = std::min(rA[k], cB[k]);
+    for (int b = 0; b < n_states; ++b)
+        ed::k_ee_scatter<<<ob_grid(op->D), kObThreads, 0, s>>>(dpsi + (size_t)b * op->D, op->dimUP, op->dimDN, m,
+                                                               blocks + (size_t)b * total);
+    // every state's blocks in one list: singular values of every block;
+    // cusolverDnDgesvd (jobu = jobvt = 'N', as entangle_entropy.h:231-291) on
+    // the device's worker streams for the blocks the cluster
+    // bidiagonalisation does not take
+    const size_t nk = (size_t)nblk * n_states;
+    std::vector<int64_t> offs(nk);
+    std::vector<int> mmv(nk), nnv(nk);
+    std::vector<int64_t> svo(nk + 1, 0);
+    for (size_t k = 0; k < nk; ++k) {
+        const size_t kb = k % nblk, b = k / nblk;
+        offs[k] = off[kb] + (int64_t)b * total;
+        mmv[k] = std::max(rA[kb], cB[kb]);
+        nnv[k] = std::min(rA[kb], cB[kb]);
         svo[k + 1] = svo[k] + nnv[k];
     }
     // blocks that fit a thread-block cluster: Householder bidiagonalisation
     // on the device + bidiagonal SVD on the host; the rest through cuSOLVER
     std::vector<double> hs(std::max<int64_t>(svo.back(), 1), 0.0);
     std::vector<char> done;
-    if (st == ED_OK) st = ed::ee_bidiag_blocks(op->device, s, blocks, off, mmv, nnv, svo, &hs, &done);
+    if (st == ED_OK) st = ed::ee_bidiag_blocks(op->device, s, blocks, offs, mmv, nnv, svo, &hs, &done);
     bool rest = false;
-    for (size_t k = 0; k < off.size(); ++k) rest = rest || (!done.empty() && !done[k] && nnv[k] > 0);
+    for (size_t k = 0; k < nk; ++k) rest = rest || (!done.empty() && !done[k] && nnv[k] > 0);
     double* sv_all = nullptr;
     if (st == ED_OK && rest) {
         if (cudaMalloc(&sv_all, sizeof(double) * std::max<int64_t>(svo.back(), 1)) != cudaSuccess) st = ED_ERR_ALLOC;
-        if (st == ED_OK) st = ee_block_svd(op->device, s, blocks, off, mmv, nnv, svo, sv_all, done);
+        if (st == ED_OK) st = ee_block_svd(op->device, s, blocks, offs, mmv, nnv, svo, sv_all, done);
         std::vector<double> hg(std::max<int64_t>(svo.back(), 1));
         if (st == ED_OK &&
             (cudaMemcpyAsync(hg.data(), sv_all, sizeof(double) * svo.back(), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
              cudaStreamSynchronize(s) != cudaSuccess))
             st = ED_ERR_CUDA;
-        for (size_t k = 0; st == ED_OK && k < off.size(); ++k)
+        for (size_t k = 0; st == ED_OK && k < nk; ++k)
             if (!done[k]) std::copy(hg.begin() + svo[k], hg.begin() + svo[k + 1], hs.begin() + svo[k]);
     }
-    double svn = 0.0, sref = 0.0;
-    if (st == ED_OK) {
+    for (int b = 0; st == ED_OK && b < n_states; ++b) {
+        double svn = 0.0, sref = 0.0;
         // block by block, each in descending order: a fixed summation order
-        for (int64_t i = 0; st == ED_OK && i < svo.back(); ++i) {
+        for (int64_t i = svo[(size_t)b * nblk]; i < svo[(size_t)(b + 1) * nblk]; ++i) {
             const double x = hs[i];
             if (x > 0.0) {
                 sref += -x * std::log(x);
@@ -861,16 +880,24 @@ ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_
                 if (q > 0.0) svn += -q * std::log(q);
             }
         }
+        if (s_vn) s_vn[b] = svn;
+        if (s_ref) s_ref[b] = sref;
     }
     cudaFree(sv_all);
     cudaFree(blocks); cudaFree(dmi); cudaFree(doff);
     if (owned) cudaFreeAsync(owned, s);
     cudaStreamSynchronize(s);
-    if (st == ED_OK) {
-        if (s_vn) *s_vn = svn;
-        if (s_ref) *s_ref = sref;
-    }
     return st;
+}
+
+ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_t a_mask, double* s_vn, double* s_ref,
+                                  void* stream) {
+    return ee_states(op, 1, psi, mem, a_mask, s_vn, s_ref, stream);
+}
+
+ed_status ed_entanglement_entropy_batch(ed_op* op, int n_states, const double* psis, int mem, uint64_t a_mask,
+                                        double* s_vn, double* s_ref, void* stream) {
+    return ee_states(op, n_states, psis, mem, a_mask, s_vn, s_ref, stream);
 }
 
 }  // extern "C"

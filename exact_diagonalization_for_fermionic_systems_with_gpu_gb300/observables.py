@@ -109,6 +109,27 @@ def entanglement_entropy(op: Hubbard, psi, a_sites: Sequence[int]):
     return svn.value, sref.value
 
 
+def entanglement_entropy_batch(op: Hubbard, psis, a_sites: Sequence[int]):
+    """(S_vN[n], S_ref[n]) of the n states psis[b] (a (n, rows) float64 CUDA
+    tensor or numpy array) of op's sector, in one batched call."""
+    mask = 0
+    for s in a_sites:
+        mask |= 1 << int(s)
+    if isinstance(psis, np.ndarray):
+        a = np.ascontiguousarray(psis, dtype=np.float64)
+        n, ptr, mem = a.shape[0], C.c_void_p(a.ctypes.data), _capi.ED_MEM_HOST
+    else:
+        a = psis.contiguous()
+        n, ptr, mem = a.shape[0], C.c_void_p(a.data_ptr()), _capi.ED_MEM_DEVICE
+    if a.shape[1] != op.rows():
+        raise ValueError("psis must be (n_states, rows)")
+    svn, sref = np.zeros(n), np.zeros(n)
+    check(_capi.load().ed_entanglement_entropy_batch(op.handle, int(n), ptr, mem, mask,
+                                                     C.c_void_p(svn.ctypes.data), C.c_void_p(sref.ctypes.data), None),
+          "ed_entanglement_entropy_batch")
+    return svn, sref
+
+
 def s2_apply(op: Hubbard, x):
     """y = S_xy x, S_xy = (S+S- + S-S+)/2 (TotalSpin::Hubbard::Hubbard_mv):
     a numpy array in gives a numpy array out, a CUDA tensor a CUDA tensor

@@ -205,10 +205,11 @@ def _mbl_batched(reals, sectors, n_sites, W, U, steps, seed, a_sites, batch, t) 
                     e0s.append(e)
             _sync()
             tl = time.perf_counter()
+            # the group's entropies in one batched call (its blocks fill the GPU together)
+            svns, srefs = ob.entanglement_entropy_batch(ops[0], evecs, a_sites)
             for b, r in enumerate(group):
                 nu, nd, _ = ob.site_densities(ops[b], evecs[b])
-                svn, sref = ob.entanglement_entropy(ops[b], evecs[b], a_sites)
-                out.append(MblPoint(int(r), (qu, qd), float(e0s[b]), svn, sref, nu, nd, steps))
+                out.append(MblPoint(int(r), (qu, qd), float(e0s[b]), float(svns[b]), float(srefs[b]), nu, nd, steps))
             _sync()
             te = time.perf_counter()
             for op in ops:

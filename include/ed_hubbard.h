@@ -391,6 +391,16 @@ ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double
 ed_status ed_entanglement_entropy(ed_op* op, const double* psi, int mem, uint64_t a_mask, double* s_vn,
                                   double* s_ref, void* stream);
 
+/* The same for n_states states of op's sector (psis: n_states x rows at
+ * mem, row-major; s_vn, s_ref: n_states values each), e.g. the ground
+ * states of the disorder realisations of one ed_lanczos_batch call (any
+ * operator of the sector serves as op).  All blocks of all states share
+ * the bidiagonalisation launches and the host SVD threads; each state's
+ * entropies equal those of its own ed_entanglement_entropy call bit for
+ * bit.  Synchronous. */
+ed_status ed_entanglement_entropy_batch(ed_op* op, int n_states, const double* psis, int mem, uint64_t a_mask,
+                                        double* s_vn, double* s_ref, void* stream);
+
 /* ---------------------------------------------------- several eigenpairs --
  * The nev lowest eigenpairs of a real operator (what TotalSpinExcited_*.cu
  * get from Spectra::SymEigsSolver<cuSpectra::Hubbard<double>> with

@@ -203,3 +203,28 @@ def test_entanglement_cluster_bidiag_matches_gesvd(ed, monkeypatch):
             monkeypatch.setenv("ED_EE_METHOD", "gesvd")
             b = ob.entanglement_entropy(op, psi, list(sites))
             assert abs(a[0] - b[0]) < 1e-12 and abs(a[1] - b[1]) < 1e-10 * max(1.0, b[1])
+
+
+@pytest.mark.parametrize("method", ["bidiag", "gesvd"])
+def test_entanglement_entropy_batch_matches_single(ed, monkeypatch, method):
+    """ed_entanglement_entropy_batch: every state's entropies equal its own
+    single-state call bit for bit (cluster bidiagonalisation and the gesvd
+    path), on the (6,6) and (8,4) sectors of the L=12 chain."""
+    import torch
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    if method == "gesvd":
+        monkeypatch.setenv("ED_EE_METHOD", "gesvd")
+    eps = list(philox_uniform(100, 12, 6.0))
+    terms = L.chain(12, periodic=False, eps=eps)
+    for qu, qd in ((6, 6), (8, 4)):
+        op = ed.Hubbard(ed.H_TBq(12, qu).extend(terms), ed.H_TBq(12, qd).extend(terms), 1.0)
+        g = torch.Generator(device="cuda").manual_seed(qu)
+        psis = torch.empty((3, op.rows()), dtype=torch.float64, device="cuda").uniform_(-1.0, 1.0, generator=g)
+        psis /= psis.norm(dim=1, keepdim=True)
+        svn, sref = ob.entanglement_entropy_batch(op, psis, range(6))
+        for b in range(3):
+            s1, r1 = ob.entanglement_entropy(op, psis[b], range(6))
+            assert svn[b] == s1 and sref[b] == r1, (qu, qd, b)
+        h_svn, _ = ob.entanglement_entropy_batch(op, psis.cpu().numpy(), range(6))
+        assert np.array_equal(h_svn, svn)
+        op.close()
