@@ -207,6 +207,21 @@ __device__ __forceinline__ void acc_up(const int64_t* __restrict__ xq, uint32_t 
     if (CPLX) i += vi;
 }
 
+// Element col of a staged row: one 16-byte shared load for a complex
+// element (row buffers are 16-byte aligned and complex rows start at
+// offset 0), one 8-byte load for a real one.
+template <bool CPLX>
+__device__ __forceinline__ void row_elem(const int64_t* xrow, uint32_t col, int64_t& r, int64_t& i) {
+    if (CPLX) {
+        const longlong2 v = *reinterpret_cast<const longlong2*>(xrow + col);
+        r = v.x;
+        i = v.y;
+    } else {
+        r = xrow[col];
+        i = 0;
+    }
+}
+
 // First row of this CTA (rowList[rowStart[b]]); false when it has none.
 __device__ __forceinline__ bool tma_first_row(const MvArgs& a, uint32_t* u) {
     const uint32_t r0 = __ldg(a.rowStart + blockIdx.x);
@@ -346,13 +361,17 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                     int64_t pr = 0, pi = 0, nr = 0, ni = 0;
                     for (uint32_t q = q0; q < qp; ++q) {
                         const uint32_t col = (S.dent[q] & kColMask) * W;
-                        pr += xrow[col];
-                        if (CPLX) pi += xrow[col + 1];
+                        int64_t vr, vi;
+                        row_elem<CPLX>(xrow, col, vr, vi);
+                        pr += vr;
+                        if (CPLX) pi += vi;
                     }
                     for (uint32_t q = qp; q < q1; ++q) {
                         const uint32_t col = (S.dent[q] & kColMask) * W;
-                        nr += xrow[col];
-                        if (CPLX) ni += xrow[col + 1];
+                        int64_t vr, vi;
+                        row_elem<CPLX>(xrow, col, vr, vi);
+                        nr += vr;
+                        if (CPLX) ni += vi;
                     }
                     if (c) {
                         dr1 = pr - nr;
@@ -414,13 +433,17 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                             const uint32_t pc = (sp >> (8 * c)) & 0xFFu, ec = (se >> (8 * c)) & 0xFFu;
                             for (uint32_t q = q0 + b; q < q0 + pc; ++q) {
                                 const uint32_t col = (S.dent[q] & kColMask) * W;
-                                r += xrow[col];
-                                if (CPLX) i += xrow[col + 1];
+                                int64_t vr, vi;
+                                row_elem<CPLX>(xrow, col, vr, vi);
+                                r += vr;
+                                if (CPLX) i += vi;
                             }
                             for (uint32_t q = q0 + pc; q < q0 + ec; ++q) {
                                 const uint32_t col = (S.dent[q] & kColMask) * W;
-                                r -= xrow[col];
-                                if (CPLX) i -= xrow[col + 1];
+                                int64_t vr, vi;
+                                row_elem<CPLX>(xrow, col, vr, vi);
+                                r -= vr;
+                                if (CPLX) i -= vi;
                             }
                             b = ec;
                             apply_class<CPLX>(ar, ai, r, i, a.coefDN, c, unitD, a.Fc);
@@ -467,8 +490,10 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                                 cur = cl;
                             }
                             const uint32_t col = (e & kColMask) * W;
-                            sr += apply_sign(xrow[col], e);
-                            if (CPLX) si += apply_sign(xrow[col + 1], e);
+                            int64_t vr, vi;
+                            row_elem<CPLX>(xrow, col, vr, vi);
+                            sr += apply_sign(vr, e);
+                            if (CPLX) si += apply_sign(vi, e);
                         }
                         if (cur >= 0) apply_class<CPLX>(ar, ai, sr, si, a.coefDN, cur, unitD, a.Fc);
                     }
@@ -480,8 +505,8 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                 const uint32_t d = c ? d1 : d0;
                 i128& ar = c ? ar1 : ar0;
                 i128& ai = c ? ai1 : ai0;
-                const int64_t xr = xrow[d * W];
-                const int64_t xi = CPLX ? xrow[d * W + 1] : 0;
+                int64_t xr, xi;
+                row_elem<CPLX>(xrow, d * W, xr, xi);
                 const int64_t dq = du + S.ddq[d] + a.Uq * (int64_t)__popcll(stu & S.dst[d] & a.mask);
                 ar += mul_wide(dq, xr);
                 if (CPLX) ai += mul_wide(dq, xi);
