@@ -6,6 +6,8 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <list>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -93,6 +95,118 @@ cudaError_t upload(T** dst, const T* src, size_t n) {
 
 // Plans and uploads the two-pass matvec when the down index's bandwidth
 // leaves a useful window in shared memory; leaves op->striped false otherwise.
+// ---- spin-table cache ----------------------------------------------------
+// A sweep over disorder realisations builds operators whose hopping terms
+// are identical and whose on-site (Make_N) terms differ.  The off-diagonal
+// part of a spin table and its gather schedule depend only on (N, Q, real or
+// complex, the ordered list of two-site terms); they are kept for the last
+// few keys, and on a hit only the folded diagonal is recomputed, adding the
+// Make_N values in term order exactly as build_spin does.
+namespace {
+
+struct SpinKey {
+    int n = 0, q = 0;
+    bool cplx = false;
+    std::vector<uint64_t> words;  // kind, (i, j), bits of value and phase of every two-site term, in order
+    bool operator==(const SpinKey& o) const { return n == o.n && q == o.q && cplx == o.cplx && words == o.words; }
+};
+
+struct SpinEntry {
+    SpinKey key;
+    ed::SpinTable table;
+    int sched_state = 0;  // 0 not built, 1 built, -1 the table takes no schedule
+    ed::GatherSchedule sched;
+};
+
+std::mutex g_spin_mu;
+std::list<SpinEntry> g_spin_cache;  // most recent first
+constexpr size_t kSpinCacheMax = 8;
+
+SpinKey spin_key(int n, int q, bool cplx, const ed_term* t, int nt) {
+    SpinKey k;
+    k.n = n;
+    k.q = q;
+    k.cplx = cplx;
+    for (int i = 0; i < nt; ++i) {
+        if (t[i].kind == ED_TERM_DENSITY) continue;
+        uint64_t v, ph;
+        std::memcpy(&v, &t[i].value, 8);
+        std::memcpy(&ph, &t[i].phase, 8);
+        k.words.push_back((uint64_t)(uint32_t)t[i].kind);
+        k.words.push_back(((uint64_t)(uint32_t)t[i].i << 32) | (uint32_t)t[i].j);
+        k.words.push_back(v);
+        k.words.push_back(ph);
+    }
+    return k;
+}
+
+// diag_re/diag_im/max_diag_abs of a table whose off-diagonal part is set
+ed_status fold_diagonal(const ed::SpinBasis& b, const ed_term* t, int nt, ed::SpinTable* tab) {
+    const int64_t count = b.count;
+    tab->diag_re.assign(count, 0.0);
+    tab->diag_im.assign(count, 0.0);
+    tab->max_diag_abs = 0.0;
+    for (int i = 0; i < nt; ++i)
+        if (t[i].kind == ED_TERM_DENSITY && (t[i].i < 0 || t[i].i >= b.n_sites)) return ED_ERR_ARG;
+    for (int64_t a = 0; a < count; ++a) {
+        const uint64_t w = b.state[a];
+        for (int i = 0; i < nt; ++i)
+            if (t[i].kind == ED_TERM_DENSITY && ((w >> t[i].i) & 1ULL)) {
+                tab->diag_re[a] += t[i].value;
+                tab->diag_im[a] += 0.0;
+            }
+        tab->max_diag_abs = std::max(tab->max_diag_abs, std::abs(std::complex<double>(tab->diag_re[a], tab->diag_im[a])));
+    }
+    return ED_OK;
+}
+
+ed_status build_spin_cached(const ed::SpinBasis& b, const ed_term* t, int nt, bool cplx, ed::SpinTable* out,
+                            std::string* err) {
+    if (nt < 0 || (nt > 0 && !t)) return ED_ERR_ARG;
+    const SpinKey k = spin_key(b.n_sites, b.n_part, cplx, t, nt);
+    {
+        std::lock_guard<std::mutex> g(g_spin_mu);
+        for (auto it = g_spin_cache.begin(); it != g_spin_cache.end(); ++it)
+            if (it->key == k) {
+                *out = it->table;
+                g_spin_cache.splice(g_spin_cache.begin(), g_spin_cache, it);
+                return fold_diagonal(b, t, nt, out);
+            }
+    }
+    const ed_status st = ed::build_spin(b, t, nt, cplx, out, nullptr, err);
+    if (st != ED_OK) return st;
+    std::lock_guard<std::mutex> g(g_spin_mu);
+    g_spin_cache.push_front(SpinEntry{k, *out, 0, {}});
+    if (g_spin_cache.size() > kSpinCacheMax) g_spin_cache.pop_back();
+    return ED_OK;
+}
+
+// The row engine's gather schedule of a table built through the cache.
+bool gather_schedule_cached(const ed::SpinBasis& b, const ed_term* t, int nt, bool cplx, const ed::SpinTable& td,
+                            ed::GatherSchedule* gs, std::string* err) {
+    const SpinKey k = spin_key(b.n_sites, b.n_part, cplx, t, nt);
+    {
+        std::lock_guard<std::mutex> g(g_spin_mu);
+        for (SpinEntry& e : g_spin_cache)
+            if (e.key == k && e.sched_state != 0) {
+                if (e.sched_state < 0) return false;
+                *gs = e.sched;
+                return true;
+            }
+    }
+    const bool ok = ed::build_gather_schedule(td, gs, err);
+    std::lock_guard<std::mutex> g(g_spin_mu);
+    for (SpinEntry& e : g_spin_cache)
+        if (e.key == k) {
+            e.sched_state = ok ? 1 : -1;
+            if (ok) e.sched = *gs;
+            break;
+        }
+    return ok;
+}
+
+}  // namespace
+
 constexpr int kDegreeBlock = 256;  // columns reordered by hop count within each block
 
 static ed_status plan_striped(ed_op* op, bool forced) {
@@ -317,8 +431,8 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
     op->D = op->dimUP * op->dimDN;
     if (op->D >= (1LL << 32)) { delete op; return ED_ERR_RANGE; }  // 32-bit element offsets
     std::string err;
-    ed_status st = ed::build_spin(op->bup, desc->up_terms, desc->n_up_terms, cplx, &op->tup, nullptr, &err);
-    if (st == ED_OK) st = ed::build_spin(op->bdn, desc->dn_terms, desc->n_dn_terms, cplx, &op->tdn, nullptr, &err);
+    ed_status st = build_spin_cached(op->bup, desc->up_terms, desc->n_up_terms, cplx, &op->tup, &err);
+    if (st == ED_OK) st = build_spin_cached(op->bdn, desc->dn_terms, desc->n_dn_terms, cplx, &op->tdn, &err);
     if (st != ED_OK) { delete op; return st; }
 
     // ---- fixed-point scale of the coefficients ----------------------------
@@ -450,7 +564,7 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
     if (!cplx && td.coef.size() <= 1 && !std::getenv("ED_NO_SCHED")) {
         ed::GatherSchedule gs;
         std::string serr;
-        if (ed::build_gather_schedule(td, &gs, &serr)) {
+        if (gather_schedule_cached(op->bdn, desc->dn_terms, desc->n_dn_terms, cplx, td, &gs, &serr)) {
             if (upload(&op->d_dnSched, gs.ent.data(), gs.ent.size()) != cudaSuccess ||
                 upload(&op->d_dnSteps, gs.steps32.data(), gs.steps32.size()) != cudaSuccess) {
                 ed_op_destroy(op);
