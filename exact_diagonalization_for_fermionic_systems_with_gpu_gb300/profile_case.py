@@ -8,6 +8,8 @@
                  timed with device timestamps
 --what solve   : the same solve without timing hooks (what bench.py runs)
 --what perform : --steps operator applies through the FP64 C-ABI path
+--what adjoint : a --steps Lanczos solve with the Ritz vector regenerated in a
+                 second pass, then dE0/dU and dE0/dt (the Lieb18 9+9 workload)
 Cases: kagome12 (6+6, dim 853,776, L2-resident vectors), kagome12_flux
 (complex, Peierls phases), chain12_66 / chain12_75 / chain12_84 (open L=12
 chain, W=6 disorder, the three sectors of the MBL sweep), chain14 (7+7 open
@@ -29,35 +31,74 @@ from .hubbard import H_TBq, Hubbard, random_vector
 from . import _capi
 
 
-def build_case(name: str):
+def case_spec(name: str):
+    """(N, N_up, N_dn, up terms, down terms, U) of a named case."""
     if name == "kagome12":
         t = L.kagome12()
-        return Hubbard(H_TBq(12, 6).extend(t), H_TBq(12, 6).extend(t), 8.0)
+        return 12, 6, 6, t, t, 8.0
     if name == "chain14":
         eps = random_vector(14, 100) * 6.0
         t = L.chain(14, periodic=False, eps=eps)
-        return Hubbard(H_TBq(14, 7).extend(t), H_TBq(14, 7).extend(t), 1.0)
+        return 14, 7, 7, t, t, 1.0
     if name == "lieb18":
         t = L.lieb18()
-        return Hubbard(H_TBq(18, 9).extend(t), H_TBq(18, 9).extend(t), 4.0)
+        return 18, 9, 9, t, t, 4.0
     if name == "lieb18_49":  # Lieb18's down rows (48,620 columns) under 3,060 up rows: 1.2 GB vectors
         t = L.lieb18()
-        return Hubbard(H_TBq(18, 4).extend(t), H_TBq(18, 9).extend(t), 4.0)
+        return 18, 4, 9, t, t, 4.0
     if name == "kagome12_flux":
         t = L.kagome12(flux=0.3)
-        return Hubbard(H_TBq(12, 6).extend(t), H_TBq(12, 6).extend(t), 4.0)
+        return 12, 6, 6, t, t, 4.0
     if name.startswith("chain12_"):  # chain12_66 / chain12_75 / chain12_84: open L=12, W=6, U=1
         qu, qd = int(name[-2]), int(name[-1])
         eps = random_vector(12, 100) * 6.0
         t = L.chain(12, periodic=False, eps=eps)
-        return Hubbard(H_TBq(12, qu).extend(t), H_TBq(12, qd).extend(t), 1.0)
+        return 12, qu, qd, t, t, 1.0
     raise SystemExit(f"unknown case {name}")
+
+
+def build_case(name: str):
+    N, qu, qd, tu, td, U = case_spec(name)
+    return Hubbard(H_TBq(N, qu).extend(tu), H_TBq(N, qd).extend(td), U)
+
+
+def adjoint_run(name: str, op: Hubbard, steps: int) -> None:
+    """The C5-style workload: a fixed-step Lanczos solve whose Ritz vector is
+    regenerated by a second recurrence (three working vectors and u on the
+    device, not the basis), then the adjoint derivatives
+    dE0/dU = sum_i <n_i,up n_i,dn> and dE0/dt = <H_kin>/t (hopping terms
+    -t with t = 1, so dE0/dt = <H_kin>), with E0 - <H_kin> - U dE0/dU as the
+    Hellmann-Feynman consistency check.  Prints one JSON line."""
+    import json
+    import torch
+    from . import observables as ob
+    from .hubbard import Lanczos
+    N, qu, qd, tu, td, U = case_spec(name)
+    ev = torch.empty(op.rows(), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lz = Lanczos()
+    e0, _ = lz.eigen(op, max_steps=steps, mode="fixed", ritz="recompute", seed=0, evec_out=ev)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    nu, nd, dd = ob.site_densities(op, ev)
+    K = Hubbard(H_TBq(N, qu).extend(L.hopping_only(tu)), H_TBq(N, qd).extend(L.hopping_only(td)), 0.0)
+    kin = ob.expect(K, ev)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    norm = float(torch.linalg.vector_norm(ev))
+    K.close()
+    print(json.dumps({"case": name, "dim": op.rows(), "lanczos_steps": steps, "ritz": "recompute",
+                      "E0": e0, "dE0_dU": float(dd.sum()), "dE0_dt": kin,
+                      "hf_check": e0 - kin - U * float(dd.sum()), "n_up": float(nu.sum()), "n_dn": float(nd.sum()),
+                      "evec_norm": norm, "lanczos_s": round(t1 - t0, 3), "adjoint_s": round(t2 - t1, 3),
+                      "matvec_kind": op.matvec_kind}))
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="kagome12")
-    ap.add_argument("--what", default="lanczos", choices=["lanczos", "fused", "solve", "perform"])
+    ap.add_argument("--what", default="lanczos", choices=["lanczos", "fused", "solve", "perform", "adjoint"])
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--ritz", default="none", choices=["none", "stored"],
                     help="stored: keep the Krylov basis and form the Ritz vector, as the bench does")
@@ -66,7 +107,9 @@ def main():
     op = build_case(args.case)
     lib = _capi.load()
     t0 = time.perf_counter()
-    if args.what in ("lanczos", "fused", "solve"):
+    if args.what == "adjoint":
+        adjoint_run(args.case, op, args.steps)
+    elif args.what in ("lanczos", "fused", "solve"):
         ritz = _capi.ED_RITZ_STORED if args.ritz == "stored" else _capi.ED_RITZ_NONE
         cfg = _capi.ed_lanczos_cfg(max_steps=args.steps, mode=_capi.ED_LANCZOS_FIXED, reorth=0,
                                    ritz=ritz, start=_capi.ED_START_RANDOM,
