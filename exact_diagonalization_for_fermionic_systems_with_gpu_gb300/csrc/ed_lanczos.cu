@@ -178,11 +178,73 @@ __global__ void __launch_bounds__(kLzThreads) k_lz_dots(const int64_t* __restric
     }
 }
 
+// Coefficient on q_k of one Gram-Schmidt pass, from the exact dot
+// <w_k, w> = sum_c part[k][c] 2^(e_k + e_w + 24): <w_k, w> / beta_k^2 in units
+// of w's exponent (the i128 total rounded once, as a host conversion of it
+// would be; IEEE divide and exact scalings).
+__device__ __forceinline__ double reorth_r(const uint64_t* lo, const uint64_t* hi, int k, int chunks, const int* e,
+                                           const double* beta, int ew) {
+    i128 acc = 0;
+    for (int c = 0; c < chunks; ++c)
+        acc += (i128)(((u128)hi[(size_t)k * chunks + c] << 64) | (u128)lo[(size_t)k * chunks + c]);
+    const double dotv = i128_to_f64(acc, e[k] + ew + 24);
+    return dotv / (beta[k] * beta[k]) * ldexp(1.0, e[k] - ew);
+}
+
+// One block: the integer coefficients (rt_k, rs_k) and common shift F of a
+// Gram-Schmidt pass against w_0 .. w_{nk-1} (fx_coefs' rule: 62 - exponent
+// bits per coefficient, less the guard bits of the sum of nk terms), so that
+// no step of a reorthogonalised run waits for the host.
+__global__ void __launch_bounds__(kLzThreads) k_reorth_coefs(const uint64_t* __restrict__ lo,
+                                                             const uint64_t* __restrict__ hi, int nk, int chunks,
+                                                             const int* __restrict__ e, const double* __restrict__ beta,
+                                                             int64_t* __restrict__ rt, int* __restrict__ rs,
+                                                             int* __restrict__ Fout) {
+    __shared__ int sm[kLzThreads / 32];
+    int extra = 0;
+    while ((1 << (10 + extra)) < nk) ++extra;
+    const int ew = e[nk];
+    int fmin = 1 << 20;
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+        const double r = reorth_r(lo, hi, k, chunks, e, beta, ew);
+        if (r != 0.0) {
+            int ka;
+            frexp(fabs(r), &ka);
+            fmin = min(fmin, 62 - ka - extra);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) fmin = min(fmin, __shfl_xor_sync(0xffffffffu, fmin, o));
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = fmin;
+    __syncthreads();
+    int Fmin = 1 << 20;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) Fmin = min(Fmin, sm[w]);
+    if (Fmin == (1 << 20)) Fmin = 0;
+    for (int k = threadIdx.x; k < nk; k += blockDim.x) {
+        const double r = reorth_r(lo, hi, k, chunks, e, beta, ew);
+        int64_t t = 0;
+        int sh = 0;
+        if (r != 0.0) {
+            int ka;
+            frexp(fabs(r), &ka);
+            const int F = 62 - ka - extra;
+            if (F - Fmin < 120) {
+                t = (int64_t)llrint(ldexp(r, F));
+                sh = F - Fmin;
+            }
+        }
+        rt[k] = t;
+        rs[k] = sh;
+    }
+    if (threadIdx.x == 0) *Fout = Fmin;
+}
+
 // w <- w - round(sum_k (rt_k q_k >> rs_k) / 2^F)
 __global__ void __launch_bounds__(kLzThreads) k_lz_reorth(int64_t* __restrict__ w, const int64_t* __restrict__ basis,
                                                           int64_t n, int64_t stride, int nk,
                                                           const int64_t* __restrict__ rt, const int* __restrict__ rs,
-                                                          int F) {
+                                                          const int* __restrict__ Fp) {
+    const int F = *Fp;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         i128 acc = 0;
         for (int k = 0; k < nk; ++k) acc += mul_wide(rt[k], basis[(int64_t)k * stride + i]) >> rs[k];
@@ -322,6 +384,7 @@ struct Workspace {
     uint64_t* dot_hi = nullptr;
     int64_t* coef_rt = nullptr;
     int* coef_rs = nullptr;
+    int* coef_F = nullptr;  // common shift of a device-computed Gram-Schmidt pass
     double* ritz_part = nullptr;
     unsigned int* ritz_ctr = nullptr;
     double* inv_norm = nullptr;
@@ -348,7 +411,7 @@ void free_ws(Workspace* w) {
     cudaFree(w->h.e); cudaFree(w->h.m); cudaFree(w->h.beta); cudaFree(w->h.alpha);
     cudaFree(w->h.part_lo); cudaFree(w->h.part_hi); cudaFree(w->h.part_max); cudaFree(w->h.counter);
     cudaFree(w->emax); cudaFree(w->flag); 
-    cudaFree(w->dot_lo); cudaFree(w->dot_hi); cudaFree(w->coef_rt); cudaFree(w->coef_rs);
+    cudaFree(w->dot_lo); cudaFree(w->dot_hi); cudaFree(w->coef_rt); cudaFree(w->coef_rs); cudaFree(w->coef_F);
     cudaFree(w->ritz_part); cudaFree(w->ritz_ctr); cudaFree(w->inv_norm); cudaFree(w->gbar);
     cudaFree(w->stamps); cudaFree(w->fxbound); cudaFree(w->cta_stamps);
     for (cudaEvent_t e : w->events) cudaEventDestroy(e);
@@ -388,6 +451,7 @@ ed_status ensure_ws(ed_op* op, Workspace* w, size_t slots, int64_t DW, int max_s
     LZ_CK(cudaMalloc(&w->dot_hi, sizeof(uint64_t) * ns * kDotChunks));
     LZ_CK(cudaMalloc(&w->coef_rt, sizeof(int64_t) * ns));
     LZ_CK(cudaMalloc(&w->coef_rs, sizeof(int) * ns));
+    LZ_CK(cudaMalloc(&w->coef_F, sizeof(int)));
     LZ_CK(cudaMalloc(&w->ritz_part, sizeof(double) * kLzMaxPartials));
     LZ_CK(cudaMalloc(&w->ritz_ctr, sizeof(unsigned int)));
     LZ_CK(cudaMemset(w->ritz_ctr, 0, sizeof(unsigned int)));
@@ -590,35 +654,13 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
                     dim3 g(nk, kDotChunks);
                     k_lz_dots<<<g, kLzThreads, 0, s>>>(w->basis, DW, w->stride, slot(j + 1), w->dot_lo, w->dot_hi);
                     LZ_CK(cudaGetLastError());
-                    std::vector<uint64_t> lo((size_t)nk * kDotChunks), hi((size_t)nk * kDotChunks);
-                    std::vector<int> ev(nk + 2);
-                    std::vector<double> bv(nk + 2);
-                    LZ_CK(cudaMemcpyAsync(lo.data(), w->dot_lo, sizeof(uint64_t) * lo.size(), cudaMemcpyDeviceToHost, s));
-                    LZ_CK(cudaMemcpyAsync(hi.data(), w->dot_hi, sizeof(uint64_t) * hi.size(), cudaMemcpyDeviceToHost, s));
-                    LZ_CK(cudaMemcpyAsync(ev.data(), H.e, sizeof(int) * (nk + 1), cudaMemcpyDeviceToHost, s));
-                    LZ_CK(cudaMemcpyAsync(bv.data(), H.beta, sizeof(double) * (nk + 1), cudaMemcpyDeviceToHost, s));
-                    LZ_CK(cudaStreamSynchronize(s));
-                    const int ew = ev[nk];
-                    std::vector<double> r(nk);
-                    for (int k = 0; k < nk; ++k) {
-                        __int128 acc = 0;
-                        for (int c = 0; c < kDotChunks; ++c)
-                            acc += (__int128)(((unsigned __int128)hi[(size_t)k * kDotChunks + c] << 64) |
-                                              lo[(size_t)k * kDotChunks + c]);
-                        // <w_k, w> = acc 2^(e_k + e_w + 24); coefficient on q_k in
-                        // units of w's exponent: <w_k,w>/beta_k^2 * 2^(e_k - e_w)
-                        const double dotv = std::ldexp((double)acc, ev[k] + ew + 24);
-                        r[k] = dotv / (bv[k] * bv[k]) * std::ldexp(1.0, ev[k] - ew);
-                    }
-                    std::vector<int64_t> rt;
-                    std::vector<int> rs;
-                    int F;
-                    fx_coefs(r, &rt, &rs, &F);
-                    LZ_CK(cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * nk, cudaMemcpyHostToDevice, s));
-                    LZ_CK(cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * nk, cudaMemcpyHostToDevice, s));
-                    k_lz_reorth<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), w->basis, DW, w->stride, nk,
-                                                                   w->coef_rt, w->coef_rs, F);
+                    k_reorth_coefs<<<1, kLzThreads, 0, s>>>(w->dot_lo, w->dot_hi, nk, kDotChunks, H.e, H.beta,
+                                                            w->coef_rt, w->coef_rs, w->coef_F);
                     LZ_CK(cudaGetLastError());
+                    k_lz_reorth<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), w->basis, DW, w->stride, nk,
+                                                                   w->coef_rt, w->coef_rs, w->coef_F);
+                    LZ_CK(cudaGetLastError());
+                    launches += 1;
                     launches += 2;
                 }
                 k_lz_stats<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), DW, lz, j + 1);
