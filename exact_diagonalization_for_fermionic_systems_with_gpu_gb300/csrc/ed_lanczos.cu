@@ -1024,7 +1024,6 @@ ed_status lanczos_batch_run(ed_op* const* ops, int B, const ed_lanczos_cfg* cfg,
     // every instance: T, status, Ritz vector
     ed_status result = ED_OK;
     for (int b = 0; b < B && result == ED_OK; ++b) {
-        ed_op* op = ops[b];
         Workspace* w = ws[b];
         const LzState& H = w->h;
         LzState hs;
