@@ -73,8 +73,6 @@ int ceil_log2(double x) {
     return f == 0.5 ? k - 1 : k;
 }
 
-int bitlen_u64h(uint64_t v) { return v ? 64 - __builtin_clzll(v) : 0; }
-
 struct OpExtra {
     void* lz_ws = nullptr;
 };
