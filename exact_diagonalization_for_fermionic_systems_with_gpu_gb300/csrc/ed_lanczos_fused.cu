@@ -589,7 +589,10 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
         __syncthreads();
 
         // ---- phase A: w_{j+1} of every instance ----------------------------
-        for (int b = 0; b < B; ++b) {
+        // last instance first: the rows phase ended on it, so its u and w_j
+        // are the vectors still in L2, and the next rows phase starts on
+        // instance 0, whose w_{j+1} this phase writes last
+        for (int b = B - 1; b >= 0; --b) {
             const LzInst& I = f.inst[b];
             const int64_t* xq = I.basis + (size_t)j * f.stride;
             const int64_t* pq = j > 0 ? I.basis + (size_t)(j - 1) * f.stride : xq;
