@@ -20,6 +20,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "ed_hubbard.h"
@@ -89,6 +90,8 @@ public:
     int64_t cols() const { return ed_op_cols(op_); }
     int64_t dimUP() const { return ed_op_dim_up(op_); }
     int64_t dimDN() const { return ed_op_dim_dn(op_); }
+    // ED_MV_ROWS, ED_MV_TWO_PASS or ED_MV_GENERIC: the matvec of its Lanczos steps
+    int matvec_kind() const { return ed_op_matvec_kind(op_); }
     ed_op* handle() const { return op_; }
 
 private:
@@ -152,6 +155,27 @@ public:
         return result.e0;
     }
 };
+
+// Entanglement entropy of a host state for the sites in a_mask
+// (EEmatHubAB_GPU::Make_Write + cusolverDsvd + the entropy sum of
+// Hubbard_EE_test.cu:78-83): {S_vN = -sum s^2 ln s^2, S_ref = -sum s ln s}.
+inline std::pair<double, double> entanglement_entropy(Hubbard& h, const std::vector<double>& psi, uint64_t a_mask) {
+    double svn = 0.0, sref = 0.0;
+    check(ed_entanglement_entropy(h.handle(), psi.data(), ED_MEM_HOST, a_mask, &svn, &sref, nullptr),
+          "ed_entanglement_entropy");
+    return {svn, sref};
+}
+
+// The same for n states of h's sector stored one after another in psis
+// (host, n x rows), in one batched call; each value equals its own call's.
+inline void entanglement_entropy_batch(Hubbard& h, int n, const std::vector<double>& psis, uint64_t a_mask,
+                                       std::vector<double>& s_vn, std::vector<double>& s_ref) {
+    s_vn.assign(n, 0.0);
+    s_ref.assign(n, 0.0);
+    check(ed_entanglement_entropy_batch(h.handle(), n, psis.data(), ED_MEM_HOST, a_mask, s_vn.data(), s_ref.data(),
+                                        nullptr),
+          "ed_entanglement_entropy_batch");
+}
 
 // Spectra::SymEigsSolver<OpType>(op, nev, ncv) with SortRule::SmallestAlge;
 // eigenvectors() is rows x nev column-major (Eigen's MatrixXd layout).

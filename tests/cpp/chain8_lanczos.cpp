@@ -1,7 +1,8 @@
 // C++ caller of the C ABI through include/ed_hubbard.hpp, written the way the
 // reference drivers are (MBL_test/src/Hubbard_test.cu): build the two H_TBq,
-// the operator, run Lanczos, print E0; then the three lowest eigenpairs
-// (TotalSpinExcited_*) and one Krylov time step (Time_evol_test.cu).
+// the operator, run Lanczos, print E0 and the entanglement entropy; then the
+// three lowest eigenpairs (TotalSpinExcited_*) and one Krylov time step
+// (Time_evol_test.cu).
 // Argument "--basis-only" exercises the host-side part without a GPU.
 #include <cstdio>
 #include <cstring>
@@ -29,6 +30,14 @@ int main(int argc, char** argv) {
         std::vector<double> evec;
         const double e0 = lanc.eigen(h, {}, evec, 100, ED_LANCZOS_FIXED, true, 0);
         std::printf("E0 %.15f steps %zu\n", e0, lanc.a.size());
+        // Hubbard_EE_test.cu: entanglement of sites 0..3, one state and a batch of two
+        const auto ee = ed::entanglement_entropy(h, evec, 0x0Fu);
+        std::vector<double> two(evec);
+        two.insert(two.end(), evec.begin(), evec.end());
+        std::vector<double> bvn, bref;
+        ed::entanglement_entropy_batch(h, 2, two, 0x0Fu, bvn, bref);
+        std::printf("EE %.15f %.15f %d %d\n", ee.first, ee.second, (int)(bvn[0] == ee.first && bvn[1] == ee.first),
+                    h.matvec_kind());
         // TotalSpinExcited_*: the lowest pairs through the Spectra-shaped solver
         ed::SymEigsSolver eigs(h, 3, 4 * (3 + 1));
         eigs.init();

@@ -36,6 +36,9 @@ def test_cpp_header_lanczos_on_gpu(tmp_path, edlib, golden_energies):
     eig = out.split("EIGS ")[1].split()
     assert int(eig[0]) == 3 and abs(float(eig[1]) - g) < 1e-10 * abs(g)
     assert abs(float(eig[2]) - golden_energies["chain8_pbc_q44_U4"]["E1"]) < 1e-9
+    ee = out.split("EE ")[1].split()
+    assert abs(float(ee[0]) - golden_energies["chain8_pbc_q44_U4"]["EE_vN_A0123"]) < 1e-8
+    assert ee[2] == "1" and int(ee[3]) in (0, 1, 2)
     kry = out.split("KRYLOV ")[1].split()
     assert abs(float(kry[3]) - 1.0) < 1e-12
 
