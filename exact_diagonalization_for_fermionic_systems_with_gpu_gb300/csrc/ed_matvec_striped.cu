@@ -43,6 +43,27 @@ constexpr int kDownThreads = 1024;
 constexpr int kUpThreads = 768;    // 24 warps (80 registers a thread): 24 rows of a stripe per item
 constexpr int kDownBatch = 8;      // pass-D schedule words loaded before their sums
 
+// One signed window word of the pass-D schedule.
+__device__ __forceinline__ int64_t down_term(const int64_t* win, uint32_t e) {
+    const int64_t v = win[e & 0x7FFFu];
+    return (e & 0x8000u) ? -v : v;
+}
+
+// Steps s0 .. n-1 of one column's schedule: kDownBatch at a time, then singly.
+__device__ __forceinline__ int64_t down_tail(const int64_t* win, const uint16_t* sc, int64_t cpad, int s0, int n) {
+    int64_t acc = 0;
+    int s = s0;
+    for (; s + kDownBatch <= n; s += kDownBatch) {
+        uint32_t e[kDownBatch];
+#pragma unroll
+        for (int t = 0; t < kDownBatch; ++t) e[t] = __ldg(sc + (size_t)(s + t) * cpad);
+#pragma unroll
+        for (int t = 0; t < kDownBatch; ++t) acc += down_term(win, e[t]);
+    }
+    for (; s < n; ++s) acc += down_term(win, __ldg(sc + (size_t)s * cpad));
+    return acc;
+}
+
 // ---------------------------------------------------------------- pass D --
 __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g) {
     extern __shared__ __align__(128) unsigned char sm[];
@@ -79,27 +100,34 @@ __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g
         }
         __syncthreads();
         if (give_up) return;  // the copy this CTA waited for has given up; none other is in flight
-        for (int64_t c = c0 + tid; c < c1; c += kDownThreads) {
-            const int n = __ldg(g.steps32 + (c >> 5));
-            const uint16_t* sc = g.sched16 + c;
-            int64_t acc = 0;
+        // two columns per iteration (c and c + 1024): their schedule words are
+        // loaded together, kDownBatch steps of each in flight
+        for (int64_t c = c0 + tid; c < c1; c += 2 * kDownThreads) {
+            const int64_t cb = c + kDownThreads;
+            const bool hb = cb < c1;
+            const int na = __ldg(g.steps32 + (c >> 5)), nb = hb ? __ldg(g.steps32 + (cb >> 5)) : 0;
+            const uint16_t* sa = g.sched16 + c;
+            const uint16_t* sb = g.sched16 + (hb ? cb : c);
+            int64_t acca = 0, accb = 0;
+            const int nm = na < nb ? na : nb;
             int s = 0;
-            for (; s + kDownBatch <= n; s += kDownBatch) {
-                uint32_t e[kDownBatch];
-#pragma unroll
-                for (int t = 0; t < kDownBatch; ++t) e[t] = __ldg(sc + (size_t)(s + t) * g.cpad);
+            for (; s + kDownBatch <= nm; s += kDownBatch) {
+                uint32_t ea[kDownBatch], eb[kDownBatch];
 #pragma unroll
                 for (int t = 0; t < kDownBatch; ++t) {
-                    const int64_t v = win[e[t] & 0x7FFFu];
-                    acc += (e[t] & 0x8000u) ? -v : v;
+                    ea[t] = __ldg(sa + (size_t)(s + t) * g.cpad);
+                    eb[t] = __ldg(sb + (size_t)(s + t) * g.cpad);
+                }
+#pragma unroll
+                for (int t = 0; t < kDownBatch; ++t) {
+                    acca += down_term(win, ea[t]);
+                    accb += down_term(win, eb[t]);
                 }
             }
-            for (; s < n; ++s) {
-                const uint32_t e = __ldg(sc + (size_t)s * g.cpad);
-                const int64_t v = win[e & 0x7FFFu];
-                acc += (e & 0x8000u) ? -v : v;
-            }
-            g.sdn[u * dimDN + c] = acc;
+            acca += down_tail(win, sa, g.cpad, s, na);
+            if (hb) accb += down_tail(win, sb, g.cpad, s, nb);
+            g.sdn[u * dimDN + c] = acca;
+            if (hb) g.sdn[u * dimDN + cb] = accb;
         }
         __syncthreads();  // the window is free for the next copy
     }
