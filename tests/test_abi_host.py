@@ -124,6 +124,34 @@ def test_op_create_argument_errors(edlib):
     assert edlib.ed_op_create(None, C.byref(d), 0) == 1
     assert edlib.ed_op_perform(None, None, None, 0, None) == 1
     assert edlib.ed_lanczos_run(None, None, None, 0, None, 0, None, None, None, None) == 1
+    assert edlib.ed_entanglement_entropy_batch(None, 1, None, 0, 0, None, None, None) == 1
+    assert edlib.ed_op_matvec_kind(None) == -1
+
+
+def test_op_create_cached_tables_still_check_onsite_sites(edlib):
+    """A second operator with the same hopping terms reuses the cached
+    off-diagonal tables; its on-site terms are still checked (a site outside
+    the lattice is an argument error, not a silent table hit)."""
+    import ctypes as C
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import _capi
+    hops = [(0, i, (i + 1) % 8, -1.0) for i in range(8)]
+    def desc(extra):
+        t = hops + extra
+        arr = (_capi.ed_term * len(t))()
+        for k, (kind, i, j, v) in enumerate(t):
+            arr[k].kind, arr[k].i, arr[k].j, arr[k].value = kind, i, j, v
+        d = _capi.ed_model_desc()
+        d.n_sites, d.n_up, d.n_dn = 8, 3, 3
+        d.up_terms, d.n_up_terms = arr, len(t)
+        d.dn_terms, d.n_dn_terms = arr, len(t)
+        return d, arr
+    h = C.c_void_p()
+    d1, keep1 = desc([(2, 3, 0, 0.5)])
+    st = edlib.ed_op_create(C.byref(h), C.byref(d1), 0)  # fills the cache (no device here: it may stop later)
+    if st == 0:
+        edlib.ed_op_destroy(h)
+    d2, keep2 = desc([(2, 9, 0, 0.5)])  # Make_N on site 9 of 8
+    assert edlib.ed_op_create(C.byref(h), C.byref(d2), 0) == 1
 
 
 def test_ell_rejects_peierls(edlib):
