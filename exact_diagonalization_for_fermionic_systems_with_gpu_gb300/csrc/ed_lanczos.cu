@@ -650,14 +650,20 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             if (cfg->reorth) {
                 // classical Gram-Schmidt, twice, against v_0..v_j
                 const int nk = j + 1;
+                // row chunks per dot: up to kDotChunks, ~2048 elements each
+                // (exact integer sums: the split does not change them)
+                const int chunks = (int)std::min<int64_t>(kDotChunks, std::max<int64_t>(1, (DW + 2047) / 2048));
+                // the update sums nk basis vectors per element: one element
+                // per thread, so that small sectors still fill the GPU
+                const int grr = (int)std::min<int64_t>(152 * 8, (DW + kLzThreads - 1) / kLzThreads);
                 for (int pass = 0; pass < 2; ++pass) {
-                    dim3 g(nk, kDotChunks);
+                    dim3 g(nk, chunks);
                     k_lz_dots<<<g, kLzThreads, 0, s>>>(w->basis, DW, w->stride, slot(j + 1), w->dot_lo, w->dot_hi);
                     LZ_CK(cudaGetLastError());
-                    k_reorth_coefs<<<1, kLzThreads, 0, s>>>(w->dot_lo, w->dot_hi, nk, kDotChunks, H.e, H.beta,
+                    k_reorth_coefs<<<1, kLzThreads, 0, s>>>(w->dot_lo, w->dot_hi, nk, chunks, H.e, H.beta,
                                                             w->coef_rt, w->coef_rs, w->coef_F);
                     LZ_CK(cudaGetLastError());
-                    k_lz_reorth<<<lz_grid(DW), kLzThreads, 0, s>>>(slot(j + 1), w->basis, DW, w->stride, nk,
+                    k_lz_reorth<<<grr, kLzThreads, 0, s>>>(slot(j + 1), w->basis, DW, w->stride, nk,
                                                                    w->coef_rt, w->coef_rs, w->coef_F);
                     LZ_CK(cudaGetLastError());
                     launches += 1;
