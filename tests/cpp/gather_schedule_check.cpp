@@ -2,7 +2,9 @@
 // for spin tables of several lattices, every entry of every row appears in
 // the schedule exactly once (as an index of +x or -x, the rest of the steps
 // reading zeros), no step of a 16-column group touches a bank pair twice, and
-// the per-block step counts cover the entries.  Prints one line
+// the per-block step counts cover the entries; the same for the permuted
+// two-pass schedules, the hop-count ordering of columns and the variants with
+// two targets per bank pair and split signs.  Prints one line
 // per case: "<name> count <n> max_len <L> steps <S> ok".
 #include <cstdio>
 #include <algorithm>
@@ -14,6 +16,54 @@
 #include "ed_tables.hpp"
 
 using namespace ed;
+
+// A permuted 32-bit schedule against its table: every entry (of the sign the
+// filter keeps) exactly once, nothing past a block's step count, at most
+// `cap` targets per bank pair in a step of a 16-column group.
+static int check32(const char* name, const SpinTable& t, const std::vector<uint32_t>& perm,
+                   const std::vector<uint32_t>& inv, const GatherSchedule32& g32, int cap, int sign_filter) {
+    const int64_t cnt = t.count;
+    for (int64_t c = 0; c < g32.count_pad; ++c) {
+        std::map<int64_t, int> want, got;
+        if (c < cnt) {
+            const int64_t d = perm[c];
+            for (int k = 0; k < t.len[d]; ++k) {
+                const uint32_t e = t.ent[(size_t)k * cnt + d];
+                if (sign_filter >= 0 && ((e & kSignBit) != 0) != (sign_filter == 1)) continue;
+                const int64_t tc = (int64_t)inv[e & kColMask] + 1;
+                ++want[(e & kSignBit) ? -tc : tc];
+            }
+        }
+        for (int s = 0; s < g32.steps; ++s) {
+            const uint32_t w = g32.ent[(size_t)s * g32.count_pad + c];
+            if (w == kSched32None) continue;
+            if (s >= g32.steps32[c / 32]) {
+                std::printf("%s cap%d/%d entry beyond the block's steps\n", name, cap, sign_filter);
+                return 1;
+            }
+            const int64_t tc = (int64_t)(w & 0x7FFFFFFFu) + 1;
+            ++got[(w & 0x80000000u) ? -tc : tc];
+        }
+        if (want != got) {
+            std::printf("%s cap%d/%d column %lld differs from the table\n", name, cap, sign_filter, (long long)c);
+            return 1;
+        }
+    }
+    for (int64_t g0 = 0; g0 < g32.count_pad; g0 += 16)
+        for (int s = 0; s < g32.steps; ++s) {
+            int use[16] = {0};
+            for (int l = 0; l < 16; ++l) {
+                const uint32_t w = g32.ent[(size_t)s * g32.count_pad + g0 + l];
+                if (w == kSched32None) continue;
+                if (++use[(w & 0x7FFFFFFFu) % 16] > cap) {
+                    std::printf("%s cap%d/%d: bank pair used more than %d times in a step\n", name, cap, sign_filter,
+                                cap);
+                    return 1;
+                }
+            }
+        }
+    return 0;
+}
 
 static int check(const char* name, int n, int q, const std::vector<ed_term>& terms) {
     SpinBasis b;
@@ -133,6 +183,79 @@ static int check(const char* name, int n, int q, const std::vector<ed_term>& ter
         std::printf("%s rcm bandwidth %lld below an entry's distance %lld\n", name, (long long)bw, (long long)bw_seen);
         return 1;
     }
+    // columns ordered by hop count within 256-column blocks: still a
+    // permutation, lengths non-increasing inside a block, bandwidth updated
+    std::vector<uint32_t> perm2 = perm, inv2 = inv;
+    int64_t bw2 = 0;
+    sort_blocks_by_degree(t, 256, &perm2, &inv2, &bw2);
+    std::vector<char> hit2(cnt, 0);
+    int64_t bw2_seen = 0;
+    for (int64_t c = 0; c < cnt; ++c) {
+        if (perm2[c] >= cnt || hit2[perm2[c]] || inv2[perm2[c]] != c ||
+            (c % 256 != 0 && t.len[perm2[c]] > t.len[perm2[c - 1]])) {
+            std::printf("%s degree-sorted order broken at %lld\n", name, (long long)c);
+            return 1;
+        }
+        hit2[perm2[c]] = 1;
+        for (int k = 0; k < t.len[perm2[c]]; ++k)
+            bw2_seen = std::max<int64_t>(bw2_seen,
+                                         std::llabs((int64_t)inv2[t.ent[(size_t)k * cnt + perm2[c]] & kColMask] - c));
+    }
+    if (bw2_seen != bw2) {
+        std::printf("%s sorted bandwidth %lld, entries reach %lld\n", name, (long long)bw2, (long long)bw2_seen);
+        return 1;
+    }
+    // two targets per bank pair (pass D's schedule), and the sign-split
+    // schedules, over the sorted order
+    for (int sf = -1; sf <= 1; ++sf) {
+        GatherSchedule32 gc;
+        if (!build_gather_schedule32(t, perm2, inv2, &gc, &err, sf, 2)) {
+            std::printf("%s cap2 schedule failed: %s\n", name, err.c_str());
+            return 1;
+        }
+        if (check32(name, t, perm2, inv2, gc, 2, sf)) return 1;
+    }
+    // the row engine's schedule with two targets per bank pair
+    GatherSchedule g2;
+    if (!build_gather_schedule(t, &g2, &err, 2)) {
+        std::printf("%s row-engine cap2 schedule failed: %s\n", name, err.c_str());
+        return 1;
+    }
+    for (int64_t d = 0; d < cp; ++d) {
+        std::map<int64_t, int> want, got;
+        if (d < cnt)
+            for (int k = 0; k < t.len[d]; ++k) {
+                const uint32_t e = t.ent[(size_t)k * cnt + d];
+                const int64_t c = (int64_t)(e & kColMask) + 1;
+                ++want[(e & kSignBit) ? -c : c];
+            }
+        for (int s = 0; s < g2.steps32[d / 32]; ++s) {
+            const int64_t w = g2.ent[(size_t)s * cp + d];
+            if (w >= zb + 16) {
+                std::printf("%s row-engine cap2 index out of the buffer\n", name);
+                return 1;
+            }
+            if (w >= zb) continue;
+            ++got[w < nb ? w + 1 : -(w - nb + 1)];
+        }
+        if (want != got) {
+            std::printf("%s row-engine cap2 row %lld differs from the table\n", name, (long long)d);
+            return 1;
+        }
+    }
+    for (int64_t g0 = 0; g0 < cp; g0 += 16)
+        for (int s = 0; s < g2.steps32[g0 / 32]; ++s) {
+            std::map<int64_t, int> addr_of_res[16];
+            for (int l = 0; l < 16; ++l) {
+                const int64_t w = g2.ent[(size_t)s * cp + g0 + l];
+                ++addr_of_res[w % 16][w];
+            }
+            for (int r = 0; r < 16; ++r)
+                if (addr_of_res[r].size() > 2) {
+                    std::printf("%s row-engine cap2: more than two addresses on a bank pair\n", name);
+                    return 1;
+                }
+        }
     std::printf("%s count %lld max_len %d steps %d rcm_bandwidth %lld steps32 %d ok\n", name, (long long)cnt, t.max_len,
                 g.steps, (long long)bw, g32.steps);
     return 0;
