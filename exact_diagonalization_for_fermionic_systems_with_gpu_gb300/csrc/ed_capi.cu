@@ -223,41 +223,14 @@ static ed_status plan_striped(ed_op* op, bool forced) {
     if (chunk < 1024) return ED_OK;  // too wide: the generic kernel stays
     if (!forced && op->dimDN * 8 <= 160 * 1024) return ED_OK;
     // Pass D's schedule: one step per hop of a column, at most two targets
-    // per bank pair in a step (a two-way conflict at worst), stored step by
-    // step as 16-bit offsets into the chunk's window | sign << 15.  A window
-    // starts on a multiple of 16 columns, so an offset keeps its column's
-    // residue mod 16; idle lanes of a step read one zero slot (a broadcast) at
-    // a residue no busy lane of their half-warp uses in that step, from the
-    // 16 zero slots [zbase, zbase + 16) past every window.
+    // per bank pair in a step, as 16-bit offsets into each chunk's window
+    // (ed::window_schedule16)
     ed::GatherSchedule32 g;
     std::string err;
     if (!ed::build_gather_schedule32(op->tdn, perm, inv, &g, &err, -1, 2)) return ED_OK;
-    const int64_t zbase = (chunk + 2 * bw + 16 + 15) / 16 * 16;
-    if (zbase + 16 > 32768) return ED_OK;
-    const int64_t cpad = g.count_pad, nsteps = std::max(g.steps, 1);
-    std::vector<uint16_t> s16((size_t)nsteps * cpad, 0);
-    for (int64_t cg = 0; cg < cpad; cg += 16) {
-        const int64_t k = cg / chunk;  // a chunk is a multiple of 1024 columns: one chunk per group
-        const int64_t w0 = std::max<int64_t>(0, k * chunk - bw) & ~(int64_t)15;
-        int64_t w1 = std::min<int64_t>(op->dimDN, (k + 1) * chunk + bw);
-        w1 = (w1 + 1) & ~(int64_t)1;
-        for (int64_t st = 0; st < nsteps; ++st) {
-            auto word = [&](int l) { return st < g.steps ? g.ent[(size_t)st * cpad + cg + l] : ed::kSched32None; };
-            uint32_t used = 0;
-            for (int l = 0; l < 16; ++l) {
-                const uint32_t e = word(l);
-                if (e == ed::kSched32None) continue;
-                const int64_t off = (int64_t)(e & 0x7FFFFFFFu) - w0;
-                if (off < 0 || off >= w1 - w0) return ED_OK;  // not within the chunk's window
-                used |= 1u << (off & 15);
-                s16[(size_t)st * cpad + cg + l] = (uint16_t)(off | ((e & 0x80000000u) ? 0x8000 : 0));
-            }
-            int z = 0;
-            while (z < 16 && ((used >> z) & 1u)) ++z;  // a step with an idle lane leaves a residue free
-            for (int l = 0; l < 16; ++l)
-                if (word(l) == ed::kSched32None) s16[(size_t)st * cpad + cg + l] = (uint16_t)(zbase + (z & 15));
-        }
-    }
+    std::vector<uint16_t> s16;
+    int64_t zbase = 0;
+    if (!ed::window_schedule16(g, op->dimDN, chunk, bw, &s16, &zbase)) return ED_OK;
     const int Fc = op->mv.Fc;
     std::vector<int64_t> dq((size_t)op->dimDN);
     std::vector<uint64_t> st((size_t)op->dimDN);
@@ -279,7 +252,7 @@ static ed_status plan_striped(ed_op* op, bool forced) {
     op->st_chunk = (int)chunk;
     op->st_win = (int)(zbase + 16);
     op->st_zbase = (int)zbase;
-    op->st_cpad = cpad;
+    op->st_cpad = g.count_pad;
     return ED_OK;
 }
 

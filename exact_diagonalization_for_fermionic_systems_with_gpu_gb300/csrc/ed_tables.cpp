@@ -426,6 +426,39 @@ bool build_gather_schedule(const SpinTable& t, GatherSchedule* g, std::string* e
     return true;
 }
 
+bool window_schedule16(const GatherSchedule32& g, int64_t count, int64_t chunk, int64_t bw, std::vector<uint16_t>* out,
+                       int64_t* zbase_out) {
+    if (chunk <= 0 || chunk % 1024 != 0) return false;  // whole 32-column blocks per chunk
+    const int64_t zbase = (chunk + 2 * bw + 16 + 15) / 16 * 16;
+    if (zbase + 16 > 32768) return false;
+    const int64_t cpad = g.count_pad, nsteps = std::max(g.steps, 1);
+    out->assign((size_t)nsteps * cpad, 0);
+    for (int64_t cg = 0; cg < cpad; cg += 16) {
+        const int64_t k = cg / chunk;  // a chunk is a multiple of 1024 columns: one chunk per group
+        const int64_t w0 = std::max<int64_t>(0, k * chunk - bw) & ~(int64_t)15;
+        int64_t w1 = std::min<int64_t>(count, (k + 1) * chunk + bw);
+        w1 = (w1 + 1) & ~(int64_t)1;
+        for (int64_t st = 0; st < nsteps; ++st) {
+            auto word = [&](int l) { return st < g.steps ? g.ent[(size_t)st * cpad + cg + l] : kSched32None; };
+            uint32_t used = 0;
+            for (int l = 0; l < 16; ++l) {
+                const uint32_t e = word(l);
+                if (e == kSched32None) continue;
+                const int64_t off = (int64_t)(e & 0x7FFFFFFFu) - w0;
+                if (off < 0 || off >= w1 - w0) return false;  // not within the chunk's window
+                used |= 1u << (off & 15);
+                (*out)[(size_t)st * cpad + cg + l] = (uint16_t)(off | ((e & 0x80000000u) ? 0x8000 : 0));
+            }
+            int z = 0;
+            while (z < 16 && ((used >> z) & 1u)) ++z;  // a step with an idle lane leaves a residue free
+            for (int l = 0; l < 16; ++l)
+                if (word(l) == kSched32None) (*out)[(size_t)st * cpad + cg + l] = (uint16_t)(zbase + (z & 15));
+        }
+    }
+    *zbase_out = zbase;
+    return true;
+}
+
 void rcm_order(const SpinTable& t, std::vector<uint32_t>* perm, std::vector<uint32_t>* inv, int64_t* bandwidth) {
     const int64_t n = t.count;
     std::vector<std::vector<uint32_t>> adj(n);

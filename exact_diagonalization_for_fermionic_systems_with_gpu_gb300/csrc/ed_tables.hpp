@@ -137,6 +137,19 @@ struct GatherSchedule32 {
 bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
                              GatherSchedule32* g, std::string* err, int sign_filter = -1, int bank_cap = 1);
 
+// Pass D's schedule (two-pass matvec): the permuted schedule g as 16-bit
+// words, step-major ([step][count_pad]), each the offset of the target in the
+// window of its column's chunk, x[w0 .. w1) with w0 = (k chunk - bw) rounded
+// down to 16 (at least 0) and w1 = min(count, (k+1) chunk + bw) rounded up to
+// even, | sign << 15.  A window starts on a multiple of 16 columns, so an
+// offset keeps its target's residue mod 16; the idle lanes of a half-warp
+// step all read one zero slot zbase + z (a broadcast) at a residue z that no
+// busy lane of that step uses, from 16 zero slots [zbase, zbase + 16) past
+// every window.  False when a target lies outside its chunk's window, the
+// chunk is not a multiple of 1024 columns, or the window needs 15 bits or more.
+bool window_schedule16(const GatherSchedule32& g, int64_t count, int64_t chunk, int64_t bw, std::vector<uint16_t>* out,
+                       int64_t* zbase);
+
 // Build both layouts for one spin from a term list.  Returns ED_OK or an
 // error (bad site, table overflow, complex term in a real operator when
 // allow_complex is false).

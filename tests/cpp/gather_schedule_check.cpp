@@ -215,6 +215,82 @@ static int check(const char* name, int n, int q, const std::vector<ed_term>& ter
         }
         if (check32(name, t, perm2, inv2, gc, 2, sf)) return 1;
     }
+    // pass D's 16-bit window schedule (what k_mv_down reads): every entry of
+    // every column once as window offset + window start, offsets inside the
+    // window or on the zero slots, at most two targets per bank pair in a
+    // half-warp step, idle lanes on one zero slot of a residue no busy lane
+    // of the step uses
+    {
+        GatherSchedule32 gc;
+        build_gather_schedule32(t, perm2, inv2, &gc, &err, -1, 2);
+        for (int64_t chunk : {(int64_t)1024, (int64_t)2048}) {
+            std::vector<uint16_t> s16;
+            int64_t zb16 = 0;
+            if (!window_schedule16(gc, cnt, chunk, bw2, &s16, &zb16)) {
+                std::printf("%s window schedule (chunk %lld) refused\n", name, (long long)chunk);
+                return 1;
+            }
+            const int64_t cpd = gc.count_pad, nst = std::max(gc.steps, 1);
+            if ((int64_t)s16.size() != nst * cpd || zb16 % 16 != 0) {
+                std::printf("%s window schedule shape\n", name);
+                return 1;
+            }
+            for (int64_t c = 0; c < cpd; ++c) {
+                const int64_t k = c / chunk;
+                const int64_t w0 = std::max<int64_t>(0, k * chunk - bw2) & ~(int64_t)15;
+                int64_t w1 = std::min<int64_t>(cnt, (k + 1) * chunk + bw2);
+                w1 = (w1 + 1) & ~(int64_t)1;
+                std::map<int64_t, int> want, got;
+                if (c < cnt)
+                    for (int kk = 0; kk < t.len[perm2[c]]; ++kk) {
+                        const uint32_t e = t.ent[(size_t)kk * cnt + perm2[c]];
+                        const int64_t tc = (int64_t)inv2[e & kColMask] + 1;
+                        ++want[(e & kSignBit) ? -tc : tc];
+                    }
+                for (int st = 0; st < gc.steps32[c / 32]; ++st) {
+                    const uint32_t w = s16[(size_t)st * cpd + c];
+                    const int64_t off = w & 0x7FFF;
+                    if (off >= zb16 + 16 || (off >= zb16 && (w & 0x8000))) {
+                        std::printf("%s window offset out of the buffer\n", name);
+                        return 1;
+                    }
+                    if (off >= zb16) continue;
+                    if (off >= w1 - w0) {
+                        std::printf("%s window offset past the copied window\n", name);
+                        return 1;
+                    }
+                    const int64_t tc = off + w0 + 1;
+                    ++got[(w & 0x8000) ? -tc : tc];
+                }
+                if (want != got) {
+                    std::printf("%s window schedule column %lld differs from the table\n", name, (long long)c);
+                    return 1;
+                }
+            }
+            for (int64_t g0 = 0; g0 < cpd; g0 += 16)
+                for (int st = 0; st < gc.steps32[g0 / 32]; ++st) {
+                    int use[16] = {0};
+                    int zres = -1;
+                    for (int l = 0; l < 16; ++l) {
+                        const int64_t off = s16[(size_t)st * cpd + g0 + l] & 0x7FFF;
+                        if (off >= zb16) {
+                            if (zres >= 0 && zres != (int)(off - zb16)) {
+                                std::printf("%s idle lanes on different zero slots\n", name);
+                                return 1;
+                            }
+                            zres = (int)(off - zb16);
+                        } else if (++use[off % 16] > 2) {
+                            std::printf("%s window schedule: more than two targets on a bank pair\n", name);
+                            return 1;
+                        }
+                    }
+                    if (zres >= 0 && use[zres]) {
+                        std::printf("%s zero slot shares a bank pair with a target\n", name);
+                        return 1;
+                    }
+                }
+        }
+    }
     // the row engine's schedule with two targets per bank pair
     GatherSchedule g2;
     if (!build_gather_schedule(t, &g2, &err, 2)) {
