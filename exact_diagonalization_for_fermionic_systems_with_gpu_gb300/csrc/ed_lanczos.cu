@@ -240,15 +240,34 @@ __global__ void __launch_bounds__(kLzThreads) k_reorth_coefs(const uint64_t* __r
 }
 
 // w <- w - round(sum_k (rt_k q_k >> rs_k) / 2^F)
+// kReorthLanes lanes share an element: lane r of the group sums the terms
+// k = r, r + kReorthLanes, ...; the exact 128-bit partials are combined by
+// shuffles (the same total in any order) and the group's first lane writes.
+constexpr int kReorthLanes = 4;
+
 __global__ void __launch_bounds__(kLzThreads) k_lz_reorth(int64_t* __restrict__ w, const int64_t* __restrict__ basis,
                                                           int64_t n, int64_t stride, int nk,
                                                           const int64_t* __restrict__ rt, const int* __restrict__ rs,
                                                           const int* __restrict__ Fp) {
     const int F = *Fp;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int r = threadIdx.x % kReorthLanes;
+    const int64_t groups = (int64_t)gridDim.x * (blockDim.x / kReorthLanes);
+    const int64_t g0 = (int64_t)blockIdx.x * (blockDim.x / kReorthLanes) + threadIdx.x / kReorthLanes;
+    // every lane of a warp runs the same number of iterations (the shuffles
+    // need all 32): lanes past the end sum nothing and write nothing
+    const int64_t iters = (n + groups - 1) / groups;
+    for (int64_t t = 0; t < iters; ++t) {
+        const int64_t i = g0 + t * groups;
         i128 acc = 0;
-        for (int k = 0; k < nk; ++k) acc += mul_wide(rt[k], basis[(int64_t)k * stride + i]) >> rs[k];
-        w[i] -= (int64_t)shr_round(acc, F);
+        if (i < n)
+            for (int k = r; k < nk; k += kReorthLanes) acc += mul_wide(rt[k], basis[(int64_t)k * stride + i]) >> rs[k];
+#pragma unroll
+        for (int o = 1; o < kReorthLanes; o <<= 1) {
+            const uint64_t lo = __shfl_xor_sync(0xffffffffu, (uint64_t)acc, o);
+            const uint64_t hi = __shfl_xor_sync(0xffffffffu, (uint64_t)((u128)acc >> 64), o);
+            acc += (i128)(((u128)hi << 64) | lo);
+        }
+        if (i < n && r == 0) w[i] -= (int64_t)shr_round(acc, F);
     }
 }
 
@@ -653,9 +672,9 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
                 // row chunks per dot: up to kDotChunks, ~2048 elements each
                 // (exact integer sums: the split does not change them)
                 const int chunks = (int)std::min<int64_t>(kDotChunks, std::max<int64_t>(1, (DW + 2047) / 2048));
-                // the update sums nk basis vectors per element: one element
-                // per thread, so that small sectors still fill the GPU
-                const int grr = (int)std::min<int64_t>(152 * 8, (DW + kLzThreads - 1) / kLzThreads);
+                // the update sums nk basis vectors per element: four lanes
+                // per element, so that small sectors still fill the GPU
+                const int grr = (int)std::min<int64_t>(152 * 8, (DW * kReorthLanes + kLzThreads - 1) / kLzThreads);
                 for (int pass = 0; pass < 2; ++pass) {
                     dim3 g(nk, chunks);
                     k_lz_dots<<<g, kLzThreads, 0, s>>>(w->basis, DW, w->stride, slot(j + 1), w->dot_lo, w->dot_hi);
