@@ -78,12 +78,15 @@ def build_oracle() -> Path:
     r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle")], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    ref_root = os.environ.get("ED_REFERENCE_ROOT", "/root/reference")
-    if Path(ref_root, "MBL_test", "include", "fermi_operator.h").exists():
-        r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF_ROOT={ref_root}"],
-                           capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"reference table dumper build failed:\n{r.stdout}\n{r.stderr}")
+    # the recipe knows where the reference checkout lies (REF_ROOT, or the
+    # environment's ED_REFERENCE_ROOT) and skips the reference targets when it
+    # is absent
+    cmd = ["make", "-s", "-C", str(ROOT / "oracle"), "ref-if-present"]
+    if os.environ.get("ED_REFERENCE_ROOT"):
+        cmd.append(f"REF_ROOT={os.environ['ED_REFERENCE_ROOT']}")
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference table dumper build failed:\n{r.stdout}\n{r.stderr}")
     return ROOT / "oracle" / "_build" / "liboracle.so"
 
 

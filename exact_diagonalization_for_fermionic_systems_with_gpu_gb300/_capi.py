@@ -11,6 +11,8 @@ from pathlib import Path
 _LIB = None
 
 ED_OK = 0
+ED_ERR_ARG, ED_ERR_CUDA, ED_ERR_ALLOC, ED_ERR_TABLE, ED_ERR_RANGE = 1, 2, 3, 4, 5
+ED_ERR_NONFINITE, ED_ERR_BREAKDOWN, ED_ERR_NOT_CONVERGED, ED_ERR_TIMEOUT, ED_ERR_NOT_BUILT = 6, 7, 8, 9, 10
 STATUS_NAMES = {
     0: "ED_OK", 1: "ED_ERR_ARG", 2: "ED_ERR_CUDA", 3: "ED_ERR_ALLOC", 4: "ED_ERR_TABLE",
     5: "ED_ERR_RANGE", 6: "ED_ERR_NONFINITE", 7: "ED_ERR_BREAKDOWN", 8: "ED_ERR_NOT_CONVERGED",

@@ -640,7 +640,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             }
             unsigned int* taken = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(w->gbar) + 160);
             LzFusedArgs fa{w->basis, w->stride, stored ? 1 : 0, j, j1, w->u, DW, lz, w->gbar, red, taken,
-                           stamps ? w->stamps : nullptr, stamps ? w->cta_stamps : nullptr};
+                           stamps ? w->stamps : nullptr, stamps ? w->cta_stamps : nullptr, grid_wait_limits()};
             if (stamps) LZ_CK(cudaEventRecord(w->events[2 * n_fused], s));
             const cudaError_t e = launch_lz_fused(op, fa, s);
             if (e == cudaSuccess && stamps) LZ_CK(cudaEventRecord(w->events[2 * n_fused + 1], s));
@@ -1021,7 +1021,8 @@ ed_status lanczos_batch_run(ed_op* const* ops, int B, const ed_lanczos_cfg* cfg,
             le = cudaMemcpyAsync(dinst, inst.data() + b0, sizeof(LzInst) * Bn, cudaMemcpyHostToDevice, s);
         if (le == cudaSuccess) {
             LzBatchArgs fa{dinst, Bn, 0, max_steps, ws[0]->stride, DW, reinterpret_cast<unsigned int*>(sync),
-                           reinterpret_cast<LzRedSet*>(sync + 128), reinterpret_cast<unsigned int*>(sync + 64)};
+                           reinterpret_cast<LzRedSet*>(sync + 128), reinterpret_cast<unsigned int*>(sync + 64),
+                           grid_wait_limits()};
             le = launch_lz_batch(op0, fa, s);
         }
         cudaFreeAsync(sync, s);

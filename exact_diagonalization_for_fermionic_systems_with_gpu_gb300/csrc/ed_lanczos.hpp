@@ -47,6 +47,19 @@ struct LzRedSet {
 };
 
 // Arguments of the persistent Lanczos kernel (steps j0 .. j1-1 in one launch).
+// Limits of the persistent kernels' grid-barrier waits: a CTA gives up after
+// `spin` polls or `ns` nanoseconds of %globaltimer, whichever comes first.
+// `extra` > 0 makes every barrier wait for that many arrivals more than the
+// grid has, so that the wait runs out (the error path's test).
+struct GridWait {
+    long long spin;
+    unsigned long long ns;
+    unsigned int extra;
+};
+
+// Defaults (2^26 polls, 4 s), or ED_GRID_WAIT="<ns>[,<extra arrivals>]".
+GridWait grid_wait_limits();
+
 struct LzFusedArgs {
     int64_t* basis;
     int64_t stride;      // slot stride in elements
@@ -62,6 +75,7 @@ struct LzFusedArgs {
                                  // points of every step (see ed_lanczos_fused.cu)
     unsigned long long* cta_stamps;  // optional: every CTA's rows-done and axpy-done
                                      // times, [step][2][gridDim.x]
+    GridWait wait;
 };
 
 // One instance of a batched run (k_lz_batch): instances share the hopping
@@ -94,6 +108,7 @@ struct LzBatchArgs {
     unsigned int* gbar;    // grid-barrier arrivals, zero at launch
     LzRedSet* red;         // 4 * B accumulator sets (set r % 4 of instance b at (r % 4) * B + b), zero at launch
     unsigned int* taken;   // two item-queue counters (step parity), zero at launch
+    GridWait wait;
 };
 
 }  // namespace ed

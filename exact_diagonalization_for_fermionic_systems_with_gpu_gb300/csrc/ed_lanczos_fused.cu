@@ -32,11 +32,15 @@
 // Vectors written during the launch are read back with L2 (coherent) loads,
 // and before the bulk copies of a row written by another CTA the issuing
 // thread orders them behind the grid barrier with a proxy fence.
-// Grid barriers are bounded (poll count and %globaltimer): a CTA that gives
-// up sets *err and leaves; the host then reports ED_ERR_TIMEOUT.
+// Grid barriers are bounded (poll count and %globaltimer, limits in
+// GridWait): a CTA that gives up sets *err and leaves; the host then reports
+// ED_ERR_TIMEOUT.  No bulk copy is in flight at a grid barrier (a CTA's row
+// copies all land before its rows are done), so leaving there is safe.
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 
 #include "ed_lanczos.hpp"
 #include "ed_lanczos_dev.cuh"
@@ -47,8 +51,6 @@ using namespace dev;
 
 namespace {
 
-constexpr long long kGridSpin = 1LL << 26;
-constexpr unsigned long long kGridWaitNs = 4000000000ULL;  // 4 s
 constexpr uint64_t kLimb = (1ULL << 42) - 1;
 
 __device__ __forceinline__ unsigned int ld_relaxed_gpu(const unsigned int* p) {
@@ -89,7 +91,8 @@ __device__ __forceinline__ void red_pull(const LzRedSet* r, i128& v, uint64_t& m
 // launch completes when k * gridDim.x CTAs have arrived.  Writes and atomics
 // before it (by any thread of any CTA) are visible after it.  False when the
 // wait gave up; *give_up is then set for the whole CTA.
-__device__ __forceinline__ bool grid_sync(unsigned int* gbar, unsigned int& target, int* give_up, int* err) {
+__device__ __forceinline__ bool grid_sync(unsigned int* gbar, unsigned int& target, int* give_up, int* err,
+                                          const GridWait& lim) {
     __syncthreads();
     if (threadIdx.x == 0) {
         target += gridDim.x;
@@ -97,9 +100,10 @@ __device__ __forceinline__ bool grid_sync(unsigned int* gbar, unsigned int& targ
         // by the CTA barrier above) before the arrival
         red_release_gpu_add(gbar, 1u);
         const unsigned long long t0 = global_ns();
+        const unsigned int want = target + lim.extra;
         long long it = 0;
-        while (ld_relaxed_gpu(gbar) < target) {
-            if (++it > kGridSpin || global_ns() - t0 > kGridWaitNs) {
+        while (ld_relaxed_gpu(gbar) < want) {
+            if (++it > lim.spin || global_ns() - t0 > lim.ns) {
                 atomicExch(err, 1);
                 *give_up = 1;
                 break;
@@ -185,7 +189,12 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
         give_up = 1;
     }
     __syncthreads();
-    if (give_up) return;  // no row copy has been issued yet
+    if (give_up) {
+        // the table copy is the only one in flight (rows are issued in the
+        // step loop): wait for it once more (bounded) before leaving
+        if (tid == 0) tma::mbar_wait(&S.bar[2], 0);
+        return;
+    }
 
     auto slot = [&](int j) -> int64_t* {
         return f.basis + (size_t)(f.stored ? j : j % 3) * (size_t)f.stride;
@@ -234,7 +243,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
             if (tid == 0) red_push(&f.red[rM % 4], dot, mx);
             if (stamp) st[2] = global_ns();
         }
-        if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
+        if (!grid_sync(f.gbar, target, &give_up, a.err, f.wait)) return;
         if (tid == 0) {
             if (stamp) st[3] = global_ns();
             i128 s;
@@ -306,7 +315,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
         }
         // a data barrier: the next matvec gathers w_{j+1} from every CTA; the
         // norm and max of w_{j+1} are read at the next step's reduction
-        if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
+        if (!grid_sync(f.gbar, target, &give_up, a.err, f.wait)) return;
         if (tid == 0) {
             if (blockIdx.x == 0 && rA >= 2) f.red[(rA - 2) % 4] = LzRedSet{0, 0, 0, 0};
             if (stamp) st[7] = st[8] = global_ns();
@@ -400,7 +409,12 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
         give_up = 1;
     }
     __syncthreads();
-    if (give_up) return;  // no row copy has been issued yet
+    if (give_up) {
+        // the table copy is the only one in flight (rows are issued in the
+        // step loop): wait for it once more (bounded) before leaving
+        if (tid == 0) tma::mbar_wait(&S.bar[2], 0);
+        return;
+    }
 
     uint32_t rc = 0;          // rows streamed through the row buffers
     unsigned int target = 0;  // grid-barrier arrivals expected so far
@@ -459,7 +473,12 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
                 }
                 __syncthreads();
                 if (give_up) {
-                    if (tid == 0 && issued_next) tma::mbar_wait(&S.bar[buf ^ 1], ((rc + 1) >> 1) & 1);
+                    // this item's copy (once more) and the next item's must
+                    // land before the CTA leaves (bounded waits)
+                    if (tid == 0) {
+                        tma::mbar_wait(&S.bar[buf], parity);
+                        if (issued_next) tma::mbar_wait(&S.bar[buf ^ 1], ((rc + 1) >> 1) & 1);
+                    }
                     return;
                 }
                 const uint32_t r_next = s_next;
@@ -555,7 +574,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
             accl[tid][0] = accl[tid][1] = accl[tid][2] = 0;
             accm[tid] = 0;
         }
-        if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
+        if (!grid_sync(f.gbar, target, &give_up, a.err, f.wait)) return;
         if (tid < B) {
             const int b = tid;
             LzState* lz = f.inst[b].lz;
@@ -634,7 +653,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
             accl[tid][0] = accl[tid][1] = accl[tid][2] = 0;
             accm[tid] = 0;
         }
-        if (!grid_sync(f.gbar, target, &give_up, a.err)) return;
+        if (!grid_sync(f.gbar, target, &give_up, a.err, f.wait)) return;
         if (tid < B && blockIdx.x == 0) {
             const int b = tid;
             if (rA >= 2) f.red[((rA - 2) % 4) * B + b] = LzRedSet{0, 0, 0, 0};
@@ -669,6 +688,19 @@ cudaError_t launch_lz_batch(const ed_op* op, const LzBatchArgs& f, cudaStream_t 
     void* args[] = {&av, &fv};
     return cudaLaunchCooperativeKernel(fn, dim3((unsigned)op->tma_grid), dim3(kTmaThreads), args,
                                        (size_t)op->tma_smem, s);
+}
+
+GridWait grid_wait_limits() {
+    GridWait w{1LL << 26, 4000000000ULL, 0u};
+    if (const char* v = std::getenv("ED_GRID_WAIT")) {
+        unsigned long long ns = 0;
+        unsigned int extra = 0;
+        if (std::sscanf(v, "%llu,%u", &ns, &extra) >= 1 && ns > 0) {
+            w.ns = ns;
+            w.extra = extra;
+        }
+    }
+    return w;
 }
 
 // Cooperative launch of steps j0 .. j1-1; cudaErrorNotSupported when the

@@ -99,7 +99,12 @@ __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g
             give_up = 1;
         }
         __syncthreads();
-        if (give_up) return;  // the copy this CTA waited for has given up; none other is in flight
+        if (give_up) {
+            // the window copy (the only one in flight) must land before the
+            // CTA leaves: wait for it once more (bounded)
+            if (tid == 0) tma::mbar_wait(&bar, phase);
+            return;
+        }
         // two columns per iteration (c and c + 1024): their schedule words are
         // loaded together, kDownBatch steps of each in flight
         for (int64_t c = c0 + tid; c < c1; c += 2 * kDownThreads) {

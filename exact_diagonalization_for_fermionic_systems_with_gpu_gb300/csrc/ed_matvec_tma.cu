@@ -53,8 +53,11 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_matvec_tma(const MvArgs a) {
     uint32_t rc = 0;
     if (!give_up) {
         tma_rows<CPLX, OUT, FAST, false, SCHED, false, SEG>(a, S, a.xq, a.uq, a.y, rc, E_out, s_u, dot, mx);
-    } else if (threadIdx.x == 0 && has_row) {
-        tma::mbar_wait(&S.bar[0], 0);  // the first row copy must land before the CTA exits
+    } else if (threadIdx.x == 0) {
+        // the table copy (the wait that gave up, once more) and the first row
+        // copy must land before the CTA exits (bounded waits)
+        tma::mbar_wait(&S.bar[2], 0);
+        if (has_row) tma::mbar_wait(&S.bar[0], 0);
     }
     if (OUT == 1) mv_lanczos_epilogue(a, dot, mx, s_u);
 }

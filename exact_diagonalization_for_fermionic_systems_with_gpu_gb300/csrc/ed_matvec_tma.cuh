@@ -300,9 +300,14 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
         }
         __syncthreads();
         if (*S.give_up) {
-            // the copy issued for the next row must land before the CTA
-            // moves on (bounded)
-            if (tid == 0 && issued_next) tma::mbar_wait(&S.bar[buf ^ 1], ((rc + 1) >> 1) & 1);
+            // every copy still counted on a barrier must land before the CTA
+            // leaves and its shared memory is reassigned: the current row's
+            // (the wait that gave up, once more) and the next row's, each
+            // wait bounded; if one gives up again the rows are undefined
+            if (tid == 0) {
+                tma::mbar_wait(&S.bar[buf], parity);
+                if (issued_next) tma::mbar_wait(&S.bar[buf ^ 1], ((rc + 1) >> 1) & 1);
+            }
             return;
         }
         const uint32_t r_next = DYN ? *snext : r + 1;  // written by thread 0 before the barrier above

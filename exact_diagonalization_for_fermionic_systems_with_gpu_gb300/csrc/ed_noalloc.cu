@@ -9,9 +9,14 @@
 // scratch from the file-scope array below instead.
 //
 // Scratch: kNoAllocMaxElems int64 values (16 MiB) plus two ints, resident on
-// every GPU that loads this library until the process exits.  Operators with
-// more than kNoAllocMaxElems stored values (rows, or 2*rows when complex) are
-// rejected with ED_ERR_RANGE.
+// a GPU from the first call on it until the process exits.  Under CUDA's
+// lazy module loading the array's module is loaded, and its 16 MiB reserved,
+// when the first call resolves the array's address: a caller whose allocator
+// will reserve the whole device makes that first call before it does (an
+// out-of-memory failure there returns ED_ERR_ALLOC).  Operators with more than
+// kNoAllocMaxElems stored values (rows, or 2*rows when complex) are rejected
+// with ED_ERR_RANGE.  Non-finite input is not detected here (the flag word is
+// shared and cleared by the next call): y is undefined for such x.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -46,8 +51,12 @@ ed_status resolve(int device, Resolved* out) {
     if (!r.ready) {
         void* p = nullptr;
         void* q = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_xq) != cudaSuccess) return ED_ERR_CUDA;
-        if (cudaGetSymbolAddress(&q, g_noalloc_words) != cudaSuccess) return ED_ERR_CUDA;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_xq);
+        if (e == cudaSuccess) e = cudaGetSymbolAddress(&q, g_noalloc_words);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return e == cudaErrorMemoryAllocation ? ED_ERR_ALLOC : ED_ERR_CUDA;
+        }
         r.xq = static_cast<int64_t*>(p);
         r.words = static_cast<int*>(q);
         r.ready = true;

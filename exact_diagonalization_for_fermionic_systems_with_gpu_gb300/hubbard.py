@@ -316,14 +316,15 @@ class Lanczos:
 
 
 def lanczos_batch(ops: Sequence[Hubbard], max_steps: int, seed: int = 0, starts: Optional[np.ndarray] = None,
-                  ritz: bool = True, evec_out=None):
+                  ritz: bool = True, evec_out=None, results: Optional[list] = None):
     """ed_lanczos_batch: fixed-step Lanczos of up to 8 operators that share
     their hopping tables (one sector, disorder in the on-site terms) in one
     persistent launch.  Run b starts from Philox(seed + b) or starts[b]
     (a numpy array or a float64 CUDA tensor, (B, rows)).
     Returns (e0 [B], evecs, alpha [B, max_steps], beta [B, max_steps + 1]):
     evecs a (B, rows) numpy array, or evec_out (a (B, rows) float64 CUDA
-    tensor) when given, or None without ritz."""
+    tensor) when given, or None without ritz.  A list passed as results
+    receives the B ed_lanczos_result records (min_bits, launches, ...)."""
     lib = _capi.load()
     B = len(ops)
     n = ops[0].rows()
@@ -356,5 +357,7 @@ def lanczos_batch(ops: Sequence[Hubbard], max_steps: int, seed: int = 0, starts:
     res = (_capi.ed_lanczos_result * B)()
     check(lib.ed_lanczos_batch(handles, B, C.byref(cfg), st_ptr, st_mem, ev_ptr, ev_mem, _ptr(alpha), _ptr(beta),
                                res, None), "ed_lanczos_batch")
+    if results is not None:
+        results.extend(res)
     return np.array([r.e0 for r in res]), evecs, alpha, beta
 

@@ -50,6 +50,8 @@ class FluxPoint:
     d1: float          # dE0/dPhi
     d2: float          # d2E0/dPhi2
     steps: int         # Lanczos steps of the ground-state run
+    min_bits: int = 0  # fewest significant bits a Lanczos vector kept (fixed-point solver)
+    err_vs_oracle: float = float("nan")  # |E0 - E0 of the FP64 oracle|, where one is given
 
 
 @dataclass
@@ -62,6 +64,8 @@ class MblPoint:
     n_up: np.ndarray   # dE0/d eps_{i,up}
     n_dn: np.ndarray   # dE0/d eps_{i,dn}
     steps: int
+    min_bits: int = 0
+    err_vs_oracle: float = float("nan")
 
 
 @dataclass
@@ -89,13 +93,13 @@ def _sync():
 
 
 def _ground(H: Hubbard, steps: int, mode: str, seed: int):
-    """(E0, Ritz vector as a CUDA tensor, steps taken)."""
+    """(E0, Ritz vector as a CUDA tensor, steps taken, min_bits)."""
     import torch
     dt = torch.complex128 if H.is_complex else torch.float64
     evec = torch.empty(H.rows(), dtype=dt, device="cuda")
     lz = Lanczos()
     e0, _ = lz.eigen(H, max_steps=steps, mode=mode, ritz="stored", seed=seed, evec_out=evec)
-    return e0, evec, int(lz.result.steps)
+    return e0, evec, int(lz.result.steps), int(lz.result.min_bits)
 
 
 def flux_phis(n_phi: int = 16) -> np.ndarray:
@@ -130,7 +134,7 @@ def flux_sweep(phis: Optional[Sequence[float]] = None, n_up: int = 6, n_dn: int 
         d2H = Hubbard(H_TBq(12, n_up).extend(d2t), H_TBq(12, n_dn).extend(d2t), 0.0)
         _sync()
         tb = time.perf_counter()
-        e0, psi, n = _ground(H, steps, mode, seed * 4096 + k)
+        e0, psi, n, bits = _ground(H, steps, mode, seed * 4096 + k)
         _sync()
         tl = time.perf_counter()
         d1, d2 = ob.response(H, dH, d2H, psi, e0, steps=response_steps)
@@ -138,7 +142,7 @@ def flux_sweep(phis: Optional[Sequence[float]] = None, n_up: int = 6, n_dn: int 
         te = time.perf_counter()
         for op in (H, dH, d2H):
             op.close()
-        out.append(FluxPoint(float(phi), e0, d1, d2, n))
+        out.append(FluxPoint(float(phi), e0, d1, d2, n, bits))
         t.instances += 1
         t.lanczos_steps += n
         t.build_s += tb - ti
@@ -194,22 +198,26 @@ def _mbl_batched(reals, sectors, n_sites, W, U, steps, seed, a_sites, batch, t) 
                 lib.ed_random_vector_device(n, seed * (1 << 20) + r * len(sectors) + s,
                                             C.c_void_p(starts[b].data_ptr()), None)
             evecs = torch.empty_like(starts)
+            results: list = []
             try:
-                e0s, _, _, _ = lanczos_batch(ops, steps, starts=starts, evec_out=evecs)
+                e0s, _, _, _ = lanczos_batch(ops, steps, starts=starts, evec_out=evecs, results=results)
+                bits = [int(r.min_bits) for r in results]
             except EdError:
-                e0s = []
+                e0s, bits = [], []
                 for b, op in enumerate(ops):
                     lz = Lanczos()
                     e, _ = lz.eigen(op, max_steps=steps, mode="fixed", ritz="stored",
                                     f=starts[b].cpu().numpy(), evec_out=evecs[b])
                     e0s.append(e)
+                    bits.append(int(lz.result.min_bits))
             _sync()
             tl = time.perf_counter()
             # the group's entropies in one batched call (its blocks fill the GPU together)
             svns, srefs = ob.entanglement_entropy_batch(ops[0], evecs, a_sites)
             for b, r in enumerate(group):
                 nu, nd, _ = ob.site_densities(ops[b], evecs[b])
-                out.append(MblPoint(int(r), (qu, qd), float(e0s[b]), float(svns[b]), float(srefs[b]), nu, nd, steps))
+                out.append(MblPoint(int(r), (qu, qd), float(e0s[b]), float(svns[b]), float(srefs[b]), nu, nd, steps,
+                                    bits[b]))
             _sync()
             te = time.perf_counter()
             for op in ops:
@@ -247,7 +255,7 @@ def mbl_sweep(n_real: int = 64, sectors: Sequence[Tuple[int, int]] = MBL_SECTORS
             H = Hubbard(H_TBq(n_sites, qu).extend(tu), H_TBq(n_sites, qd).extend(td), U)
             _sync()
             tb = time.perf_counter()
-            e0, psi, n = _ground(H, steps, mode, seed * (1 << 20) + r * len(sectors) + s)
+            e0, psi, n, bits = _ground(H, steps, mode, seed * (1 << 20) + r * len(sectors) + s)
             _sync()
             tl = time.perf_counter()
             nu, nd, _ = ob.site_densities(H, psi)
@@ -255,7 +263,7 @@ def mbl_sweep(n_real: int = 64, sectors: Sequence[Tuple[int, int]] = MBL_SECTORS
             _sync()
             te = time.perf_counter()
             H.close()
-            out.append(MblPoint(int(r), (qu, qd), e0, svn, sref, nu, nd, n))
+            out.append(MblPoint(int(r), (qu, qd), e0, svn, sref, nu, nd, n, bits))
             t.instances += 1
             t.lanczos_steps += n
             t.build_s += tb - ti
@@ -266,44 +274,73 @@ def mbl_sweep(n_real: int = 64, sectors: Sequence[Tuple[int, int]] = MBL_SECTORS
     return out
 
 
+def attach_oracle(points, oracle_e0) -> float:
+    """Set err_vs_oracle = |E0 - oracle_e0[key]| on the points the table
+    covers (key: round(Phi, 12) for twist points, (realisation, (N_up, N_dn))
+    for disorder points); returns the largest such error (nan if none)."""
+    worst = float("nan")
+    for p in points:
+        key = round(p.phi, 12) if isinstance(p, FluxPoint) else (p.realisation, tuple(p.sector))
+        if key in oracle_e0:
+            p.err_vs_oracle = abs(p.e0 - float(oracle_e0[key]))
+            worst = p.err_vs_oracle if not worst >= p.err_vs_oracle else worst
+    return worst
+
+
 def flux_rows(points: Sequence[FluxPoint]):
-    """Rows (Phi, E0, dE0/dPhi, d2E0/dPhi2) for datio.append_rows."""
-    return [(p.phi, p.e0, p.d1, p.d2) for p in points]
+    """Rows (Phi, E0, dE0/dPhi, d2E0/dPhi2, min_bits, |E0 - E0_oracle|) for
+    datio.append_rows (nan where no oracle value was attached)."""
+    return [(p.phi, p.e0, p.d1, p.d2, p.min_bits, p.err_vs_oracle) for p in points]
 
 
 def mbl_rows(points: Sequence[MblPoint]):
-    """Rows (realisation, N_up, N_dn, E0, S_vN, n_up[0..L-1], n_dn[0..L-1])."""
+    """Rows (realisation, N_up, N_dn, E0, S_vN, n_up[0..L-1], n_dn[0..L-1],
+    min_bits, |E0 - E0_oracle|)."""
     return [(p.realisation, p.sector[0], p.sector[1], p.e0, p.s_vn) + tuple(p.n_up) + tuple(p.n_dn)
-            for p in points]
+            + (p.min_bits, p.err_vs_oracle) for p in points]
 
 
-FLUX_HEADER = "#       Phi       E0        dE0/dPhi        d2E0/dPhi2      "
-MBL_HEADER = "#       xid       Nup       Ndn       E0        S_A       n_up(i)...      n_dn(i)...      "
+FLUX_HEADER = "#       Phi       E0        dE0/dPhi        d2E0/dPhi2      min_bits        err_vs_oracle   "
+MBL_HEADER = ("#       xid       Nup       Ndn       E0        S_A       n_up(i)...      n_dn(i)...      "
+              "min_bits        err_vs_oracle   ")
 
 
 # The plain per-instance GPU form the tuned sweep is compared with: the
 # generic matvec kernel, host-driven per-step Lanczos launches, and one
 # cusolverDnDgesvd per entanglement block on one stream.
 PLAIN_ENV = {"ED_MATVEC": "generic", "ED_LZ_FUSED": "0", "ED_EE_METHOD": "gesvd", "ED_EE_STREAMS": "1"}
+# The same plain Lanczos form with the tuned entanglement path (cluster
+# bidiagonalisation), so that a comparison shows what batching, the
+# persistent kernel and the row engine buy on their own.
+PLAIN_SAME_EE_ENV = {"ED_MATVEC": "generic", "ED_LZ_FUSED": "0"}
+FORM_ENV = {"tuned": {}, "plain": PLAIN_ENV, "plain_same_ee": PLAIN_SAME_EE_ENV}
 
 
-def _run(a, n, form: str):
+def run_form(what: str, n: int, form: str, steps: int = 300, mode: str = "fixed", seed: int = 0, warmup: int = 1,
+             batch: int = 8):
+    """One sweep (what = "flux" | "mbl") in one form of FORM_ENV: the tuned
+    form autotunes the twist operators and batches disorder realisations,
+    the plain forms run one instance per launch sequence.  Returns
+    (points, SweepTiming)."""
     import os
-    saved = {k: os.environ.get(k) for k in PLAIN_ENV}
-    if form == "plain":
-        os.environ.update(PLAIN_ENV)
+    env = FORM_ENV[form]
+    keys = set(PLAIN_ENV) | set(env)
+    saved = {k: os.environ.get(k) for k in keys}
+    for k in keys:
+        os.environ.pop(k, None)
+    os.environ.update(env)
     try:
         tm = SweepTiming()
-        if a.what == "flux":
+        if what == "flux":
             tune = form == "tuned"
-            if a.warmup:
-                flux_sweep(flux_phis(n)[: a.warmup], steps=a.steps, mode=a.mode, seed=a.seed, autotune=tune)
-            pts = flux_sweep(flux_phis(n), steps=a.steps, mode=a.mode, seed=a.seed, timing=tm, autotune=tune)
+            if warmup:
+                flux_sweep(flux_phis(n)[:warmup], steps=steps, mode=mode, seed=seed, autotune=tune)
+            pts = flux_sweep(flux_phis(n), steps=steps, mode=mode, seed=seed, timing=tm, autotune=tune)
         else:
-            bt = a.batch if form == "tuned" else 1
-            if a.warmup:
-                mbl_sweep(realisations=range(max(a.warmup, bt)), steps=a.steps, mode=a.mode, seed=a.seed + 1, batch=bt)
-            pts = mbl_sweep(n, steps=a.steps, mode=a.mode, seed=a.seed, timing=tm, batch=bt)
+            bt = batch if form == "tuned" else 1
+            if warmup:
+                mbl_sweep(realisations=range(max(warmup, bt)), steps=steps, mode=mode, seed=seed + 1, batch=bt)
+            pts = mbl_sweep(n, steps=steps, mode=mode, seed=seed, timing=tm, batch=bt)
     finally:
         for k, v in saved.items():
             if v is None:
@@ -311,6 +348,10 @@ def _run(a, n, form: str):
             else:
                 os.environ[k] = v
     return pts, tm
+
+
+def _run(a, n, form: str):
+    return run_form(a.what, n, form, steps=a.steps, mode=a.mode, seed=a.seed, warmup=a.warmup, batch=a.batch)
 
 
 def main(argv: Optional[Sequence[str]] = None) -> None:
@@ -324,9 +365,10 @@ def main(argv: Optional[Sequence[str]] = None) -> None:
     ap.add_argument("--out", default=None, help="append the result rows to this .dat file")
     ap.add_argument("--batch", type=int, default=8,
                     help="disorder realisations per Lanczos launch in the tuned form (1: one launch per run)")
-    ap.add_argument("--form", choices=["tuned", "plain", "compare"], default="tuned",
-                    help="plain: the per-instance form of PLAIN_ENV; compare: both, with the largest "
-                         "differences of their outputs")
+    ap.add_argument("--form", choices=["tuned", "plain", "plain_same_ee", "compare"], default="tuned",
+                    help="plain: the per-instance form of PLAIN_ENV; plain_same_ee: the same with the tuned "
+                         "entanglement path; compare: tuned and plain, with the largest differences of their "
+                         "outputs")
     a = ap.parse_args(argv)
     import torch
     if not torch.cuda.is_available():
@@ -350,8 +392,8 @@ def main(argv: Optional[Sequence[str]] = None) -> None:
             "ms_per_instance_median": round(1e3 * float(np.median(tm.per_instance)), 3)}
     if a.form == "compare":
         p_pts, p_tm = runs["plain"]
-        diff = np.abs(np.array(rows, dtype=float) -
-                      np.array(flux_rows(p_pts) if a.what == "flux" else mbl_rows(p_pts), dtype=float))
+        diff = np.abs(np.array(rows, dtype=float)[:, :-2] -
+                      np.array(flux_rows(p_pts) if a.what == "flux" else mbl_rows(p_pts), dtype=float)[:, :-2])
         line["plain"] = p_tm.summary()
         line["speedup_vs_plain"] = round(p_tm.total_s / tm.total_s, 3)
         line["max_abs_diff_vs_plain"] = {"E0": float(np.max(diff[:, 1 if a.what == "flux" else 3])),

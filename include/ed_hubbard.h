@@ -157,13 +157,18 @@ ed_status ed_op_perform(ed_op* op, const double* x, double* y, int mem, void* st
  * cudaFree may cause.  Same result and argument meaning as ed_op_perform with
  * ED_MEM_DEVICE (x, y device pointers, asynchronous on stream, y
  * overwritten), but the int64 copy of x lives in a fixed static device array
- * of 2^21 values (16 MiB, held on every GPU that loads this library until the
+ * of 2^21 values (16 MiB, held on a GPU from the first call there until the
  * process exits): operators with more than 2^21 stored values (rows, or
  * 2*rows for complex operators) return ED_ERR_RANGE.  The first call on a
- * device resolves the array's device address (cudaGetSymbolAddress), so make
- * that first call before any stream capture.  All calls share the one array
- * and it keeps the last call's contents: calls that overlap on the GPU (other
- * streams, other threads, other operators on the same device) race. */
+ * device resolves the array's device address (cudaGetSymbolAddress), which
+ * under CUDA's lazy module loading also loads the module holding the array
+ * and so reserves its 16 MiB: make that first call before any stream capture
+ * and before another allocator reserves the device (ED_ERR_ALLOC if the
+ * reservation fails).  All calls share the one array and it keeps the last
+ * call's contents: calls that overlap on the GPU (other streams, other
+ * threads, other operators on the same device) race.  NaN or Inf in x is not
+ * detected by this entry (ED_OK is returned and y is undefined); use
+ * ed_op_perform where that check is wanted. */
 ed_status ed_op_perform_noalloc(ed_op* op, const double* x, double* y, void* stream);
 
 /* ---------------------------------------------------------------- Lanczos -- */

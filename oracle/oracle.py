@@ -146,6 +146,30 @@ def mask_all(N: int) -> int:
     return (1 << N) - 1
 
 
+# KagomeLattice12, DrudeWeight/src/drude_v2_cal_Kagome_randomHop.cu:794-808:
+# Make_H(first[b], second[b], -r_i r_j) on the 24 bonds (lists :796-797), then
+# Make_N(i, -2 r_i^2) on every site.  Restated here so that the CPU baseline
+# builds the workload without the product package.
+_KAGOME12_FIRST = (0, 1, 3, 4, 6, 7, 9, 10, 0, 2, 6, 8, 3, 5, 9, 11, 2, 1, 8, 7, 5, 4, 11, 10)
+_KAGOME12_SECOND = (1, 3, 4, 0, 7, 9, 10, 6, 2, 6, 8, 0, 5, 9, 11, 3, 1, 11, 7, 5, 4, 8, 10, 2)
+
+
+def kagome12_terms() -> List[tuple]:
+    """The uniform (r_i = 1) KagomeLattice12 term list."""
+    terms = [("H", i, j, -1.0, 0.0) for i, j in zip(_KAGOME12_FIRST, _KAGOME12_SECOND)]
+    return terms + [("N", i, 0, -2.0, 0.0) for i in range(12)]
+
+
+def philox_uniform(seed: int, n: int, scale: float = 1.0) -> np.ndarray:
+    """scale * uniform(-1, 1) from numpy's Philox4x64-10 keyed by (seed, 0):
+    the 52 high mantissa bits of each raw 64-bit word give a double in [1, 2),
+    mapped to 2u - 3.  The library's counter-based start vector produces the
+    same doubles."""
+    bg = np.random.Philox(key=np.array([seed, 0], dtype=np.uint64))
+    r = bg.random_raw(n)
+    return scale * (((r >> np.uint64(12)) | np.uint64(0x3FF0000000000000)).view(np.float64) * 2.0 - 3.0)
+
+
 def matvec(up: Tables, dn: Tables, U: float, x: np.ndarray, mask: int | None = None) -> np.ndarray:
     """Restated Hubbard_mv_ (HubMatrix_GPU.cuh:114-161) on the CPU."""
     lib = load()

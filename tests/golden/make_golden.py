@@ -6,12 +6,25 @@ the reference's own MBL_test/include/fermi_operator.h into
 oracle/_ref/ref_tables):
 
     make -C oracle ref && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --flux     (flux fixtures only; no
+                                                   reference build needed)
+    python tests/golden/make_golden.py --sweep    (disorder-sweep instances)
 
 Outputs
   tables_small.npz   reference H_TBq state/Ax/Aj arrays for small cases
   tables_digest.json sha256 digests of the reference tables for large cases
   energies.json      ground-state energies (dense or scipy eigsh on the
                      reference tables) and entanglement entropies
+  flux_kagome12_q66_U4.json
+                     the twisted Kagome12 6+6, U=4 sector at three of the
+                     sixteen twists Phi_k = (2 pi / 4) k / 15: E0 and E1
+                     (scipy eigsh on the oracle's Kronecker-sum Hamiltonian
+                     with the Peierls phases), dE0/dPhi = <psi|H'|psi> and
+                     d2E0/dPhi2 = <psi|H''|psi> - 2 <b|(H - E0)^+|b>,
+                     b = Q H' psi, from a projected conjugate-gradient solve
+  sweep_chain12_W6.json
+                     E0 of the first disorder realisations of the L=12 chain
+                     sweep in its three sectors (scipy eigsh)
 """
 from __future__ import annotations
 
@@ -136,5 +149,85 @@ def main() -> None:
     print(json.dumps(en, indent=1))
 
 
+def flux_fixtures(ks=(0, 7, 15), n_phi: int = 16) -> dict:
+    """E0, E1, dE0/dPhi, d2E0/dPhi2 of Kagome12 6+6, U=4 with the twist
+    phase Phi * dx_b on every bond (KagomeCurrent12's x projections,
+    drude_v2_cal_Kagome_randomHop.cu:849-851), on the CPU."""
+    import math
+    import scipy.sparse.linalg as sla
+    out = {"lattice": "Kagome12 (KagomeLattice12 incl. -2 r^2 on-site), r_i = 1", "n_up": 6, "n_dn": 6, "U": 4.0,
+           "phi_k": "(2 pi / KAGOME12_LX) * k / 15, KAGOME12_LX = 4", "points": []}
+    for k in ks:
+        t0 = time.time()
+        phi = (2.0 * math.pi / L.KAGOME12_LX) * k / (n_phi - 1)
+        terms = L.kagome12(flux=phi, peierls=True)
+        d1t, d2t = L.kagome12_flux_derivatives(phi)
+        H = O.hamiltonian(12, 6, 6, terms, terms, 4.0)
+        H1 = O.hamiltonian(12, 6, 6, d1t, d1t, 0.0)
+        H2 = O.hamiltonian(12, 6, 6, d2t, d2t, 0.0)
+        v0 = np.random.default_rng(k).standard_normal(H.shape[0]).astype(np.complex128)
+        w, v = sla.eigsh(H, k=2, which="SA", tol=1e-14, maxiter=50000, v0=v0)
+        order = np.argsort(w)
+        e0, e1 = float(w[order[0]]), float(w[order[1]])
+        psi = v[:, order[0]]
+        psi = psi / np.linalg.norm(psi)
+        h1 = H1 @ psi
+        d1 = float(np.vdot(psi, h1).real)
+        b = h1 - psi * np.vdot(psi, h1)
+        n = H.shape[0]
+
+        def apply(x):
+            # Q (H - E0) Q + psi psi^H: positive definite, b and the solution orthogonal to psi
+            x = np.asarray(x).reshape(-1)
+            xq = x - psi * np.vdot(psi, x)
+            y = H @ xq - e0 * xq
+            y = y - psi * np.vdot(psi, y)
+            return y + psi * np.vdot(psi, x)
+
+        A = sla.LinearOperator((n, n), matvec=apply, dtype=np.complex128)
+        its = [0]
+
+        def cb(_):
+            its[0] += 1
+
+        phi_sol, info = sla.cg(A, b, rtol=1e-14, atol=0.0, maxiter=20000, callback=cb)
+        if info != 0:
+            raise RuntimeError(f"CG did not converge at k={k} (info {info})")
+        res = float(np.linalg.norm(apply(phi_sol) - b) / np.linalg.norm(b))
+        d2 = float(np.vdot(psi, H2 @ psi).real - 2.0 * np.vdot(b, phi_sol).real)
+        ritz_res = float(np.linalg.norm(H @ psi - e0 * psi))
+        out["points"].append({"k": int(k), "phi": phi, "E0": e0, "E1": e1, "dE0_dphi": d1, "d2E0_dphi2": d2,
+                              "eigsh_residual": ritz_res, "cg_iterations": its[0], "cg_rel_residual": res})
+        print(f"flux k={k} phi={phi:.6f} E0={e0!r} gap={e1 - e0:.4f} d1={d1!r} d2={d2!r} "
+              f"res={ritz_res:.1e} cg={its[0]} ({res:.1e}) {time.time() - t0:.1f}s", flush=True)
+    return out
+
+
+def sweep_fixtures(realisations=(0, 1), sectors=((6, 6), (7, 5), (8, 4)), W: float = 6.0, seed: int = 0) -> dict:
+    """E0 of disorder-sweep instances (open L=12 chain, t=1, U=1, on-site
+    W * uniform(-1,1) from Philox keyed by seed * 2^20 + realisation, the
+    first 12 numbers for the up operator and the next 12 for the down one)
+    by scipy eigsh on the oracle's Kronecker-sum Hamiltonian."""
+    import scipy.sparse.linalg as sla
+    out = {"workload": "open chain L=12, t=1, U=1, W=6", "points": []}
+    for r in realisations:
+        x = O.philox_uniform(seed * (1 << 20) + r, 24, W)
+        tu = L.chain(12, periodic=False, eps=list(x[:12]))
+        td = L.chain(12, periodic=False, eps=list(x[12:]))
+        for qu, qd in sectors:
+            t0 = time.time()
+            H = O.hamiltonian(12, qu, qd, tu, td, 1.0)
+            v0 = np.random.default_rng(r).standard_normal(H.shape[0])
+            w = np.sort(sla.eigsh(H, k=2, which="SA", tol=1e-14, maxiter=50000, v0=v0)[0])
+            out["points"].append({"realisation": int(r), "sector": [qu, qd], "E0": float(w[0]), "E1": float(w[1])})
+            print(f"mbl r={r} ({qu},{qd}) E0={w[0]!r} gap={w[1] - w[0]:.3e} {time.time() - t0:.1f}s", flush=True)
+    return out
+
+
 if __name__ == "__main__":
-    main()
+    if "--sweep" in sys.argv[1:]:
+        (OUT / "sweep_chain12_W6.json").write_text(json.dumps(sweep_fixtures(), indent=1))
+    elif "--flux" in sys.argv[1:]:
+        (OUT / "flux_kagome12_q66_U4.json").write_text(json.dumps(flux_fixtures(), indent=1))
+    else:
+        main()

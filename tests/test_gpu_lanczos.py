@@ -335,3 +335,25 @@ def test_reorth_coefficients_match_oracle(ed, orc):
     assert np.max(np.abs(a[:40] - np.asarray(a_o)[:40])) < 1e-11 * np.max(np.abs(a_o))
     assert np.max(np.abs(b[1:40] - np.asarray(b_o)[1:40])) < 1e-11 * np.max(np.abs(b_o))
     assert abs(runs[0][0] - e_o) < 1e-12 * abs(e_o)
+
+
+def test_grid_barrier_timeout_is_reported_and_operator_recovers(ed, golden_energies, monkeypatch):
+    """The persistent kernel's bounded grid-barrier wait, made to run out on
+    purpose: ED_GRID_WAIT="1000000,1" gives every barrier a 1 ms limit and
+    makes it wait for one arrival more than the grid has, an arrival that
+    never comes.  Every CTA gives up at its first barrier (no bulk copy is in
+    flight there) and ed_lanczos_run returns ED_ERR_TIMEOUT; the next run on
+    the same operator, without the knob, returns the golden E0."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import _capi, lattices as L
+    op = op_for(ed, 12, 6, 6, L.kagome12(), L.kagome12(), 8.0)
+    monkeypatch.setenv("ED_GRID_WAIT", "1000000,1")
+    with pytest.raises(_capi.EdError) as ei:
+        ed.Lanczos().eigen(op, max_steps=30, mode="fixed", ritz="none", seed=0)
+    assert ei.value.status == _capi.ED_ERR_TIMEOUT
+    monkeypatch.delenv("ED_GRID_WAIT")
+    lz = ed.Lanczos()
+    e0, v = lz.eigen(op, max_steps=300, mode="fixed", seed=0)
+    assert lz.result.launches <= 8  # the persistent path, not the per-step kernels
+    g = golden_energies["kagome12_q66_U8"]["E0"]
+    assert abs(e0 - g) < 1e-10 * abs(g)
+    assert np.linalg.norm(op.matvec(v) - e0 * v) < 1e-6

@@ -194,3 +194,12 @@ def test_sxy_oracle_total_spin_multiplets(orc):
     ws = np.linalg.eigvalsh(S)
     ss = (-1 + np.sqrt(1 + 4 * np.clip(ws, 0, None))) / 2
     assert np.max(np.abs(ss - np.round(ss))) < 1e-10
+
+
+def test_oracle_kagome12_terms_match_the_package_lattice():
+    """The CPU baseline builds Kagome12 from the oracle's own restatement of
+    KagomeLattice12; it must be the term list the library is given."""
+    from oracle import oracle as O
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    assert O.kagome12_terms() == L.kagome12()
+    assert np.array_equal(O.philox_uniform(7, 33, 2.0), philox_uniform(7, 33, 2.0))

@@ -41,7 +41,7 @@ def test_reference_arm_two_ranks_rank0_prints_once():
     alone runs the host-core reference sample and prints one JSON line; the
     other rank exits 0 without work."""
     port = free_port()
-    env = dict(os.environ, ED_BENCH_BACKEND="gloo")
+    env = dict(os.environ, ED_BENCH_BACKEND="gloo", ED_BENCH_SOLVE_STEPS="10")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), str(ROOT / "bench.py"), "--impl", "reference",
            "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-seconds", "0.3"]
@@ -52,3 +52,4 @@ def test_reference_arm_two_ranks_rank0_prints_once():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+    assert d["config"]["lanczos_steps_per_solve"] == 10

@@ -35,6 +35,14 @@ def test_flux_grid_and_rows():
     terms = L.kagome12(flux=0.0, peierls=True)
     assert sum(t[0] == "P" for t in terms) == 24 and all(t[4] == 0.0 for t in terms if t[0] == "P")
     pts = [sweeps.MblPoint(2, (7, 5), -1.5, 0.3, 0.4, np.arange(3.0), np.arange(3.0) + 10, 300)]
-    assert sweeps.mbl_rows(pts) == [(2, 7, 5, -1.5, 0.3, 0.0, 1.0, 2.0, 10.0, 11.0, 12.0)]
-    fp = [sweeps.FluxPoint(0.1, -2.0, 0.5, 1.5, 300)]
-    assert sweeps.flux_rows(fp) == [(0.1, -2.0, 0.5, 1.5)]
+    pts[0].min_bits = 51
+    rows = sweeps.mbl_rows(pts)
+    assert rows[0][:11] == (2, 7, 5, -1.5, 0.3, 0.0, 1.0, 2.0, 10.0, 11.0, 12.0)
+    assert rows[0][11] == 51 and math.isnan(rows[0][12])
+    fp = [sweeps.FluxPoint(0.1, -2.0, 0.5, 1.5, 300, 52)]
+    assert sweeps.flux_rows(fp)[0][:5] == (0.1, -2.0, 0.5, 1.5, 52)
+    # errors against an oracle table are attached by key, the largest returned
+    assert sweeps.attach_oracle(fp, {0.1: -2.0 + 3e-12}) == abs(-2.0 - (-2.0 + 3e-12))
+    assert sweeps.flux_rows(fp)[0][5] == fp[0].err_vs_oracle
+    assert sweeps.attach_oracle(pts, {(2, (7, 5)): -1.5}) == 0.0
+    assert math.isnan(sweeps.attach_oracle(pts, {(3, (7, 5)): -1.5}))
