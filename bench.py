@@ -272,13 +272,15 @@ def _golden_sweep_e0() -> dict:
 def sweep_record() -> dict:
     """C3 (16 twists of Kagome12 6+6 U=4: E0, dE0/dPhi, d2E0/dPhi2) + C4 (64
     disorder realisations x 3 sectors of the L=12 chain: E0, entanglement,
-    dE0/d eps_i), 300 fixed Lanczos steps per instance, in three forms: tuned
-    (batched + adjoint), plain per-instance, and plain per-instance with the
-    tuned entanglement path.  Host clock with device synchronisation."""
+    dE0/d eps_i), fixed Lanczos steps per instance (500 per twist, 300 per
+    disorder sample), in three forms: tuned (batched + adjoint), plain
+    per-instance, and plain per-instance with the tuned entanglement path.
+    Host clock with device synchronisation."""
     from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import sweeps
     table = _golden_sweep_e0()
     out = {"workload": "C3 16 twists Kagome12 6+6 U=4 + C4 64 realisations x (6,6),(7,5),(8,4) L=12 U=1 W=6",
-           "lanczos_steps": 300, "forms": {}}
+           "lanczos_steps": {"twist": sweeps.FLUX_STEPS, "disorder": 300},
+           "response_steps": sweeps.FLUX_RESPONSE_STEPS, "forms": {}}
     worst, bits = float("nan"), 1 << 30
     for form in ("tuned", "plain_same_ee", "plain"):
         tot, parts = 0.0, {}

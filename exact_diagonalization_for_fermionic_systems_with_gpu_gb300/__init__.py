@@ -7,8 +7,9 @@ The compute path is the compiled C-ABI library ``_lib/libedgb300.so``
 """
 from ._capi import EdError, load  # noqa: F401
 from .hubbard import (H_TBq, Hubbard, Lanczos, basis_rank, basis_unrank, binom,  # noqa: F401
-                      lanczos_batch, random_vector, tridiag_lowest)
+                      lanczos_batch, lanczos_multi, random_vector, tridiag_lowest)
+from . import hubbard  # noqa: F401
 from . import lattices  # noqa: F401
 
 __all__ = ["EdError", "load", "H_TBq", "Hubbard", "Lanczos", "basis_rank", "basis_unrank", "binom",
-           "lanczos_batch", "random_vector", "tridiag_lowest", "lattices"]
+           "lanczos_batch", "lanczos_multi", "random_vector", "tridiag_lowest", "lattices"]

@@ -141,6 +141,10 @@ SIGNATURES = {
                                 C.POINTER(ed_kubo_cfg), C.POINTER(ed_kubo_result), C.c_void_p, C.c_void_p]),
     "ed_response": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_int, C.c_void_p,
                               C.c_void_p, C.c_void_p]),
+    "ed_response_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ed_response_subspace": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_double, C.c_int,
+                                       C.c_void_p, C.c_void_p, C.c_void_p]),
     "ed_entanglement_entropy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64, C.c_void_p, C.c_void_p,
                                           C.c_void_p]),
     "ed_entanglement_entropy_batch": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_uint64, C.c_void_p,

@@ -29,6 +29,7 @@ using namespace dev;
 
 cudaError_t launch_lz_fused(const ed_op* op, const LzFusedArgs& f, cudaStream_t s);
 cudaError_t launch_lz_batch(const ed_op* op, const LzBatchArgs& f, cudaStream_t s);
+cudaError_t launch_lz_multi(int device, int kinds, const LzMultiArgs& f, cudaStream_t s);
 
 constexpr int kLzThreads = 256;
 
@@ -949,28 +950,223 @@ ed_status lanczos_replay(ed_op* op, void* ws_slot, int n, const std::function<cu
     return ED_OK;
 }
 
-// B fixed-step Lanczos runs of operators that share their hopping tables, in
-// one persistent launch (k_lz_batch), each with its own workspace (the op's)
-// and start vector; then each run's T and Ritz vector as lanczos_run forms
-// them from the stored basis.
+// Row-engine variant of an operator's persistent Lanczos kernel.
+static int lz_kind(const ed_op* o) {
+    if (o->cplx) return o->mv_fast ? kKindCplxFast : (o->mv.upSegE ? kKindCplxSeg : kKindCplx);
+    if (o->mv_fast) return o->mv.dnSched ? kKindRealSched : kKindRealFast;
+    return o->mv.upSegE ? kKindRealSeg : kKindReal;
+}
+
+static bool same_tables(const ed_op* a, const ed_op* b) {
+    return a->dimUP == b->dimUP && a->dimDN == b->dimDN && a->cplx == b->cplx && a->mask == b->mask &&
+           a->tma_smem == b->tma_smem && lz_kind(a) == lz_kind(b) && a->tup.ent == b->tup.ent &&
+           a->tup.len == b->tup.len && a->tup.npos == b->tup.npos && a->tdn.ent == b->tdn.ent &&
+           a->tdn.len == b->tdn.len && a->tdn.npos == b->tdn.npos;
+}
+
+// B (<= kLzMultiMax) fixed-step Lanczos runs of operators of any sectors and
+// kinds (each with a shared-memory plan, none on the two-pass matvec) in one
+// persistent launch (k_lz_multi); starts, evecs, alpha and beta hold the
+// instances one after another.  Then each run's T and Ritz vector as
+// lanczos_run forms them from the stored basis.
+static ed_status lanczos_multi_run(ed_op* const* ops, int B, const ed_lanczos_cfg* cfg, const double* starts,
+                                   int start_mem, double* evecs, int evec_mem, double* alpha_h, double* beta_h,
+                                   ed_lanczos_result* res, cudaStream_t s) {
+    ed_op* op0 = ops[0];
+    const int max_steps = cfg->max_steps;
+    const bool want_ritz = cfg->ritz == ED_RITZ_STORED && evecs;
+    std::vector<Workspace*> ws(B);
+    std::vector<LzMultiInst> inst(B);
+    std::vector<MvArgs> args(B);
+    std::vector<int64_t> offs(B + 1, 0);
+    int smem = 0;
+    int64_t launches = 0;
+    for (int b = 0; b < B; ++b) {
+        ed_op* op = ops[b];
+        if (op->tma_smem <= 0 || op->striped) return ED_ERR_NOT_BUILT;
+        if (op->device != op0->device) return ED_ERR_ARG;
+        const int64_t DW = op->D * (op->cplx ? 2 : 1);
+        offs[b + 1] = offs[b] + DW;
+        smem = std::max(smem, op->tma_smem);
+        void** slot = lanczos_ws_slot(op);
+        if (!*slot) *slot = new WsHolder();
+        Workspace* w = &reinterpret_cast<WsHolder*>(*slot)->ws;
+        ed_status st = ensure_ws(op, w, (size_t)max_steps + 1, DW, max_steps);
+        if (st != ED_OK) return st;
+        ws[b] = w;
+        LZ_CK(cudaMemsetAsync(w->h.counter, 0, sizeof(unsigned int) * 4, s));
+        LZ_CK(cudaMemsetAsync(w->ritz_ctr, 0, sizeof(unsigned int), s));
+        if (cfg->start == ED_START_USER) {
+            LZ_CK(cudaMemcpyAsync(w->fbuf, starts + offs[b], sizeof(double) * DW,
+                                  start_mem == ED_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+        } else {
+            LZ_CK(launch_random(w->fbuf, DW, cfg->seed + (uint64_t)b, s));
+            ++launches;
+        }
+        LZ_CK(launch_emax(w->fbuf, DW, w->emax, w->flag, s));
+        k_lz_start<<<lz_grid(DW), kLzThreads, 0, s>>>(w->fbuf, DW, w->emax, w->flag, w->basis, w->lz);
+        LZ_CK(cudaGetLastError());
+        launches += 2;
+        int group = b;
+        for (int c = 0; c < b; ++c)
+            if (same_tables(ops[c], op)) { group = inst[c].group; break; }
+        inst[b] = LzMultiInst{w->basis, w->u, w->lz, DW, w->stride, lz_kind(op), group, (int)op->dimUP, 0};
+        args[b] = op->mv;
+        args[b].err = op0->d_err;  // one error word for the launch
+    }
+    {
+        const size_t sync_bytes = 128 + sizeof(unsigned int) * 2 * kLzMultiMax + sizeof(LzRedSet) * 4 * (size_t)B;
+        unsigned char* sync = nullptr;
+        LzMultiInst* dinst = nullptr;
+        MvArgs* dargs = nullptr;
+        if (cudaMallocAsync(&sync, sync_bytes, s) != cudaSuccess) return ED_ERR_ALLOC;
+        if (cudaMallocAsync(&dinst, sizeof(LzMultiInst) * B, s) != cudaSuccess ||
+            cudaMallocAsync(&dargs, sizeof(MvArgs) * B, s) != cudaSuccess) {
+            cudaFreeAsync(sync, s);
+            cudaFreeAsync(dinst, s);
+            return ED_ERR_ALLOC;
+        }
+        cudaError_t le = cudaMemsetAsync(sync, 0, sync_bytes, s);
+        if (le == cudaSuccess)
+            le = cudaMemcpyAsync(dinst, inst.data(), sizeof(LzMultiInst) * B, cudaMemcpyHostToDevice, s);
+        if (le == cudaSuccess) le = cudaMemcpyAsync(dargs, args.data(), sizeof(MvArgs) * B, cudaMemcpyHostToDevice, s);
+        if (le == cudaSuccess) {
+            // sync: barrier counter at 0, 2 * B queue counters at 128, then the reduction sets
+            LzMultiArgs fa{dargs, dinst, B, 0, max_steps, smem, reinterpret_cast<unsigned int*>(sync),
+                           reinterpret_cast<LzRedSet*>(sync + 128 + sizeof(unsigned int) * 2 * kLzMultiMax),
+                           reinterpret_cast<unsigned int*>(sync + 128), grid_wait_limits()};
+            int kinds = 0;
+            for (int b = 0; b < B; ++b) kinds |= 1 << inst[b].kind;
+            le = launch_lz_multi(op0->device, kinds, fa, s);
+        }
+        // the host copies of inst and args stay alive until the stream is synchronised below
+        cudaFreeAsync(sync, s);
+        cudaFreeAsync(dinst, s);
+        cudaFreeAsync(dargs, s);
+        if (le == cudaErrorNotSupported || le == cudaErrorCooperativeLaunchTooLarge) {
+            cudaGetLastError();
+            cudaStreamSynchronize(s);
+            return ED_ERR_NOT_BUILT;
+        }
+        if (le != cudaSuccess) {
+            cudaGetLastError();
+            cudaStreamSynchronize(s);
+            return ED_ERR_CUDA;
+        }
+        ++launches;
+    }
+    ed_status result = ED_OK;
+    for (int b = 0; b < B && result == ED_OK; ++b) {
+        Workspace* w = ws[b];
+        const int64_t DW = offs[b + 1] - offs[b];
+        const LzState& H = w->h;
+        LzState hs;
+        std::vector<double> ha(max_steps + 2), hb(max_steps + 2), tri(max_steps + 2);
+        int n = max_steps, err_flag = 0;
+        if (cudaMemcpyAsync(&hs, w->lz, sizeof(LzState), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(ha.data(), H.alpha, sizeof(double) * n, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(hb.data(), H.beta, sizeof(double) * (n + 1), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(&err_flag, op0->d_err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess) {
+            result = ED_ERR_CUDA;
+            break;
+        }
+        if (err_flag) {
+            cudaMemset(op0->d_err, 0, sizeof(int));
+            result = ED_ERR_TIMEOUT;
+            break;
+        }
+        if (hs.status == 7) {
+            int nb = n;
+            for (int k = 0; k < n; ++k)
+                if (hb[k + 1] == 0.0) { nb = k + 1; break; }
+            n = std::max(1, nb);
+        } else if (hs.status != 0) {
+            result = ED_ERR_NONFINITE;
+            break;
+        }
+        tri[0] = tridiag_lowest_host(n, ha.data(), hb.data() + 1, tri.data() + 1);
+        if (want_ritz) {
+            std::vector<int> ev(n);
+            if (cudaMemcpy(ev.data(), H.e, sizeof(int) * n, cudaMemcpyDeviceToHost) != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+            std::vector<double> r(n);
+            for (int k = 0; k < n; ++k) r[k] = tri[1 + k] / hb[k] * std::ldexp(1.0, ev[k]);
+            std::vector<int64_t> rt;
+            std::vector<int> rs;
+            int F;
+            fx_coefs(r, &rt, &rs, &F);
+            double* out = evec_mem == ED_MEM_DEVICE ? evecs + offs[b] : w->fbuf;
+            int64_t gr = (DW / 2 + kLzThreads - 1) / kLzThreads;
+            gr = std::max<int64_t>(1, std::min<int64_t>(gr, kLzMaxPartials));
+            if (cudaMemcpyAsync(w->coef_rt, rt.data(), sizeof(int64_t) * n, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+                cudaMemcpyAsync(w->coef_rs, rs.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+            k_ritz<<<(int)gr, kLzThreads, 0, s>>>(w->basis, DW, w->stride, n, w->coef_rt, w->coef_rs, F, out,
+                                                  w->ritz_part, w->ritz_ctr, w->inv_norm);
+            k_scale<<<lz_grid(DW), kLzThreads, 0, s>>>(out, DW, w->inv_norm);
+            launches += 2;
+            if (cudaGetLastError() != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+            if (evec_mem != ED_MEM_DEVICE &&
+                cudaMemcpyAsync(evecs + offs[b], out, sizeof(double) * DW, cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+            if (cudaStreamSynchronize(s) != cudaSuccess) {
+                result = ED_ERR_CUDA;
+                break;
+            }
+        }
+        if (alpha_h) std::memcpy(alpha_h + (size_t)b * max_steps, ha.data(), sizeof(double) * n);
+        if (beta_h) std::memcpy(beta_h + (size_t)b * (max_steps + 1), hb.data(), sizeof(double) * (n + 1));
+        if (res) {
+            ed_lanczos_result& R = res[b];
+            std::memset(&R, 0, sizeof(R));
+            R.e0 = tri[0];
+            R.steps = n;
+            R.status = hs.status == 7 ? ED_ERR_BREAKDOWN : ED_OK;
+            R.min_bits = hs.min_bits;
+            R.residual = std::fabs(hb[n] * tri[n]);
+            R.n_matvec = max_steps;
+            R.launches = b == 0 ? launches : 0;
+        }
+    }
+    cudaStreamSynchronize(s);
+    return result;
+}
+
+// B fixed-step Lanczos runs in one persistent launch, each with its own
+// workspace (the op's) and start vector; then each run's T and Ritz vector as
+// lanczos_run forms them from the stored basis.  Operators that share their
+// hopping tables (real, one class, gather schedule, B <= kLzBatchMax) run in
+// k_lz_batch; any other mix of sectors and kinds in k_lz_multi
+// (ED_LZ_BATCH=multi sends every batch there).
 ed_status lanczos_batch_run(ed_op* const* ops, int B, const ed_lanczos_cfg* cfg, const double* starts, int start_mem,
                             double* evecs, int evec_mem, double* alpha_h, double* beta_h, ed_lanczos_result* res,
                             cudaStream_t s) {
-    if (!ops || B < 1 || B > kLzBatchMax || !cfg || cfg->max_steps < 1 || cfg->max_steps > 100000) return ED_ERR_ARG;
+    if (!ops || B < 1 || B > kLzMultiMax || !cfg || cfg->max_steps < 1 || cfg->max_steps > 100000) return ED_ERR_ARG;
     if (cfg->mode != ED_LANCZOS_FIXED || cfg->reorth || cfg->ritz == ED_RITZ_RECOMPUTE) return ED_ERR_ARG;
     if (cfg->start == ED_START_USER && !starts) return ED_ERR_ARG;
     ed_op* op0 = ops[0];
-    for (int b = 0; b < B; ++b) {
+    for (int b = 0; b < B; ++b)
+        if (!ops[b]) return ED_ERR_ARG;
+    bool homogeneous = B <= kLzBatchMax;
+    for (int b = 0; b < B && homogeneous; ++b) {
         const ed_op* o = ops[b];
-        if (!o) return ED_ERR_ARG;
-        if (o->cplx || !o->mv_fast || !o->mv.dnSched || o->tma_smem <= 0 || o->striped) return ED_ERR_NOT_BUILT;
-        if (o->device != op0->device || o->dimUP != op0->dimUP || o->dimDN != op0->dimDN || o->mask != op0->mask)
-            return ED_ERR_ARG;
-        // the kernel walks op0's tables for every instance
-        if (o->tup.ent != op0->tup.ent || o->tup.len != op0->tup.len || o->tup.npos != op0->tup.npos ||
-            o->tdn.ent != op0->tdn.ent || o->tdn.len != op0->tdn.len || o->tdn.npos != op0->tdn.npos)
-            return ED_ERR_ARG;
+        if (o->cplx || !o->mv_fast || !o->mv.dnSched || o->tma_smem <= 0 || o->striped || o->device != op0->device ||
+            !same_tables(o, op0))
+            homogeneous = false;
     }
+    const char* force = std::getenv("ED_LZ_BATCH");
+    if (!homogeneous || (force && std::strcmp(force, "multi") == 0))
+        return lanczos_multi_run(ops, B, cfg, starts, start_mem, evecs, evec_mem, alpha_h, beta_h, res, s);
     const int64_t DW = op0->D;
     const int max_steps = cfg->max_steps;
     const bool want_ritz = cfg->ritz == ED_RITZ_STORED && evecs;

@@ -111,4 +111,46 @@ struct LzBatchArgs {
     GridWait wait;
 };
 
+struct MvArgs;
+
+// Heterogeneous batch (k_lz_multi): instances of any sectors, real or
+// complex, each with its own operator arguments; instances with equal
+// `group` share the shared-memory tables (same sector and hopping terms).
+constexpr int kLzMultiMax = 16;
+
+// Row-engine variant of an operator (the k_lz_fused instantiation it takes).
+enum LzKind : int {
+    kKindRealSched = 0,  // real, one class per table, gather schedule
+    kKindRealFast = 1,   // real, one class per table, CSR down table
+    kKindRealSeg = 2,    // real, class-segmented tables
+    kKindReal = 3,       // real, any classes
+    kKindCplxFast = 4,   // complex, one class per table
+    kKindCplxSeg = 5,    // complex, class-segmented tables
+    kKindCplx = 6,       // complex, any classes
+};
+
+struct LzMultiInst {
+    int64_t* basis;   // stored Krylov basis, slot stride `stride`
+    int64_t* u;       // matvec output
+    LzState* lz;
+    int64_t n;        // stored values (rows, or 2 rows complex)
+    int64_t stride;
+    int kind;         // LzKind
+    int group;        // instances with equal group share staged tables
+    int dimUP;
+    int pad_;
+};
+
+struct LzMultiArgs {
+    const MvArgs* args;         // B operator arguments (device; err of the first)
+    const LzMultiInst* inst;    // B instances (device)
+    int B;
+    int j0, j1;
+    int smem;                   // dynamic shared memory of the launch
+    unsigned int* gbar;         // grid-barrier arrivals, zero at launch
+    LzRedSet* red;              // 4 * B accumulator sets, zero at launch
+    unsigned int* taken;        // 2 * B row-queue counters (step parity, instance), zero at launch
+    GridWait wait;
+};
+
 }  // namespace ed

@@ -668,6 +668,265 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_batch(const MvArgs a, con
     }
 }
 
+// ---------------------------------------------------------------- multi --
+// B Lanczos runs of any sectors, real or complex, in lockstep in one
+// persistent launch (k_lz_multi).  Each step walks the instances in order:
+// for instance b every CTA takes rows from b's own queue (its first row at
+// blockIdx.x, the rest by an atomic counter, heaviest first) with the row
+// engine variant of b's operator, and moves on to b + 1 as soon as b's queue
+// is empty, so the CTAs' finishing spread is paid once per step, not per
+// instance.  A CTA copies b's operator arguments into shared memory when it
+// reaches b, and re-stages the down-spin tables when b's group (sector and
+// hopping terms) differs from the staged one; the folded down diagonal, which
+// instances of one group need not share, is read from global memory.  The
+// <x, u> and max|u| partials of every instance go through per-instance shared
+// limb sums, the barriers, reduction sets and per-instance scalar updates are
+// k_lz_batch's, so every run's coefficients equal its own single run's bit
+// for bit (the matvec sums are exact integers whatever the variant).
+
+template <bool CPLX>
+__device__ __forceinline__ void multi_first_row(const MvArgs& a, const TmaSmem& S, const int64_t* xq, uint32_t rc) {
+    tma::fence_proxy_async_global();
+    tma::fence_proxy_async_smem();
+    tma_issue_row<CPLX>(a, S, xq, __ldg(a.rowQueue + blockIdx.x), rc & 1);
+}
+
+// The row-engine variant of instance kind `kind`; KINDS (a bit per LzKind)
+// lists the variants this instantiation of k_lz_multi carries, so that a
+// batch of one or two kinds does not pay the registers of all seven.
+template <int KINDS>
+__device__ __forceinline__ void multi_rows(int kind, const MvArgs& a, const TmaSmem& S, const int64_t* xq, int64_t* uq,
+                                           uint32_t& rc, int s_u, i128& dot, uint64_t& mx, unsigned int* taken,
+                                           uint32_t* snext) {
+#define ED_MULTI_CASE(K, C, F, SC, SG)                                                                              \
+    if (((KINDS >> K) & 1) && kind == K) {                                                                          \
+        tma_rows<C, 1, F, true, SC, true, SG, true>(a, S, xq, uq, nullptr, rc, 0, s_u, dot, mx, taken, snext);     \
+        return;                                                                                                     \
+    }
+    ED_MULTI_CASE(kKindRealSched, false, true, true, false)
+    ED_MULTI_CASE(kKindRealFast, false, true, false, false)
+    ED_MULTI_CASE(kKindRealSeg, false, false, false, true)
+    ED_MULTI_CASE(kKindReal, false, false, false, false)
+    ED_MULTI_CASE(kKindCplxFast, true, true, false, false)
+    ED_MULTI_CASE(kKindCplxSeg, true, false, false, true)
+    ED_MULTI_CASE(kKindCplx, true, false, false, false)
+#undef ED_MULTI_CASE
+}
+
+template <int KINDS>
+__global__ void __launch_bounds__(kTmaThreads, 2) k_lz_multi(const LzMultiArgs f) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint32_t uoff[kTmaUpStage];
+    __shared__ uint32_t uent[kTmaUpStage];
+    __shared__ int give_up;
+    __shared__ uint32_t s_next;
+    __shared__ __align__(16) MvArgs s_args;
+    __shared__ SlotScalars sX[kLzMultiMax], sP[kLzMultiMax];
+    __shared__ int s_status[kLzMultiMax], s_min_bits[kLzMultiMax], s_ew[kLzMultiMax];
+    __shared__ LzCoefs s_coef[kLzMultiMax];
+    __shared__ unsigned long long accl[kLzMultiMax][3], accm[kLzMultiMax];
+    const int tid = threadIdx.x;
+    const int B = f.B;
+    const uint32_t G = gridDim.x;
+
+    if (tid == 0) {
+        TmaSmem S0;
+        S0.bar = reinterpret_cast<uint64_t*>(sm);
+        S0.give_up = &give_up;
+        tma_init(S0);
+    }
+    if (tid < B) {
+        const LzState* lz = f.inst[tid].lz;
+        const int j = f.j0;
+        sX[tid] = {lz->e[j], lz->m[j], lz->beta[j], lz_inv(lz->beta[j])};
+        if (j > 0) sP[tid] = {lz->e[j - 1], lz->m[j - 1], lz->beta[j - 1], lz_inv(lz->beta[j - 1])};
+        else sP[tid] = {0, 0, 0.0, 0.0};
+        s_status[tid] = lz->status;
+        s_min_bits[tid] = lz->min_bits;
+        s_ew[tid] = 0;
+        accl[tid][0] = accl[tid][1] = accl[tid][2] = 0;
+        accm[tid] = 0;
+    }
+    __syncthreads();
+
+    uint32_t rc = 0;          // rows streamed through the row buffers
+    uint32_t tc = 0;          // table stagings (phases of bar[2])
+    int cur = -1, staged = -1;
+    unsigned int target = 0;  // grid-barrier arrivals expected so far
+    for (int j = f.j0; j < f.j1; ++j) {
+        const int rM = 2 * (j - f.j0), rA = rM + 1;
+        if (tid >= kTmaThreads - 32 && tid < kTmaThreads - 32 + B && j > f.j0) {
+            // slot j of instance b from the previous step's axpy reduction
+            const int b = tid - (kTmaThreads - 32);
+            i128 ss;
+            uint64_t mw;
+            red_pull(&f.red[((rM - 1) % 4) * B + b], ss, mw);
+            slot_done(f.inst[b].lz, j, s_ew[b], ss, mw, sX[b], sP[b], s_status[b], s_min_bits[b], blockIdx.x == 0);
+        }
+        // ---- phase M: u_b = H_b w_j of every instance, instance by instance
+        for (int b = 0; b < B; ++b) {
+            const LzMultiInst I = f.inst[b];
+            if (b != cur) {
+                __syncthreads();  // the previous instance's rows and arguments are done with
+                const uint64_t* src = reinterpret_cast<const uint64_t*>(f.args + b);
+                uint64_t* dst = reinterpret_cast<uint64_t*>(&s_args);
+                for (int k = tid; k < (int)(sizeof(MvArgs) / 8); k += blockDim.x) dst[k] = __ldg(src + k);
+                __syncthreads();
+                cur = b;
+            }
+            const TmaSmem S = tma_view(s_args, sm, uoff, uent, &give_up);
+            if (I.group != staged) {
+                if (tid == 0) {
+                    tma::fence_proxy_async_smem();
+                    tma_issue_tables(s_args, S);
+                }
+                if (I.kind == kKindRealSched) tma_zero_slots(s_args, S);
+                if (!tma::mbar_wait(&S.bar[2], tc & 1)) {
+                    if (tid == 0) atomicExch(s_args.err, 1);
+                    give_up = 1;
+                }
+                __syncthreads();
+                if (give_up) {
+                    if (tid == 0) tma::mbar_wait(&S.bar[2], tc & 1);  // the table copy lands before the CTA leaves
+                    return;
+                }
+                ++tc;
+                staged = I.group;
+            }
+            const int sb = s_args.bq_bits + kFxBits - 62;
+            const int s_u = sb > 0 ? sb : 0;
+            const int64_t* xq = I.basis + (size_t)j * (size_t)I.stride;
+            const bool cplx = I.kind >= kKindCplxFast;
+            if (tid == 0 && blockIdx.x < (uint32_t)I.dimUP) {
+                if (cplx) multi_first_row<true>(s_args, S, xq, rc);
+                else multi_first_row<false>(s_args, S, xq, rc);
+            }
+            i128 dot = 0;
+            uint64_t mx = 0;
+            multi_rows<KINDS>(I.kind, s_args, S, xq, I.u, rc, s_u, dot, mx, f.taken + (j & 1) * B + b, &s_next);
+            if (give_up) return;
+            batch_flush(dot, mx, accl[b], &accm[b]);
+        }
+        __syncthreads();
+        if (tid < B) {
+            red_push(&f.red[(rM % 4) * B + tid], batch_total(accl[tid]), accm[tid]);
+            accl[tid][0] = accl[tid][1] = accl[tid][2] = 0;
+            accm[tid] = 0;
+        }
+        if (!grid_sync(f.gbar, target, &give_up, f.args[0].err, f.wait)) return;
+        if (tid < B) {
+            const int b = tid;
+            LzState* lz = f.inst[b].lz;
+            const MvArgs& ab = f.args[b];
+            i128 s;
+            uint64_t m;
+            red_pull(&f.red[(rM % 4) * B + b], s, m);
+            if (blockIdx.x == 0) {
+                if (rM >= 2) f.red[((rM - 2) % 4) * B + b] = LzRedSet{0, 0, 0, 0};
+                // the other parity's queue counters are next taken from after the next barrier
+                f.taken[((j + 1) & 1) * B + b] = 0;
+            }
+            const int sb = ab.bq_bits + kFxBits - 62;
+            const int s_u = sb > 0 ? sb : 0;
+            const int e_u = sX[b].e - ab.Fc + s_u;
+            s_coef[b] = lz_coefs(j, s, e_u, m, sX[b].e, sX[b].m, sX[b].beta, sX[b].ib, sP[b].e, sP[b].m, sP[b].ib,
+                                 s_status[b]);
+            s_ew[b] = s_coef[b].e_w;
+            if (blockIdx.x == 0) {
+                lz->s_u = s_u;
+                lz->e_u = e_u;
+                lz->m_u = m;
+                lz->alpha[j] = s_coef[b].alpha;
+                for (int k = 0; k < 3; ++k) {
+                    lz->at[k] = s_coef[b].at[k];
+                    lz->sh[k] = 0;
+                }
+                lz->Fa = s_coef[b].Fa;
+                lz->e_w = s_coef[b].e_w;
+            }
+        }
+        __syncthreads();
+
+        // ---- phase A: w_{j+1} of every instance, last instance first ------
+        for (int b = B - 1; b >= 0; --b) {
+            const LzMultiInst I = f.inst[b];
+            const int64_t* xq = I.basis + (size_t)j * (size_t)I.stride;
+            const int64_t* pq = j > 0 ? I.basis + (size_t)(j - 1) * (size_t)I.stride : xq;
+            int64_t* wq = I.basis + (size_t)(j + 1) * (size_t)I.stride;
+            const int64_t a0 = s_coef[b].at[0], a1 = s_coef[b].at[1], a2 = s_coef[b].at[2];
+            const int Fa = s_coef[b].Fa;
+            i128 ss = 0;
+            uint64_t mw = 0;
+            const int64_t npair = I.n >> 1;
+            const longlong2* u2 = reinterpret_cast<const longlong2*>(I.u);
+            const longlong2* x2 = reinterpret_cast<const longlong2*>(xq);
+            const longlong2* p2 = reinterpret_cast<const longlong2*>(pq);
+            longlong2* w2 = reinterpret_cast<longlong2*>(wq);
+            for (int64_t i = (int64_t)blockIdx.x * blockDim.x + tid; i < npair; i += (int64_t)G * blockDim.x) {
+                const longlong2 uu = __ldcg(u2 + i), xx = __ldcg(x2 + i), pp = __ldcg(p2 + i);
+                longlong2 w;
+                w.x = shr_round_i64(mul_wide(a0, uu.x) + mul_wide(a1, xx.x) + mul_wide(a2, pp.x), Fa);
+                w.y = shr_round_i64(mul_wide(a0, uu.y) + mul_wide(a1, xx.y) + mul_wide(a2, pp.y), Fa);
+                w2[i] = w;
+                ss += (mul_wide(w.x, w.x) >> 16) + (mul_wide(w.y, w.y) >> 16);
+                const uint64_t ax = (uint64_t)(w.x < 0 ? -w.x : w.x), ay = (uint64_t)(w.y < 0 ? -w.y : w.y);
+                mw = ax > mw ? ax : mw;
+                mw = ay > mw ? ay : mw;
+            }
+            if ((I.n & 1) && blockIdx.x == 0 && tid == 0) {
+                const int64_t i = I.n - 1;
+                const int64_t w = shr_round_i64(
+                    mul_wide(a0, __ldcg(I.u + i)) + mul_wide(a1, __ldcg(xq + i)) + mul_wide(a2, __ldcg(pq + i)), Fa);
+                wq[i] = w;
+                ss += mul_wide(w, w) >> 16;
+                const uint64_t aw = (uint64_t)(w < 0 ? -w : w);
+                mw = aw > mw ? aw : mw;
+            }
+            batch_flush(ss, mw, accl[b], &accm[b]);
+        }
+        __syncthreads();
+        if (tid < B) {
+            red_push(&f.red[(rA % 4) * B + tid], batch_total(accl[tid]), accm[tid]);
+            accl[tid][0] = accl[tid][1] = accl[tid][2] = 0;
+            accm[tid] = 0;
+        }
+        if (!grid_sync(f.gbar, target, &give_up, f.args[0].err, f.wait)) return;
+        if (tid < B && blockIdx.x == 0) {
+            const int b = tid;
+            if (rA >= 2) f.red[((rA - 2) % 4) * B + b] = LzRedSet{0, 0, 0, 0};
+            if (j + 1 == f.j1) {
+                i128 ss;
+                uint64_t mw;
+                red_pull(&f.red[(rA % 4) * B + b], ss, mw);
+                slot_done(f.inst[b].lz, j + 1, s_coef[b].e_w, ss, mw, sX[b], sP[b], s_status[b], s_min_bits[b], true);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Cooperative launch of a heterogeneous batch: f.smem dynamic bytes (the
+// largest plan of its operators), as many CTAs as are co-resident (one or
+// two per SM; the row queues take any grid).
+cudaError_t launch_lz_multi(int device, int kinds, const LzMultiArgs& f, cudaStream_t s) {
+    constexpr int kRS = 1 << kKindRealSched, kCS = 1 << kKindCplxSeg, kAll = (1 << 7) - 1;
+    const void* fn = (kinds & ~kRS) == 0          ? (const void*)k_lz_multi<kRS>
+                     : (kinds & ~kCS) == 0        ? (const void*)k_lz_multi<kCS>
+                     : (kinds & ~(kRS | kCS)) == 0 ? (const void*)k_lz_multi<kRS | kCS>
+                                                   : (const void*)k_lz_multi<kAll>;
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, f.smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, sms = 0, coop = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTmaThreads, f.smem)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device)) != cudaSuccess) return e;
+    if (!coop || per_sm < 1) return cudaErrorNotSupported;
+    per_sm = per_sm > 2 ? 2 : per_sm;
+    LzMultiArgs fv = f;
+    void* args[] = {&fv};
+    return cudaLaunchCooperativeKernel(fn, dim3((unsigned)(per_sm * sms)), dim3(kTmaThreads), args, (size_t)f.smem, s);
+}
+
 // Cooperative launch of the batch: grid and shared memory of the first
 // operator's plan.
 // Cooperative launch of the batch: grid and shared memory of the first

@@ -248,7 +248,10 @@ __device__ __forceinline__ bool tma_first_row_dyn(const MvArgs& a, uint32_t* u) 
     return true;
 }
 
-template <bool CPLX, int OUT, bool FAST, bool COH, bool SCHED, bool DYN, bool SEG = false>
+// GDIAG: the folded down diagonal is read from a.dDNq in global memory
+// instead of the staged copy (instances that share staged tables but not
+// their on-site terms, k_lz_multi).
+template <bool CPLX, int OUT, bool FAST, bool COH, bool SCHED, bool DYN, bool SEG = false, bool GDIAG = false>
 __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, const int64_t* __restrict__ xq,
                                          int64_t* __restrict__ uq, double* __restrict__ y, uint32_t& rc, int E_out,
                                          int s_u, i128& dot, uint64_t& mx, unsigned int* taken = nullptr,
@@ -512,7 +515,8 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                 i128& ai = c ? ai1 : ai0;
                 int64_t xr, xi;
                 row_elem<CPLX>(xrow, d * W, xr, xi);
-                const int64_t dq = du + S.ddq[d] + a.Uq * (int64_t)__popcll(stu & S.dst[d] & a.mask);
+                const int64_t ddn = GDIAG ? __ldg(a.dDNq + d) : S.ddq[d];
+                const int64_t dq = du + ddn + a.Uq * (int64_t)__popcll(stu & S.dst[d] & a.mask);
                 ar += mul_wide(dq, xr);
                 if (CPLX) ai += mul_wide(dq, xi);
                 const size_t o = (size_t)(ubase + d) * W;

@@ -695,6 +695,36 @@ ed_status ed_drude_kubo(ed_op* H, ed_op* J, ed_op* K, const double* psi, double 
     return st;
 }
 
+}  // extern "C"
+
+namespace {
+
+// <x|(H - E0)^-1|x> for a device vector x orthogonal to the ground level:
+// -|x|^2 g(0), with g from the continued fraction of a `steps`-step Lanczos
+// run of H started at x, at w = 0 without broadening:
+// g(0) = 1/(E0 - a0 - b1^2/(E0 - a1 - ...)).
+ed_status resolvent_form(ed_op* H, const double* x, double e0, int steps, double* out, cudaStream_t s) {
+    std::vector<double> a(steps), bt(steps + 1);
+    ed_lanczos_cfg lc;
+    std::memset(&lc, 0, sizeof(lc));
+    lc.max_steps = steps;
+    lc.mode = ED_LANCZOS_FIXED;
+    lc.ritz = ED_RITZ_NONE;
+    lc.start = ED_START_USER;
+    ed_lanczos_result lr;
+    const ed_status st = ed_lanczos_run(H, &lc, x, ED_MEM_DEVICE, nullptr, ED_MEM_DEVICE, a.data(), bt.data(), &lr, s);
+    if (st != ED_OK) return st;
+    const int m = lr.steps;
+    long double gz = 1.0L / ((long double)e0 - a[m - 1]);
+    for (int i = m - 2; i >= 0; --i) gz = 1.0L / ((long double)e0 - a[i] - gz * (long double)bt[i + 1] * bt[i + 1]);
+    *out = -(double)((long double)bt[0] * bt[0] * gz);
+    return ED_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double e0, int steps, double* first,
                       double* second, void* stream) {
     if (!H || !dH || !psi || steps < 1 || (second && !d2H)) return ED_ERR_ARG;
@@ -717,23 +747,10 @@ ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double
         double c[2] = {ov[0] / nn[0], cplx ? ov[1] / nn[0] : 0.0};
         cudaMemcpyAsync(coef, c, sizeof(double) * 2, cudaMemcpyHostToDevice, s);
         ed::k_project<<<ob_grid(H->D), kObThreads, 0, s>>>(phi, psi, coef, H->D, cplx ? 1 : 0, b);
-        std::vector<double> a(steps), bt(steps + 1);
-        ed_lanczos_cfg lc;
-        std::memset(&lc, 0, sizeof(lc));
-        lc.max_steps = steps;
-        lc.mode = ED_LANCZOS_FIXED;
-        lc.ritz = ED_RITZ_NONE;
-        lc.start = ED_START_USER;
-        ed_lanczos_result lr;
-        st = ed_lanczos_run(H, &lc, b, ED_MEM_DEVICE, nullptr, ED_MEM_DEVICE, a.data(), bt.data(), &lr, stream);
+        double resp = 0.0;
+        st = resolvent_form(H, b, e0, steps, &resp, s);
         if (st == ED_OK) {
-            // <b|(H - E0)^-1|b> = -|b|^2 * g(0) with g from the continued
-            // fraction at w = 0 (no broadening): 1/(E0 - a0 - b1^2/(E0 - a1 - ...))
-            const int m = lr.steps;
-            long double gz = 1.0L / ((long double)e0 - a[m - 1]);
-            for (int i = m - 2; i >= 0; --i)
-                gz = 1.0L / ((long double)e0 - a[i] - gz * (long double)bt[i + 1] * bt[i + 1]);
-            const double resp = -(double)((long double)bt[0] * bt[0] * gz) / nn[0];
+            resp /= nn[0];
             double d2[2] = {0.0, 0.0};
             st = ed_op_expect(d2H, psi, ED_MEM_DEVICE, d2, stream);
             if (st == ED_OK) *second = d2[0] / nn[0] - 2.0 * resp;
@@ -741,6 +758,210 @@ ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double
     }
     cudaFreeAsync(phi, s);
     cudaFreeAsync(b, s);
+    cudaFreeAsync(coef, s);
+    cudaStreamSynchronize(s);
+    return st;
+}
+
+ed_status ed_response_batch(ed_op* const* H, ed_op* const* dH, ed_op* const* d2H, int n, const double* psis,
+                            const double* e0, int steps, double* first, double* second, void* stream) {
+    if (!H || !dH || !psis || !e0 || !first || n < 1 || n > 16 || steps < 1 || (second && !d2H)) return ED_ERR_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    std::vector<int64_t> off(n + 1, 0);
+    for (int i = 0; i < n; ++i) {
+        if (!H[i] || !dH[i] || (second && !d2H[i])) return ED_ERR_ARG;
+        if (dH[i]->D != H[i]->D || dH[i]->cplx != H[i]->cplx ||
+            (second && (d2H[i]->D != H[i]->D || d2H[i]->cplx != H[i]->cplx)))
+            return ED_ERR_ARG;
+        off[i + 1] = off[i] + H[i]->D * (H[i]->cplx ? 2 : 1);
+    }
+    double *phi = nullptr, *b = nullptr, *coef = nullptr;
+    if (cudaMallocAsync(&phi, sizeof(double) * off[n], s) != cudaSuccess ||
+        cudaMallocAsync(&b, sizeof(double) * off[n], s) != cudaSuccess ||
+        cudaMallocAsync(&coef, sizeof(double) * 2, s) != cudaSuccess) {
+        cudaFreeAsync(phi, s);
+        cudaFreeAsync(b, s);
+        return ED_ERR_ALLOC;
+    }
+    std::vector<double> nn(n, 0.0);
+    ed_status st = ED_OK;
+    // b_i = Q dH_i psi_i, first_i = <psi_i|dH_i|psi_i> / <psi_i|psi_i>
+    for (int i = 0; i < n && st == ED_OK; ++i) {
+        const bool cplx = H[i]->cplx;
+        const double* psi = psis + off[i];
+        st = ed_op_perform(dH[i], psi, phi + off[i], ED_MEM_DEVICE, stream);
+        double ov[2] = {0.0, 0.0}, n2[2] = {0.0, 0.0};
+        if (st == ED_OK) st = dev_dot(psi, phi + off[i], H[i]->D, cplx, ov, s);
+        if (st == ED_OK) st = dev_dot(psi, psi, H[i]->D, cplx, n2, s);
+        if (st != ED_OK) break;
+        nn[i] = n2[0];
+        first[i] = ov[0] / n2[0];
+        if (second) {
+            const double c[2] = {ov[0] / n2[0], cplx ? ov[1] / n2[0] : 0.0};
+            if (cudaMemcpyAsync(coef, c, sizeof(double) * 2, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+                st = ED_ERR_CUDA;
+                break;
+            }
+            ed::k_project<<<ob_grid(H[i]->D), kObThreads, 0, s>>>(phi + off[i], psi, coef, H[i]->D, cplx ? 1 : 0,
+                                                                 b + off[i]);
+        }
+    }
+    if (st == ED_OK && second) {
+        // every resolvent form from one batched Lanczos launch started at the b_i
+        std::vector<double> a((size_t)n * steps), bt((size_t)n * (steps + 1));
+        std::vector<ed_lanczos_result> lr(n);
+        ed_lanczos_cfg lc;
+        std::memset(&lc, 0, sizeof(lc));
+        lc.max_steps = steps;
+        lc.mode = ED_LANCZOS_FIXED;
+        lc.ritz = ED_RITZ_NONE;
+        lc.start = ED_START_USER;
+        st = ed::lanczos_batch_run(H, n, &lc, b, ED_MEM_DEVICE, nullptr, ED_MEM_DEVICE, a.data(), bt.data(), lr.data(),
+                                   s);
+        if (st == ED_ERR_NOT_BUILT) {
+            // no persistent plan for these operators: one run each
+            st = ED_OK;
+            for (int i = 0; i < n && st == ED_OK; ++i) {
+                double r = 0.0, d2[2] = {0.0, 0.0};
+                st = resolvent_form(H[i], b + off[i], e0[i], steps, &r, s);
+                if (st == ED_OK) st = ed_op_expect(d2H[i], psis + off[i], ED_MEM_DEVICE, d2, stream);
+                if (st == ED_OK) second[i] = d2[0] / nn[i] - 2.0 * r / nn[i];
+            }
+        } else {
+            for (int i = 0; i < n && st == ED_OK; ++i) {
+                const double* ai = a.data() + (size_t)i * steps;
+                const double* bi = bt.data() + (size_t)i * (steps + 1);
+                const int m = lr[i].steps;
+                long double gz = 1.0L / ((long double)e0[i] - ai[m - 1]);
+                for (int k = m - 2; k >= 0; --k)
+                    gz = 1.0L / ((long double)e0[i] - ai[k] - gz * (long double)bi[k + 1] * bi[k + 1]);
+                const double resp = -(double)((long double)bi[0] * bi[0] * gz) / nn[i];
+                double d2[2] = {0.0, 0.0};
+                st = ed_op_expect(d2H[i], psis + off[i], ED_MEM_DEVICE, d2, stream);
+                if (st == ED_OK) second[i] = d2[0] / nn[i] - 2.0 * resp;
+            }
+        }
+    }
+    cudaFreeAsync(phi, s);
+    cudaFreeAsync(b, s);
+    cudaFreeAsync(coef, s);
+    cudaStreamSynchronize(s);
+    return st;
+}
+
+ed_status ed_response_subspace(ed_op* H, ed_op* dH, ed_op* d2H, const double* psis, int g, double e0, int steps,
+                               double* d1, double* d2m, void* stream) {
+    if (!H || !dH || !d2H || !psis || !d1 || !d2m || g < 1 || g > 4 || steps < 1) return ED_ERR_ARG;
+    if (dH->D != H->D || dH->cplx != H->cplx || d2H->D != H->D || d2H->cplx != H->cplx) return ED_ERR_ARG;
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    const bool cplx = H->cplx;
+    const int64_t n = H->D, nd = n * (cplx ? 2 : 1);
+    auto col = [&](const double* base, int i) { return base + (size_t)i * (size_t)nd; };
+    auto wcol = [&](double* base, int i) { return base + (size_t)i * (size_t)nd; };
+    double *sv = nullptr, *phi = nullptr, *bv = nullptr, *x = nullptr, *coef = nullptr;
+    if (cudaMallocAsync(&sv, sizeof(double) * nd * g, s) != cudaSuccess ||
+        cudaMallocAsync(&phi, sizeof(double) * nd * g, s) != cudaSuccess ||
+        cudaMallocAsync(&bv, sizeof(double) * nd * g, s) != cudaSuccess ||
+        cudaMallocAsync(&x, sizeof(double) * nd, s) != cudaSuccess ||
+        cudaMallocAsync(&coef, sizeof(double) * 2, s) != cudaSuccess) {
+        cudaFreeAsync(sv, s);
+        cudaFreeAsync(phi, s);
+        cudaFreeAsync(bv, s);
+        cudaFreeAsync(x, s);
+        return ED_ERR_ALLOC;
+    }
+    std::vector<double> D1(2 * g * g, 0.0), E2(2 * g * g, 0.0), R(2 * g * g, 0.0), Rd(g, 0.0);
+    ed_status st = ED_OK;
+    // the states, orthonormalised in order (classical Gram-Schmidt, twice)
+    if (cudaMemcpyAsync(sv, psis, sizeof(double) * nd * g, cudaMemcpyDeviceToDevice, s) != cudaSuccess) st = ED_ERR_CUDA;
+    for (int i = 0; i < g && st == ED_OK; ++i) {
+        for (int pass = 0; pass < 2 && st == ED_OK; ++pass)
+            for (int k = 0; k < i && st == ED_OK; ++k) {
+                double c[2] = {0.0, 0.0};
+                st = dev_dot(col(sv, k), col(sv, i), n, cplx, c, s);
+                if (st != ED_OK) break;
+                if (!cplx) c[1] = 0.0;
+                if (cudaMemcpyAsync(coef, c, sizeof(double) * 2, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+                    st = ED_ERR_CUDA;
+                    break;
+                }
+                ed::k_project<<<ob_grid(n), kObThreads, 0, s>>>(col(sv, i), col(sv, k), coef, n, cplx ? 1 : 0,
+                                                               wcol(sv, i));
+            }
+        double nn[2] = {0.0, 0.0};
+        if (st == ED_OK) st = dev_dot(col(sv, i), col(sv, i), n, cplx, nn, s);
+        if (st == ED_OK && !(nn[0] > 0.0)) st = ED_ERR_ARG;  // the states are not independent
+        if (st == ED_OK) {
+            const double c[2] = {1.0 - 1.0 / std::sqrt(nn[0]), 0.0};  // y = x - c x = x / |x|
+            if (cudaMemcpyAsync(coef, c, sizeof(double) * 2, cudaMemcpyHostToDevice, s) != cudaSuccess) st = ED_ERR_CUDA;
+            ed::k_project<<<ob_grid(n), kObThreads, 0, s>>>(col(sv, i), col(sv, i), coef, n, cplx ? 1 : 0,
+                                                           wcol(sv, i));
+        }
+    }
+    psis = sv;
+    // phi_j = dH psi_j, D1_ij = <psi_i|phi_j>
+    for (int j = 0; j < g && st == ED_OK; ++j) st = ed_op_perform(dH, col(psis, j), wcol(phi, j), ED_MEM_DEVICE, s);
+    for (int i = 0; i < g && st == ED_OK; ++i)
+        for (int j = 0; j < g && st == ED_OK; ++j) st = dev_dot(col(psis, i), col(phi, j), n, cplx, &D1[2 * (i * g + j)], s);
+    // b_j = phi_j - sum_i psi_i D1_ij (the ground subspace projected out);
+    // each coefficient is copied in stream order before the kernel using it
+    for (int j = 0; j < g && st == ED_OK; ++j) {
+        if (cudaMemcpyAsync(wcol(bv, j), col(phi, j), sizeof(double) * nd, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            st = ED_ERR_CUDA;
+        for (int i = 0; i < g && st == ED_OK; ++i) {
+            const double c[2] = {D1[2 * (i * g + j)], cplx ? D1[2 * (i * g + j) + 1] : 0.0};
+            if (cudaMemcpyAsync(coef, c, sizeof(double) * 2, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+                st = ED_ERR_CUDA;
+                break;
+            }
+            ed::k_project<<<ob_grid(n), kObThreads, 0, s>>>(col(bv, j), col(psis, i), coef, n, cplx ? 1 : 0,
+                                                           wcol(bv, j));
+        }
+    }
+    // E2_ij = <psi_i|d2H|psi_j> (phi reused as d2H psi_j)
+    for (int j = 0; j < g && st == ED_OK; ++j) st = ed_op_perform(d2H, col(psis, j), wcol(phi, j), ED_MEM_DEVICE, s);
+    for (int i = 0; i < g && st == ED_OK; ++i)
+        for (int j = 0; j < g && st == ED_OK; ++j) st = dev_dot(col(psis, i), col(phi, j), n, cplx, &E2[2 * (i * g + j)], s);
+    // resolvent forms: R(b_i) on the diagonal; off the diagonal by
+    // polarisation, Re R_ij = (R(b_i + b_j) - R(b_i) - R(b_j)) / 2 and
+    // Im R_ij = -(R(b_i + i b_j) - R(b_i) - R(b_j)) / 2
+    for (int i = 0; i < g && st == ED_OK; ++i) st = resolvent_form(H, col(bv, i), e0, steps, &Rd[i], s);
+    for (int i = 0; i < g && st == ED_OK; ++i) {
+        R[2 * (i * g + i)] = Rd[i];
+        for (int j = i + 1; j < g && st == ED_OK; ++j) {
+            for (int part = 0; part < (cplx ? 2 : 1) && st == ED_OK; ++part) {
+                // x = b_i - c b_j with c = -1 (sum) or -i (b_i + i b_j)
+                const double c[2] = {part ? 0.0 : -1.0, part ? -1.0 : 0.0};
+                if (cudaMemcpyAsync(coef, c, sizeof(double) * 2, cudaMemcpyHostToDevice, s) != cudaSuccess) {
+                    st = ED_ERR_CUDA;
+                    break;
+                }
+                ed::k_project<<<ob_grid(n), kObThreads, 0, s>>>(col(bv, i), col(bv, j), coef, n, cplx ? 1 : 0, x);
+                double r = 0.0;
+                st = resolvent_form(H, x, e0, steps, &r, s);
+                const double v = 0.5 * (r - Rd[i] - Rd[j]);
+                if (part == 0) {
+                    R[2 * (i * g + j)] = v;
+                    R[2 * (j * g + i)] = v;
+                } else {
+                    R[2 * (i * g + j) + 1] = -v;
+                    R[2 * (j * g + i) + 1] = v;
+                }
+            }
+        }
+    }
+    if (st == ED_OK) {
+        for (int k = 0; k < 2 * g * g; ++k) {
+            d1[k] = D1[k];
+            d2m[k] = E2[k] - 2.0 * R[k];
+        }
+        if (!cplx)
+            for (int k = 0; k < g * g; ++k) d1[2 * k + 1] = d2m[2 * k + 1] = 0.0;
+    }
+    cudaFreeAsync(sv, s);
+    cudaFreeAsync(phi, s);
+    cudaFreeAsync(bv, s);
+    cudaFreeAsync(x, s);
     cudaFreeAsync(coef, s);
     cudaStreamSynchronize(s);
     return st;

@@ -315,6 +315,65 @@ class Lanczos:
         return res.e0, evec
 
 
+def lanczos_multi(ops: Sequence[Hubbard], max_steps: int, starts=None, ritz: bool = True, evec_out=None,
+                  seed: int = 0, results: Optional[list] = None):
+    """ed_lanczos_batch over operators of any sectors, real or complex (up to
+    16, one persistent launch).  starts: None (run b from Philox(seed + b)) or
+    a float64 CUDA tensor holding the start vectors one after another (rows_b
+    values each, 2 rows_b interleaved for complex operators).  evec_out: a
+    float64 CUDA tensor of the same packed layout for the Ritz vectors (or
+    None: numpy arrays are returned).  Returns (e0 [B], evecs as a list of
+    per-run views, alpha [B, max_steps], beta [B, max_steps + 1])."""
+    lib = _capi.load()
+    B = len(ops)
+    sizes = [op.rows() * (2 if op.is_complex else 1) for op in ops]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    cfg = _capi.ed_lanczos_cfg()
+    cfg.max_steps = int(max_steps)
+    cfg.mode = _capi.ED_LANCZOS_FIXED
+    cfg.reorth = 0
+    cfg.ritz = _capi.ED_RITZ_STORED if ritz else _capi.ED_RITZ_NONE
+    cfg.seed = int(seed)
+    handles = (C.c_void_p * B)(*[op.handle for op in ops])
+    st_ptr, st_mem = None, _capi.ED_MEM_HOST
+    if starts is not None:
+        if isinstance(starts, np.ndarray):
+            f = np.ascontiguousarray(starts, dtype=np.float64).reshape(-1)
+            st_ptr = _ptr(f)
+        else:
+            st_ptr, st_mem = C.c_void_p(starts.data_ptr()), _capi.ED_MEM_DEVICE
+        cfg.start = _capi.ED_START_USER
+    else:
+        cfg.start = _capi.ED_START_RANDOM
+    evecs, ev_ptr, ev_mem = None, None, _capi.ED_MEM_HOST
+    if ritz:
+        if evec_out is not None:
+            evecs, ev_ptr, ev_mem = evec_out, C.c_void_p(evec_out.data_ptr()), _capi.ED_MEM_DEVICE
+        else:
+            evecs = np.empty(int(offs[-1]))
+            ev_ptr = _ptr(evecs)
+    alpha = np.zeros((B, max_steps))
+    beta = np.zeros((B, max_steps + 1))
+    res = (_capi.ed_lanczos_result * B)()
+    check(lib.ed_lanczos_batch(handles, B, C.byref(cfg), st_ptr, st_mem, ev_ptr, ev_mem, _ptr(alpha), _ptr(beta),
+                               res, None), "ed_lanczos_batch")
+    if results is not None:
+        results.extend(res)
+    views = None
+    if ritz:
+        views = []
+        for b, op in enumerate(ops):
+            v = evecs[int(offs[b]):int(offs[b + 1])]
+            if op.is_complex:
+                if isinstance(v, np.ndarray):
+                    v = v.view(np.complex128)
+                else:
+                    import torch
+                    v = v.view(torch.complex128)
+            views.append(v)
+    return np.array([r.e0 for r in res]), views, alpha, beta
+
+
 def lanczos_batch(ops: Sequence[Hubbard], max_steps: int, seed: int = 0, starts: Optional[np.ndarray] = None,
                   ritz: bool = True, evec_out=None, results: Optional[list] = None):
     """ed_lanczos_batch: fixed-step Lanczos of up to 8 operators that share

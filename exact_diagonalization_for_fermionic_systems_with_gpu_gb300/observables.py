@@ -97,6 +97,51 @@ def response(H: Hubbard, dH: Hubbard, d2H: Optional[Hubbard], psi, e0: float, st
     return first.value, (second.value if d2H is not None else None)
 
 
+def response_batch(Hs: Sequence[Hubbard], dHs: Sequence[Hubbard], d2Hs: Sequence[Hubbard], psis, e0s,
+                   steps: int = 200):
+    """ed_response_batch: (first [n], second [n]) for n operators whose
+    normalised ground states psis (a float64 CUDA tensor) holds one after
+    another; the n linear-response Lanczos runs share one launch."""
+    n = len(Hs)
+    arr = lambda ops: (C.c_void_p * n)(*[o.handle for o in ops])  # noqa: E731
+    e0 = np.ascontiguousarray(e0s, dtype=np.float64)
+    first = np.zeros(n)
+    second = np.zeros(n)
+    check(_capi.load().ed_response_batch(arr(Hs), arr(dHs), arr(d2Hs), n, C.c_void_p(psis.data_ptr()),
+                                         C.c_void_p(e0.ctypes.data), steps, C.c_void_p(first.ctypes.data),
+                                         C.c_void_p(second.ctypes.data), None), "ed_response_batch")
+    return first, second
+
+
+def response_subspace(H: Hubbard, dH: Hubbard, d2H: Hubbard, psis, e0: float, steps: int = 200):
+    """ed_response_subspace: (D1, M), the g x g first- and second-order
+    matrices over the ground subspace spanned by the g states psis (a (g,
+    rows) CUDA tensor, complex for complex operators); see lowest_branch."""
+    g = int(psis.shape[0])
+    a = psis.contiguous()
+    d1 = np.zeros(2 * g * g)
+    d2 = np.zeros(2 * g * g)
+    check(_capi.load().ed_response_subspace(H.handle, dH.handle, d2H.handle, C.c_void_p(a.data_ptr()), g, e0, steps,
+                                            C.c_void_p(d1.ctypes.data), C.c_void_p(d2.ctypes.data), None),
+          "ed_response_subspace")
+    return d1.view(np.complex128).reshape(g, g), d2.view(np.complex128).reshape(g, g)
+
+
+def lowest_branch(D1: np.ndarray, M: np.ndarray, tol: float = 1e-9):
+    """(dE0/dtheta, d2E0/dtheta2) of the lowest branch of a degenerate level:
+    the lowest eigenvalue of the first-order matrix D1 and, when D1 splits
+    nothing (all its eigenvalues equal within tol), the lowest eigenvalue of
+    the second-order matrix M; otherwise M's expectation value in D1's lowest
+    eigenvector."""
+    D1 = 0.5 * (D1 + D1.conj().T)
+    M = 0.5 * (M + M.conj().T)
+    w1, v1 = np.linalg.eigh(D1)
+    if w1[-1] - w1[0] <= tol * max(1.0, abs(w1[0])):
+        return float(w1[0]), float(np.linalg.eigvalsh(M)[0])
+    c = v1[:, 0]
+    return float(w1[0]), float(np.real(np.vdot(c, M @ c)))
+
+
 def entanglement_entropy(op: Hubbard, psi, a_sites: Sequence[int]):
     """(S_vN, S_ref) for the sites in a_sites."""
     mask = 0

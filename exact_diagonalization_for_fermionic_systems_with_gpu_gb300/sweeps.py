@@ -40,7 +40,7 @@ import numpy as np
 
 from . import lattices as L
 from . import observables as ob
-from .hubbard import H_TBq, Hubbard, Lanczos, lanczos_batch, random_vector
+from .hubbard import H_TBq, Hubbard, Lanczos, lanczos_batch, lanczos_multi, random_vector
 
 
 @dataclass
@@ -102,21 +102,49 @@ def _ground(H: Hubbard, steps: int, mode: str, seed: int):
     return e0, evec, int(lz.result.steps), int(lz.result.min_bits)
 
 
+# Lanczos steps of a twist's ground state (fixed) and of its response solve.
+# The twisted Kagome12 ground level comes within 0.014 of the next one
+# (near Phi = 0.73, the pair split from the zero-twist doublet); the
+# second-order response needs the ground state to about 1e-9 there, which
+# 300 steps do not give and 500 do.
+FLUX_STEPS = 500
+FLUX_RESPONSE_STEPS = 200
+
+
+def _real_twist(phi: float) -> bool:
+    """Every bond phase phi * dx_b is a multiple of pi: the operator is real
+    and time-reversal symmetric, where the ground level can be degenerate."""
+    return all(abs(math.sin(phi * dx)) < 1e-15 for dx in L.KAGOME12_DX)
+
+
 def flux_phis(n_phi: int = 16) -> np.ndarray:
     """n_phi twists evenly spaced over [0, 2 pi / KAGOME12_LX], both ends included."""
     return np.linspace(0.0, 2.0 * math.pi / L.KAGOME12_LX, n_phi)
 
 
 def flux_sweep(phis: Optional[Sequence[float]] = None, n_up: int = 6, n_dn: int = 6, U: float = 4.0,
-               steps: int = 300, mode: str = "fixed", response_steps: int = 200, seed: int = 0,
+               steps: int = FLUX_STEPS, mode: str = "fixed", response_steps: int = FLUX_RESPONSE_STEPS, seed: int = 0,
                rand: Optional[Sequence[float]] = None, timing: Optional[SweepTiming] = None,
-               autotune: bool = False) -> List[FluxPoint]:
+               autotune: bool = False, batch: int = 1) -> List[FluxPoint]:
     """E0(Phi), dE0/dPhi, d2E0/dPhi2 of Kagome12 (complex operator at every
     Phi, Phi = 0 included, so the second-order response sees the current).
+    At twists where the operator is real a second ground state from another
+    start vector tests the ground level for a two-fold degeneracy (the zero
+    twist of the 6+6 sector is one); a degenerate level gets the derivatives
+    of its lowest branch from ed_response_subspace.
     autotune: time the Lanczos kernel choices on the first twist's operator
-    and apply the fastest to every twist (same shape, same tables)."""
+    and apply the fastest to every twist (same shape, same tables).
+    batch > 1 (fixed-step mode): up to `batch` (<= 16) twists share one
+    persistent Lanczos launch for their ground states and one for their
+    response solves (ed_lanczos_batch, ed_response_batch); the same start
+    vectors, so the same results bit for bit."""
     phis = flux_phis() if phis is None else phis
     t = timing if timing is not None else SweepTiming()
+    if batch > 1 and mode == "fixed":
+        t0 = time.perf_counter()
+        out = _flux_batched(list(phis), n_up, n_dn, U, steps, response_steps, seed, rand, min(batch, 16), t)
+        t.total_s += time.perf_counter() - t0
+        return out
     out: List[FluxPoint] = []
     tuned = None
     t0 = time.perf_counter()
@@ -137,7 +165,15 @@ def flux_sweep(phis: Optional[Sequence[float]] = None, n_up: int = 6, n_dn: int 
         e0, psi, n, bits = _ground(H, steps, mode, seed * 4096 + k)
         _sync()
         tl = time.perf_counter()
-        d1, d2 = ob.response(H, dH, d2H, psi, e0, steps=response_steps)
+        states = [psi]
+        if _real_twist(float(phi)):
+            states = ground_multiplet(H, psi, e0, steps, mode, seed * 4096 + k)
+        if len(states) > 1:
+            import torch
+            D1, M = ob.response_subspace(H, dH, d2H, torch.stack(states), e0, steps=response_steps)
+            d1, d2 = ob.lowest_branch(D1, M)
+        else:
+            d1, d2 = ob.response(H, dH, d2H, psi, e0, steps=response_steps)
         _sync()
         te = time.perf_counter()
         for op in (H, dH, d2H):
@@ -150,6 +186,106 @@ def flux_sweep(phis: Optional[Sequence[float]] = None, n_up: int = 6, n_dn: int 
         t.observables_s += te - tl
         t.per_instance.append(te - ti)
     t.total_s += time.perf_counter() - t0
+    return out
+
+
+def ground_multiplet(H: Hubbard, psi, e0: float, steps: int, mode: str, seed: int, max_states: int = 4):
+    """The ground level's states as far as Lanczos runs from further start
+    vectors find new directions: each run whose Ritz value equals E0 (1e-10)
+    and whose state keeps more than 1e-4 of its norm outside the span of the
+    states found so far adds it; the first run that adds nothing ends the
+    search.  A non-degenerate level costs one extra run."""
+    states = [psi]
+    for extra in range(1, max_states):
+        e0b, psib, _, _ = _ground(H, steps, mode, seed + 2048 * extra)
+        if abs(e0b - e0) > 1e-10 * abs(e0):
+            break
+        g = len(states)
+        G = np.empty((g, g), dtype=np.complex128)
+        for i in range(g):
+            for j in range(g):
+                G[i, j] = complex(*_zdot(states[i], states[j]))
+        c = np.array([complex(*_zdot(states[i], psib)) for i in range(g)])
+        nb = complex(*_zdot(psib, psib)).real
+        outside = nb - float(np.real(np.vdot(c, np.linalg.solve(G, c))))
+        if not outside > 1e-8 * nb:  # 1e-4 of the norm
+            break
+        states.append(psib)
+    return states
+
+
+def _zdot(x, y):
+    """<x|y> of two CUDA tensors through the library (re, im)."""
+    from ._capi import load
+    out = np.zeros(2)
+    n = x.numel()
+    if x.is_complex():
+        check_ = load().ed_vec_zdot(int(n), C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), 1,
+                                    C.c_void_p(out.ctypes.data), None)
+    else:
+        check_ = load().ed_vec_dot(int(n), C.c_void_p(x.data_ptr()), C.c_void_p(y.data_ptr()), 1,
+                                   C.c_void_p(out.ctypes.data), None)
+    if check_ != 0:
+        from ._capi import EdError
+        raise EdError(check_, "ed_vec_(z)dot")
+    return out[0], out[1]
+
+
+def _flux_batched(phis, n_up, n_dn, U, steps, response_steps, seed, rand, batch, t) -> List[FluxPoint]:
+    import torch
+    from ._capi import load
+    lib = load()
+    out: List[FluxPoint] = []
+    for g0 in range(0, len(phis), batch):
+        group = [(g0 + i, float(p)) for i, p in enumerate(phis[g0:g0 + batch])]
+        ti = time.perf_counter()
+        Hs, dHs, d2Hs = [], [], []
+        for k, phi in group:
+            terms = L.kagome12(rand, flux=phi, peierls=True)
+            d1t, d2t = L.kagome12_flux_derivatives(phi, rand)
+            Hs.append(Hubbard(H_TBq(12, n_up).extend(terms), H_TBq(12, n_dn).extend(terms), U))
+            dHs.append(Hubbard(H_TBq(12, n_up).extend(d1t), H_TBq(12, n_dn).extend(d1t), 0.0))
+            d2Hs.append(Hubbard(H_TBq(12, n_up).extend(d2t), H_TBq(12, n_dn).extend(d2t), 0.0))
+        sizes = [2 * H.rows() for H in Hs]
+        offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        starts = torch.empty(int(offs[-1]), dtype=torch.float64, device="cuda")
+        for (k, _), o, n in zip(group, offs, sizes):
+            lib.ed_random_vector_device(int(n), seed * 4096 + k, C.c_void_p(starts[int(o)].data_ptr()), None)
+        evecs = torch.empty_like(starts)
+        _sync()
+        tb = time.perf_counter()
+        results: list = []
+        e0s, views, _, _ = lanczos_multi(Hs, steps, starts=starts, evec_out=evecs, results=results)
+        _sync()
+        tl = time.perf_counter()
+        d1s, d2s, normal = [0.0] * len(group), [0.0] * len(group), []
+        for i, (k, phi) in enumerate(group):
+            if _real_twist(phi):
+                states = ground_multiplet(Hs[i], views[i], float(e0s[i]), steps, "fixed", seed * 4096 + k)
+                if len(states) > 1:
+                    D1, M = ob.response_subspace(Hs[i], dHs[i], d2Hs[i], torch.stack(states), float(e0s[i]),
+                                                 steps=response_steps)
+                    d1s[i], d2s[i] = ob.lowest_branch(D1, M)
+                    continue
+            normal.append(i)
+        if normal:
+            psis = torch.cat([evecs[int(offs[i]):int(offs[i + 1])] for i in normal])
+            f, sec = ob.response_batch([Hs[i] for i in normal], [dHs[i] for i in normal], [d2Hs[i] for i in normal],
+                                       psis, [float(e0s[i]) for i in normal], steps=response_steps)
+            for j, i in enumerate(normal):
+                d1s[i], d2s[i] = float(f[j]), float(sec[j])
+        _sync()
+        te = time.perf_counter()
+        for i, (k, phi) in enumerate(group):
+            out.append(FluxPoint(phi, float(e0s[i]), d1s[i], d2s[i], steps, int(results[i].min_bits)))
+        for op in Hs + dHs + d2Hs:
+            op.close()
+        t.instances += len(group)
+        t.lanczos_steps += steps * len(group)
+        t.build_s += tb - ti
+        t.lanczos_s += tl - tb
+        t.observables_s += te - tl
+        t.per_instance.extend([(te - ti) / len(group)] * len(group))
     return out
 
 
@@ -316,12 +452,15 @@ PLAIN_SAME_EE_ENV = {"ED_MATVEC": "generic", "ED_LZ_FUSED": "0"}
 FORM_ENV = {"tuned": {}, "plain": PLAIN_ENV, "plain_same_ee": PLAIN_SAME_EE_ENV}
 
 
-def run_form(what: str, n: int, form: str, steps: int = 300, mode: str = "fixed", seed: int = 0, warmup: int = 1,
-             batch: int = 8):
+def run_form(what: str, n: int, form: str, steps: Optional[int] = None, mode: str = "fixed", seed: int = 0,
+             warmup: int = 1, batch: int = 8):
     """One sweep (what = "flux" | "mbl") in one form of FORM_ENV: the tuned
-    form autotunes the twist operators and batches disorder realisations,
-    the plain forms run one instance per launch sequence.  Returns
-    (points, SweepTiming)."""
+    form batches twists (2 * batch per launch, at most 16) and disorder
+    realisations (batch per launch), the plain forms run one instance per
+    launch sequence.  steps: Lanczos steps per instance (None: FLUX_STEPS
+    for twists, 300 for disorder samples).  Returns (points, SweepTiming)."""
+    if steps is None:
+        steps = FLUX_STEPS if what == "flux" else 300
     import os
     env = FORM_ENV[form]
     keys = set(PLAIN_ENV) | set(env)
@@ -332,10 +471,10 @@ def run_form(what: str, n: int, form: str, steps: int = 300, mode: str = "fixed"
     try:
         tm = SweepTiming()
         if what == "flux":
-            tune = form == "tuned"
+            fb = min(batch * 2, 16) if form == "tuned" else 1
             if warmup:
-                flux_sweep(flux_phis(n)[:warmup], steps=steps, mode=mode, seed=seed, autotune=tune)
-            pts = flux_sweep(flux_phis(n), steps=steps, mode=mode, seed=seed, timing=tm, autotune=tune)
+                flux_sweep(flux_phis(n)[:max(warmup, 2)], steps=steps, mode=mode, seed=seed, batch=fb)
+            pts = flux_sweep(flux_phis(n), steps=steps, mode=mode, seed=seed, timing=tm, batch=fb)
         else:
             bt = batch if form == "tuned" else 1
             if warmup:
@@ -358,7 +497,7 @@ def main(argv: Optional[Sequence[str]] = None) -> None:
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--what", choices=["flux", "mbl"], default="mbl")
     ap.add_argument("--n", type=int, default=None, help="flux points (16) or realisations (64)")
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=None, help="Lanczos steps (default: 500 twists, 300 disorder)")
     ap.add_argument("--mode", choices=["fixed", "reference"], default="fixed")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=1, help="instances run (untimed) before the sweep")

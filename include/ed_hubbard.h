@@ -237,19 +237,23 @@ ed_status ed_lanczos_run(ed_op* op, const ed_lanczos_cfg* cfg,
  * zeroed matrix).  rows <= 65536.  H at mem; synchronous. */
 ed_status ed_op_write_dense(ed_op* op, double* H, int mem, void* stream);
 
-/* n_ops (1..8) fixed-step Lanczos runs in one persistent launch, for
- * operators that share their hopping tables (same sector and lattice terms;
- * the on-site terms, U and so the folded diagonals may differ): the
- * disorder realisations of one sector, the batched form of the sweeps that
- * call Lanczos::eigen once per realisation (MBL_test/src/Hubbard_EE_test.cu:
- * 62-72, TotalSpinExcited_Lieb_randomHop.cu:110-136).  Real operators with one
- * hopping class and a shared-memory plan (else ED_ERR_NOT_BUILT).  cfg: mode
- * ED_LANCZOS_FIXED, no reorthogonalisation, ritz ED_RITZ_STORED (evecs:
- * n_ops x rows at evec_mem) or ED_RITZ_NONE; start ED_START_RANDOM (run b
- * seeded cfg->seed + b) or ED_START_USER (starts: n_ops x rows at start_mem).
- * alpha (n_ops x max_steps), beta (n_ops x (max_steps+1)) and res (n_ops) are
- * optional host outputs; each run's coefficients equal those of its own
- * ed_lanczos_run bit for bit.  Synchronous. */
+/* n_ops (1..16) fixed-step Lanczos runs in one persistent launch: the
+ * batched form of the sweeps that call Lanczos::eigen once per disorder
+ * realisation, sector or twist (MBL_test/src/Hubbard_EE_test.cu:62-72,
+ * TotalSpinExcited_Lieb_randomHop.cu:110-136,
+ * drude_v2_cal_Kagome_randomHop.cu:129-158).  The operators may belong to
+ * different (N_up, N_dn) sectors of uneven dimension and be real or complex;
+ * each needs a shared-memory plan (not the two-pass matvec of the largest
+ * sectors; else ED_ERR_NOT_BUILT).  Up to 8 real one-class operators that
+ * share their hopping tables run in a kernel specialised for that case,
+ * anything else in the general one.  cfg: mode ED_LANCZOS_FIXED, no
+ * reorthogonalisation, ritz ED_RITZ_STORED or ED_RITZ_NONE; start
+ * ED_START_RANDOM (run b seeded cfg->seed + b) or ED_START_USER.  starts and
+ * evecs (at start_mem / evec_mem) hold the runs one after another, rows_b
+ * values each (2*rows_b for complex operators: n_ops x rows when all are
+ * equal); alpha (n_ops x max_steps), beta (n_ops x (max_steps+1)) and res
+ * (n_ops) are optional host outputs; each run's coefficients, E0 and Ritz
+ * vector equal those of its own ed_lanczos_run bit for bit.  Synchronous. */
 ed_status ed_lanczos_batch(ed_op* const* ops, int n_ops, const ed_lanczos_cfg* cfg, const double* starts,
                            int start_mem, double* evecs, int evec_mem, double* alpha, double* beta,
                            ed_lanczos_result* res, void* stream);
@@ -384,6 +388,34 @@ ed_status ed_drude_kubo(ed_op* H, ed_op* J, ed_op* K, const double* psi, double 
  * theta = Phi this is d2E0/dPhi2, the Drude weight without broadening. */
 ed_status ed_response(ed_op* H, ed_op* dH, ed_op* d2H, const double* psi, double e0, int steps, double* first,
                       double* second, void* stream);
+
+/* ed_response for n (1..16) operators at once, e.g. the twists of a flux
+ * sweep: psis holds the n normalised ground states one after another (rows
+ * values each, 2*rows for complex), device memory; e0, first, second are
+ * host arrays of n.  The n linear-response Lanczos runs share one persistent
+ * launch (the batched form of ed_lanczos_batch; one run each when the
+ * operators have no persistent plan).  d2H and second may be NULL together.
+ * Synchronous.  No counterpart in the reference (its drivers loop over
+ * drude_weight_Jx, drude_v2_cal_Kagome_randomHop.cu:129-158). */
+ed_status ed_response_batch(ed_op* const* H, ed_op* const* dH, ed_op* const* d2H, int n, const double* psis,
+                            const double* e0, int steps, double* first, double* second, void* stream);
+
+/* The same response for a degenerate ground level (a multiplet the reference
+ * drivers do not treat: they differentiate whichever ground state Lanczos
+ * returns, e.g. at the zero twist of drude_v2_cal_Kagome_randomHop.cu:
+ * 129-158, where Kagome12 6+6 is two-fold degenerate).  psis: g (1..4)
+ * linearly independent ground states, one after another (rows values each,
+ * 2*rows for complex operators), device memory; the call orthonormalises a
+ * copy of them in order (S below; ED_ERR_ARG when they are dependent).
+ * Outputs, g x g complex row-major
+ * (interleaved re, im; host):
+ *   d1  = S^H dH S                                  (first-order matrix)
+ *   d2m = S^H d2H S - 2 B^H (Q (H - E0) Q)^-1 B,     B = Q dH S, Q = 1 - S S^H
+ * with each resolvent form from a `steps`-step Lanczos run (off-diagonal
+ * elements by polarisation).  The branch derivatives of E0(theta) are the
+ * eigenvalues of d1 and, where d1 vanishes, of d2m.  Synchronous. */
+ed_status ed_response_subspace(ed_op* H, ed_op* dH, ed_op* d2H, const double* psis, int g, double e0, int steps,
+                               double* d1, double* d2m, void* stream);
 /* Entanglement entropy of psi for the sites in a_mask: the matrix
  * psi[(a_up a_dn), (b_up b_dn)] (entangle_entropy.h:177-197) is block-diagonal
  * in the particle numbers of A; singular values s of every block from a

@@ -118,6 +118,45 @@ def test_drude_kubo_matches_oracle(ed, orc):
     assert np.max(np.abs(run)) < 2e-3 * np.sum(np.abs(sig)) * 0.004
 
 
+def test_response_subspace_of_degenerate_level_vs_dense(ed, orc):
+    """Kagome12 2+2 at zero twist has a three-fold ground level.  The device
+    first- and second-order matrices over it (ed_response_subspace, given
+    the dense ground states in a random unitary mix) against the dense
+    degenerate perturbation theory: their eigenvalues (basis independent) to
+    1e-8, and the flux sweep's lowest branch at Phi = 0 (which finds the
+    multiplet with Lanczos runs from further start vectors) to 1e-8."""
+    import torch
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob, sweeps
+    N, q, U = 12, 2, 4.0
+    terms = L.kagome12(flux=0.0, peierls=True)
+    d1t, d2t = L.kagome12_flux_derivatives(0.0)
+    Hd = orc.hamiltonian(N, q, q, terms, terms, U).toarray()
+    A1 = orc.hamiltonian(N, q, q, d1t, d1t, 0.0).toarray()
+    A2 = orc.hamiltonian(N, q, q, d2t, d2t, 0.0).toarray()
+    w, V = np.linalg.eigh(Hd)
+    g = int(np.sum(w - w[0] < 1e-9))
+    assert g == 3
+    S = V[:, :g]
+    D1 = S.conj().T @ A1 @ S
+    C = V[:, g:].conj().T @ (A1 @ S)
+    M = S.conj().T @ A2 @ S - 2 * (C.conj().T @ (C / (w[g:] - w[0])[:, None]))
+    rng = np.random.default_rng(4)
+    Uq, _ = np.linalg.qr(rng.standard_normal((g, g)) + 1j * rng.standard_normal((g, g)))
+    psis = torch.from_numpy(np.ascontiguousarray((S @ Uq).T)).to("cuda")
+    H = ed.Hubbard(ed.H_TBq(N, q).extend(terms), ed.H_TBq(N, q).extend(terms), U)
+    dH = ed.Hubbard(ed.H_TBq(N, q).extend(d1t), ed.H_TBq(N, q).extend(d1t), 0.0)
+    d2H = ed.Hubbard(ed.H_TBq(N, q).extend(d2t), ed.H_TBq(N, q).extend(d2t), 0.0)
+    D1g, Mg = ob.response_subspace(H, dH, d2H, psis, float(w[0]), steps=200)
+    assert np.allclose(np.linalg.eigvalsh(0.5 * (D1g + D1g.conj().T)), np.linalg.eigvalsh(0.5 * (D1 + D1.conj().T)),
+                       atol=1e-9, rtol=0)
+    assert np.allclose(np.linalg.eigvalsh(0.5 * (Mg + Mg.conj().T)), np.linalg.eigvalsh(0.5 * (M + M.conj().T)),
+                       atol=1e-8, rtol=1e-8)
+    d1_ref, d2_ref = ob.lowest_branch(D1, M)
+    p = sweeps.flux_sweep([0.0], n_up=q, n_dn=q, U=U)[0]
+    assert abs(p.e0 - w[0]) < 1e-10 * abs(w[0])
+    assert abs(p.d1 - d1_ref) < 1e-9 and abs(p.d2 - d2_ref) < 1e-8 * max(1.0, abs(d2_ref))
+
+
 @pytest.mark.parametrize("flux", [0.3, 1.1])
 def test_flux_response_vs_dense_sum_over_states(ed, orc, flux):
     """dE0/dPhi and d2E0/dPhi2 from the device (Hellmann-Feynman + a
