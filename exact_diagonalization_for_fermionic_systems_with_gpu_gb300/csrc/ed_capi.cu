@@ -231,6 +231,8 @@ static ed_status plan_striped(ed_op* op, bool forced) {
     std::vector<uint16_t> s16;
     int64_t zbase = 0;
     if (!ed::window_schedule16(g, op->dimDN, chunk, bw, &s16, &zbase)) return ED_OK;
+    const int64_t sched_steps = std::max(g.steps, 1);
+    const std::vector<uint16_t> s16bm = ed::block_major16(s16, g.count_pad, sched_steps);
     const int Fc = op->mv.Fc;
     std::vector<int64_t> dq((size_t)op->dimDN);
     std::vector<uint64_t> st((size_t)op->dimDN);
@@ -239,7 +241,7 @@ static ed_status plan_striped(ed_op* op, bool forced) {
         st[c] = op->bdn.state[perm[c]];
     }
     if (upload(&op->d_permDN, perm.data(), perm.size()) != cudaSuccess ||
-        upload(&op->d_sched16, s16.data(), s16.size()) != cudaSuccess ||
+        upload(&op->d_sched16, s16bm.data(), s16bm.size()) != cudaSuccess ||
         upload(&op->d_steps32, g.steps32.data(), g.steps32.size()) != cudaSuccess ||
         upload(&op->d_dDNqP, dq.data(), dq.size()) != cudaSuccess ||
         upload(&op->d_stDNp, st.data(), st.size()) != cudaSuccess)
@@ -253,6 +255,10 @@ static ed_status plan_striped(ed_op* op, bool forced) {
     op->st_win = (int)(zbase + 16);
     op->st_zbase = (int)zbase;
     op->st_cpad = g.count_pad;
+    op->st_smax = (int)sched_steps;
+    int maxlen = 0;
+    for (int64_t u = 0; u < op->dimUP; ++u) maxlen = std::max<int>(maxlen, op->tup.len[u]);
+    op->st_up_maxlen = maxlen;
     return ED_OK;
 }
 

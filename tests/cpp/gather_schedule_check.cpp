@@ -235,6 +235,14 @@ static int check(const char* name, int n, int q, const std::vector<ed_term>& ter
                 std::printf("%s window schedule shape\n", name);
                 return 1;
             }
+            // the block-major copy k_mv_down reads: word (c, st) at ((c / 32) nst + st) 32 + c % 32
+            const std::vector<uint16_t> bm = block_major16(s16, cpd, nst);
+            for (int64_t c = 0; c < cpd; ++c)
+                for (int64_t st = 0; st < nst; ++st)
+                    if (bm[(size_t)(((c / 32) * nst + st) * 32 + c % 32)] != s16[(size_t)(st * cpd + c)]) {
+                        std::printf("%s block-major schedule\n", name);
+                        return 1;
+                    }
             for (int64_t c = 0; c < cpd; ++c) {
                 const int64_t k = c / chunk;
                 const int64_t w0 = std::max<int64_t>(0, k * chunk - bw2) & ~(int64_t)15;

@@ -30,7 +30,8 @@ def _ops(ed):
 def test_mixed_sector_mixed_kind_batch_equals_single_runs(ed, edlib, steps):
     import torch
     ops = _ops(ed)
-    assert len({(op.dimUP, op.dimDN, op.is_complex) for op in ops}) == 5
+    # four shapes (924^2, 792^2, 495^2 real; 792^2 complex), five table groups
+    assert len({(op.dimUP, op.dimDN, op.is_complex) for op in ops}) == 4
     sizes = [op.rows() * (2 if op.is_complex else 1) for op in ops]
     offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
     starts = torch.empty(int(offs[-1]), dtype=torch.float64, device="cuda")
