@@ -296,6 +296,7 @@ def sweep_record() -> dict:
     t = out["forms"]["tuned"]["total_s"]
     out["speedup_vs_plain"] = round(out["forms"]["plain"]["total_s"] / t, 3)
     out["speedup_vs_plain_same_entropy"] = round(out["forms"]["plain_same_ee"]["total_s"] / t, 3)
+    out["batch_sizes"] = sweeps.batch_choices()
     out["err_vs_oracle_max"] = worst
     out["err_vs_oracle_instances"] = len(table)
     out["min_bits"] = bits

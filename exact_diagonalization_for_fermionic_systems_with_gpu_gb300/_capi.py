@@ -74,7 +74,9 @@ class ed_tune_cfg(C.Structure):
 
 class ed_tune_result(C.Structure):
     _fields_ = [("persistent", C.c_int32), ("candidates", C.c_int32), ("row_cost", C.c_double),
-                ("us_per_step", C.c_double), ("per_step_us", C.c_double), ("persistent_us", C.c_double * 3)]
+                ("us_per_step", C.c_double), ("per_step_us", C.c_double), ("persistent_us", C.c_double * 3),
+                ("ctas_per_sm", C.c_int32), ("chunk", C.c_int32), ("one_cta_us", C.c_double),
+                ("chunk_us", C.c_double * 2)]
 
 
 class ed_eigs_cfg(C.Structure):

@@ -207,7 +207,7 @@ bool gather_schedule_cached(const ed::SpinBasis& b, const ed_term* t, int nt, bo
 
 constexpr int kDegreeBlock = 256;  // columns reordered by hop count within each block
 
-static ed_status plan_striped(ed_op* op, bool forced) {
+static ed_status plan_striped(ed_op* op, bool forced, int64_t chunk_cap = 16384) {
     std::vector<uint32_t> perm, inv;
     int64_t bw = 0;
     ed::rcm_order(op->tdn, &perm, &inv, &bw);
@@ -217,7 +217,7 @@ static ed_status plan_striped(ed_op* op, bool forced) {
     // window of chunk + 2 bw columns (+ alignment) in at most ~220 KB
     const int64_t max_win = 220 * 1024 / 8;
     int64_t chunk = (max_win - 2 * bw - 64) / 1024 * 1024;
-    if (chunk > 16384) chunk = 16384;
+    if (chunk > chunk_cap) chunk = chunk_cap / 1024 * 1024;
     const int64_t dn_pad = (op->dimDN + 1023) / 1024 * 1024;
     if (chunk > dn_pad) chunk = dn_pad;
     if (chunk < 1024) return ED_OK;  // too wide: the generic kernel stays
@@ -240,6 +240,11 @@ static ed_status plan_striped(ed_op* op, bool forced) {
         dq[c] = (int64_t)std::llrint(std::ldexp(op->tdn.diag_re[perm[c]], Fc));
         st[c] = op->bdn.state[perm[c]];
     }
+    // a re-plan (the autotuner's chunk axis) replaces the previous tables
+    cudaFree(op->d_permDN); cudaFree(op->d_sched16); cudaFree(op->d_steps32); cudaFree(op->d_dDNqP);
+    cudaFree(op->d_stDNp);
+    op->d_permDN = nullptr; op->d_sched16 = nullptr; op->d_steps32 = nullptr; op->d_dDNqP = nullptr;
+    op->d_stDNp = nullptr;
     if (upload(&op->d_permDN, perm.data(), perm.size()) != cudaSuccess ||
         upload(&op->d_sched16, s16bm.data(), s16bm.size()) != cudaSuccess ||
         upload(&op->d_steps32, g.steps32.data(), g.steps32.size()) != cudaSuccess ||
@@ -256,9 +261,6 @@ static ed_status plan_striped(ed_op* op, bool forced) {
     op->st_zbase = (int)zbase;
     op->st_cpad = g.count_pad;
     op->st_smax = (int)sched_steps;
-    int maxlen = 0;
-    for (int64_t u = 0; u < op->dimUP; ++u) maxlen = std::max<int>(maxlen, op->tup.len[u]);
-    op->st_up_maxlen = maxlen;
     return ED_OK;
 }
 
@@ -758,8 +760,57 @@ ed_status ed_op_autotune(ed_op* op, const ed_tune_cfg* cfg, ed_tune_result* res,
             }
         }
     }
+    // rows per CTA: the persistent kernel at one CTA per SM (each CTA takes
+    // twice the rows of the two-per-SM grid), at the best weight
+    const int saved_grid = op->lz_grid;
+    r.ctas_per_sm = r.persistent ? 2 : 0;
+    if (st == ED_OK && op->tma_smem > 0 && op->tma_grid > 1) {
+        int sms = 152;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op->device);
+        if (op->tma_grid >= 2 * sms) {
+            op->lz_mode = 2;
+            op->lz_grid = sms;
+            const double w_best = r.persistent ? r.row_cost : weights[1];
+            st = set_row_plan(op, w_best);
+            if (st == ED_OK) st = time_run(&r.one_cta_us);
+            ++r.candidates;
+            if (st == ED_OK && r.one_cta_us < r.us_per_step) {
+                r.us_per_step = r.one_cta_us;
+                r.persistent = 1;
+                r.row_cost = w_best;
+                r.ctas_per_sm = 1;
+            }
+        }
+    }
+    op->lz_grid = saved_grid;
+    // two-pass sectors: pass D's window, the largest chunk and half of it
+    // (the plan is rebuilt for each; the per-step kernels run these sectors)
+    const int saved_chunk = op->striped ? op->st_chunk : 0;
+    if (st == ED_OK && op->striped && saved_chunk >= 2048) {
+        const int chunks[2] = {saved_chunk, saved_chunk / 2};
+        double best = 1e300;
+        int pick = saved_chunk;
+        for (int k = 0; k < 2 && st == ED_OK; ++k) {
+            if (k > 0) st = plan_striped(op, true, chunks[k]);
+            if (st == ED_OK && (!op->striped || op->st_chunk != chunks[k])) break;  // no such plan
+            if (st == ED_OK) st = time_run(&r.chunk_us[k]);
+            ++r.candidates;
+            if (st == ED_OK && r.chunk_us[k] < best) {
+                best = r.chunk_us[k];
+                pick = chunks[k];
+            }
+        }
+        r.chunk = pick;
+        if (st == ED_OK && best < r.us_per_step) r.us_per_step = best;
+        const int keep = (st == ED_OK && cfg->apply) ? pick : saved_chunk;
+        if (op->st_chunk != keep) {
+            const ed_status s2 = plan_striped(op, true, keep);
+            if (st == ED_OK) st = s2;
+        }
+    }
     if (st == ED_OK && cfg->apply) {
         op->lz_mode = r.persistent ? 2 : 1;
+        op->lz_grid = r.ctas_per_sm == 1 ? op->tma_grid / 2 : 0;
         if (op->tma_smem > 0) st = set_row_plan(op, r.persistent ? r.row_cost : saved_w);
     } else {
         op->lz_mode = saved_mode;
@@ -776,6 +827,11 @@ ed_status ed_op_set_tuning(ed_op* op, const ed_tune_result* tuned) {
     if (!op || !tuned) return ED_ERR_ARG;
     if (cudaSetDevice(op->device) != cudaSuccess) return ED_ERR_CUDA;
     op->lz_mode = tuned->persistent ? 2 : 1;
+    op->lz_grid = (tuned->persistent && tuned->ctas_per_sm == 1) ? op->tma_grid / 2 : 0;
+    if (op->striped && tuned->chunk > 0 && tuned->chunk != op->st_chunk) {
+        const ed_status st = plan_striped(op, true, tuned->chunk);
+        if (st != ED_OK) return st;
+    }
     if (op->tma_smem > 0 && tuned->persistent) return set_row_plan(op, tuned->row_cost);
     return ED_OK;
 }

@@ -141,11 +141,11 @@ struct ed_op {
     // two-pass matvec (striped): down index permuted by perm (new -> old)
     bool striped = false;
     int st_grid = 0, st_win = 0, st_chunk = 0, st_zbase = 0;
-    int st_up_maxlen = 0;       // longest up row (pass U's staged gathers hold up to 22)
     int st_smax = 0;            // steps of pass D's schedule (block-major layout)
     // tuning (ed_op_autotune): Lanczos kernels 0 by the default rule, 1 per
     // step, 2 persistent; weight of the persistent kernel's row queue
     int lz_mode = 0;
+    int lz_grid = 0;            // persistent kernel's CTAs (0: tma_grid, two per SM)
     double row_cost = -1.0;
     int64_t st_bw = 0, st_cpad = 0;
     uint32_t* d_permDN = nullptr;

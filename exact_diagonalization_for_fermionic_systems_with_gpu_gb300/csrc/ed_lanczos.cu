@@ -630,7 +630,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             LZ_CK(cudaMemsetAsync(w->gbar, 0, kFusedSync, s));
             LzRedSet* red = reinterpret_cast<LzRedSet*>(reinterpret_cast<char*>(w->gbar) + 32);
             if (stamps) {
-                const size_t need = (size_t)2 * max_steps * op->tma_grid;
+                const size_t need = (size_t)2 * max_steps * (op->lz_grid > 0 ? op->lz_grid : op->tma_grid);
                 if (w->cta_stamps_n < need) {
                     cudaFree(w->cta_stamps);
                     w->cta_stamps = nullptr;
@@ -879,7 +879,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             bar_ms += ms(q[2], q[3]) + ms(q[6], q[7]);
             sc_ms += ms(q[3], q[4]) + ms(q[7], q[8]);
         }
-        const int G = op->tma_grid;
+        const int G = op->lz_grid > 0 ? op->lz_grid : op->tma_grid;
         std::vector<unsigned long long> c((size_t)2 * steps_run * G);
         LZ_CK(cudaMemcpy(c.data(), w->cta_stamps, sizeof(unsigned long long) * c.size(), cudaMemcpyDeviceToHost));
         for (int j2 = 0; j2 < steps_run; ++j2)

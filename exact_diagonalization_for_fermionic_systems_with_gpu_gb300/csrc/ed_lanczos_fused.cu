@@ -984,9 +984,9 @@ cudaError_t launch_lz_fused(const ed_op* op, const LzFusedArgs& f, cudaStream_t 
         return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, op->device)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, op->device)) != cudaSuccess) return e;
-    // the row plan is made for op->tma_grid CTAs, all of which must be resident
-    if (!coop || (int64_t)per_sm * sms < op->tma_grid) return cudaErrorNotSupported;
-    const int64_t g = op->tma_grid;
+    // the work queue takes any grid; every CTA must be resident
+    const int64_t g = op->lz_grid > 0 ? op->lz_grid : op->tma_grid;
+    if (!coop || (int64_t)per_sm * sms < g) return cudaErrorNotSupported;
     MvArgs av = op->mv;
     LzFusedArgs fv = f;
     void* args[] = {&av, &fv};

@@ -29,7 +29,6 @@
 
 #include <algorithm>
 #include <cstdint>
-#include <cstdlib>
 
 #include "ed_device.cuh"
 #include "ed_internal.hpp"
@@ -259,224 +258,6 @@ __global__ void __launch_bounds__(kUpThreads, 1) k_mv_up(const MvArgs a, const S
     if (OUT == 1) mv_lanczos_epilogue(a, dot, mx, s_u);
 }
 
-// ------------------------------------------------- pass U, staged gathers --
-// The Lanczos form of pass U with the up-neighbour segments moved by bulk
-// copies instead of warp loads, so that many more bytes are in flight per SM
-// than registers allow: a producer warp walks the CTA's items (the same
-// stripe-major items, CTA b taking b, b + G, ...), and for each copies the
-// stripe segments x[u', c0 .. c0 + 128) of the row's up neighbours, the row's
-// own x segment and its S_dn segment (1 KB each) into one of kUpStages
-// shared-memory stages; consumer warp w owns stage w and sums item after item
-// from it (same arithmetic as k_mv_up, so the same results bit for bit).
-// Each stage has a full barrier (the producer's arrival with the byte count,
-// completed by the copies) and an empty barrier (the consumer's arrival when
-// it has read the stage).  Waits are bounded; after a give-up every stage
-// whose copies are still counted is waited for once more before the CTA
-// leaves.
-constexpr int kUpStages = 8;
-constexpr int kUpTmaMaxLen = 22;                       // longest up row the stages hold
-constexpr int kUpSlots = kUpTmaMaxLen + 2;             // + own x, S_dn
-constexpr int kUpSlotBytes = kStripe * 8;              // 1 KB
-constexpr int kUpStageBytes = kUpSlots * kUpSlotBytes;  // 24 KB
-constexpr int kUpTmaThreads = 32 * (kUpStages + 1);
-constexpr int kUpTmaSmem = kUpStages * kUpStageBytes + 256;
-
-__global__ void __launch_bounds__(kUpTmaThreads, 1) k_mv_up_tma(const MvArgs a, const StripedArgs g) {
-    extern __shared__ __align__(128) unsigned char sm[];
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm + kUpStages * kUpStageBytes);
-    uint64_t* empty = full + kUpStages;
-    __shared__ int armed[kUpStages];        // stage copies issued and not yet consumed
-    __shared__ uint32_t stage_use[kUpStages];
-    // the item's row scalars, written by the producer before its arrival on
-    // the full barrier (release) and read by the consumer after its wait
-    __shared__ uint32_t h_len[kUpStages], h_npos[kUpStages];
-    __shared__ uint64_t h_st[kUpStages];
-    __shared__ int64_t h_du[kUpStages];
-    __shared__ int give_up;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int64_t dimUP = g.dimUP, dimDN = g.dimDN;
-    const int64_t nstripe = (dimDN + kStripe - 1) / kStripe;
-    const int64_t nitems = nstripe * dimUP;
-    const int64_t G = gridDim.x;
-    if (threadIdx.x == 0) {
-        for (int s = 0; s < kUpStages; ++s) {
-            tma::mbar_init(&full[s], 1);
-            tma::mbar_init(&empty[s], 1);
-            armed[s] = 0;
-            stage_use[s] = 0;
-        }
-        tma::fence_mbar_init();
-        give_up = 0;
-    }
-    __syncthreads();
-    const int b = a.bq_bits + bitlen_u64(*a.p_mx) - 62;
-    const int s_u = b > 0 ? b : 0;
-    i128 dot = 0;
-    uint64_t mx = 0;
-    if (warp == 0) {
-        // ---- producer
-        for (int64_t k = 0;; ++k) {
-            const int64_t it = blockIdx.x + k * G;
-            if (it >= nitems || *(volatile int*)&give_up) break;
-            const int s = (int)(k % kUpStages);
-            const uint32_t use = (uint32_t)(k / kUpStages);
-            if (use > 0 && !tma::mbar_wait(&empty[s], (use - 1) & 1)) {
-                if (lane == 0) {
-                    atomicExch(g.err, 1);
-                    give_up = 1;
-                }
-                break;
-            }
-            const int64_t st = it / dimUP, u = it - st * dimUP;
-            const int64_t c0 = st * kStripe;
-            const int64_t ncols = min((int64_t)kStripe, dimDN - c0);  // even: dim_dn is even
-            const uint32_t bytes = (uint32_t)(ncols * 8);
-            const uint32_t p0 = __ldg(a.upPtr + u), len = __ldg(a.upPtr + u + 1) - p0;
-            unsigned char* stage = sm + (size_t)s * kUpStageBytes;
-            if (lane == 0) {
-                stage_use[s] = use;
-                armed[s] = 1;
-                h_len[s] = len;
-                h_npos[s] = __ldg(a.upNpos + u);
-                h_st[s] = __ldg(a.stUP + u);
-                h_du[s] = __ldg(a.dUPq + u);
-                tma::expect_tx(&full[s], (len + 2) * bytes);
-            }
-            __syncwarp();
-            tma::fence_proxy_async_smem();
-            for (uint32_t i = lane; i < len + 2; i += 32) {
-                const int64_t* src;
-                int slot;
-                if (i < len) {
-                    src = g.xq + (int64_t)(__ldg(a.upEntC + p0 + i) & kColMask) * dimDN + c0;
-                    slot = (int)i;
-                } else if (i == len) {
-                    src = g.xq + u * dimDN + c0;
-                    slot = kUpTmaMaxLen;
-                } else {
-                    src = g.sdn + u * dimDN + c0;
-                    slot = kUpTmaMaxLen + 1;
-                }
-                tma::bulk_g2s(stage + (size_t)slot * kUpSlotBytes, src, bytes, &full[s]);
-            }
-        }
-    } else {
-        // ---- consumer warp w - 1 owns stage w - 1
-        const int s = warp - 1;
-        const bool merge = a.mergeUD != 0;
-        const bool unitU = a.unitUP != 0 && a.nclsUP == 1;
-        const bool unitD = a.unitDN != 0 && a.nclsDN == 1;
-        const unsigned char* stage = sm + (size_t)s * kUpStageBytes;
-        int64_t cur_st = -1;
-        int64_t cdq[4] = {0, 0, 0, 0};  // the stripe's folded down diagonal and bitstrings at the lane's columns
-        uint64_t cst[4] = {0, 0, 0, 0};
-        for (int64_t k = s;; k += kUpStages) {
-            const int64_t it = blockIdx.x + k * G;
-            if (it >= nitems) break;
-            const uint32_t use = (uint32_t)(k / kUpStages);
-            if (!tma::mbar_wait(&full[s], use & 1)) {
-                if (lane == 0) {
-                    atomicExch(g.err, 1);
-                    give_up = 1;
-                }
-                break;
-            }
-            const int64_t st = it / dimUP, u = it - st * dimUP;
-            const uint32_t c0 = (uint32_t)(st * kStripe);
-            const uint32_t c = c0 + 2u * (uint32_t)lane;
-            const uint32_t dn32 = (uint32_t)dimDN;
-            const uint32_t len = h_len[s];
-            const int npos = (int)h_npos[s];
-            if (c < dn32) {
-                const bool two = c + 64u < dn32;
-                if (st != cur_st) {
-                    cur_st = st;
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        const uint32_t cq = c + 64u * (q >> 1) + (q & 1);
-                        const bool ok = (q < 2) || two;
-                        cdq[q] = ok ? __ldg(g.dDNq + cq) : 0;
-                        cst[q] = ok ? __ldg(g.stDN + cq) : 0;
-                    }
-                }
-                const int lo = 16 * lane;  // byte offset of the lane's first pair in a slot
-                int64_t sp[4] = {0, 0, 0, 0};
-                int kk = 0;
-#pragma unroll 4
-                for (; kk < npos; ++kk) {
-                    const unsigned char* sl = stage + (size_t)kk * kUpSlotBytes;
-                    const longlong2 v0 = *reinterpret_cast<const longlong2*>(sl + lo);
-                    const longlong2 v1 = two ? *reinterpret_cast<const longlong2*>(sl + lo + 512) : make_longlong2(0, 0);
-                    sp[0] += v0.x;
-                    sp[1] += v0.y;
-                    sp[2] += v1.x;
-                    sp[3] += v1.y;
-                }
-#pragma unroll 4
-                for (; kk < (int)len; ++kk) {
-                    const unsigned char* sl = stage + (size_t)kk * kUpSlotBytes;
-                    const longlong2 v0 = *reinterpret_cast<const longlong2*>(sl + lo);
-                    const longlong2 v1 = two ? *reinterpret_cast<const longlong2*>(sl + lo + 512) : make_longlong2(0, 0);
-                    sp[0] -= v0.x;
-                    sp[1] -= v0.y;
-                    sp[2] -= v1.x;
-                    sp[3] -= v1.y;
-                }
-                const unsigned char* sx = stage + (size_t)kUpTmaMaxLen * kUpSlotBytes;
-                const unsigned char* sd = stage + (size_t)(kUpTmaMaxLen + 1) * kUpSlotBytes;
-                longlong2 xs[2], dsv[2];
-                xs[0] = *reinterpret_cast<const longlong2*>(sx + lo);
-                dsv[0] = *reinterpret_cast<const longlong2*>(sd + lo);
-                xs[1] = two ? *reinterpret_cast<const longlong2*>(sx + lo + 512) : make_longlong2(0, 0);
-                dsv[1] = two ? *reinterpret_cast<const longlong2*>(sd + lo + 512) : make_longlong2(0, 0);
-                const uint64_t stu = h_st[s];
-                const int64_t du = h_du[s];
-                const uint32_t rowu = (uint32_t)u * dn32 + c;
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    if (h == 1 && !two) break;
-                    int64_t oq[2];
-#pragma unroll
-                    for (int e = 0; e < 2; ++e) {
-                        const int q = 2 * h + e;
-                        const int64_t dn_sum = e ? dsv[h].y : dsv[h].x;
-                        const int64_t xv = e ? xs[h].y : xs[h].x;
-                        i128 ar = 0, ai = 0;
-                        if (merge) {
-                            apply_class<false>(ar, ai, sp[q] + dn_sum, 0, a.coefUP, 0, unitU, a.Fc);
-                        } else {
-                            if (len) apply_class<false>(ar, ai, sp[q], 0, a.coefUP, 0, unitU, a.Fc);
-                            if (a.nclsDN) apply_class<false>(ar, ai, dn_sum, 0, a.coefDN, 0, unitD, a.Fc);
-                        }
-                        const int64_t dq = du + cdq[q] + a.Uq * (int64_t)__popcll(stu & cst[q] & a.mask);
-                        ar += mul_wide(dq, xv);
-                        oq[e] = shr_round_i64(ar, s_u);
-                        dot += mul_wide(xv, oq[e]) >> 24;
-                        const uint64_t aq = (uint64_t)(oq[e] < 0 ? -oq[e] : oq[e]);
-                        mx = aq > mx ? aq : mx;
-                    }
-                    __stcs(reinterpret_cast<longlong2*>(a.uq + rowu + 64u * h), make_longlong2(oq[0], oq[1]));
-                }
-            }
-            __syncwarp();  // every lane has read the stage
-            if (lane == 0) {
-                armed[s] = 0;
-                tma::mbar_arrive(&empty[s]);
-            }
-        }
-    }
-    __syncthreads();
-    if (give_up) {
-        // copies still counted on a stage's full barrier land before the CTA
-        // leaves (bounded waits; after a second give-up the stages are undefined)
-        if (threadIdx.x == 0)
-            for (int s = 0; s < kUpStages; ++s)
-                if (armed[s]) tma::mbar_wait(&full[s], stage_use[s] & 1);
-        return;
-    }
-    mv_lanczos_epilogue(a, dot, mx, s_u);
-}
-
 // ---------------------------------------------------- down-index permutes --
 // out[u, c'] = in[u, perm[c']] (forward: table order -> permuted order) or
 // out[u, perm[c']] = in[u, c'] (back).  Grid-stride over elements, so each
@@ -518,20 +299,8 @@ cudaError_t launch_striped_down(const ed_op* op, const StripedArgs& g, cudaStrea
 }
 
 cudaError_t launch_striped_up(const ed_op* op, const MvArgs& a, const StripedArgs& g, int out, cudaStream_t s) {
-    if (out == 0) {
-        k_mv_up<0><<<op->st_grid, kUpThreads, 0, s>>>(a, g);
-        return cudaGetLastError();
-    }
-    // staged gathers unless a row is longer than the stages hold (or
-    // ED_PASS_U=loads asks for the register-load kernel)
-    const char* pu = std::getenv("ED_PASS_U");
-    if (op->st_up_maxlen <= kUpTmaMaxLen && !(pu && pu[0] == 'l')) {
-        cudaError_t e = cudaFuncSetAttribute(k_mv_up_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, kUpTmaSmem);
-        if (e != cudaSuccess) return e;
-        k_mv_up_tma<<<op->st_grid, kUpTmaThreads, kUpTmaSmem, s>>>(a, g);
-        return cudaGetLastError();
-    }
-    k_mv_up<1><<<op->st_grid, kUpThreads, 0, s>>>(a, g);
+    if (out == 0) k_mv_up<0><<<op->st_grid, kUpThreads, 0, s>>>(a, g);
+    else k_mv_up<1><<<op->st_grid, kUpThreads, 0, s>>>(a, g);
     return cudaGetLastError();
 }
 

@@ -234,7 +234,9 @@ class Hubbard:
         res = _capi.ed_tune_result()
         check(_capi.load().ed_op_autotune(self.handle, C.byref(cfg), C.byref(res), None), "ed_op_autotune")
         return {"persistent": bool(res.persistent), "row_cost": res.row_cost, "us_per_step": res.us_per_step,
-                "per_step_us": res.per_step_us, "persistent_us": list(res.persistent_us), "result": res}
+                "per_step_us": res.per_step_us, "persistent_us": list(res.persistent_us),
+                "ctas_per_sm": res.ctas_per_sm, "one_cta_us": res.one_cta_us, "chunk": res.chunk,
+                "chunk_us": list(res.chunk_us), "candidates": res.candidates, "result": res}
 
     def set_tuning(self, result) -> None:
         """ed_op_set_tuning: apply another operator's autotune result."""
@@ -323,7 +325,8 @@ def lanczos_multi(ops: Sequence[Hubbard], max_steps: int, starts=None, ritz: boo
     values each, 2 rows_b interleaved for complex operators).  evec_out: a
     float64 CUDA tensor of the same packed layout for the Ritz vectors (or
     None: numpy arrays are returned).  Returns (e0 [B], evecs as a list of
-    per-run views, alpha [B, max_steps], beta [B, max_steps + 1])."""
+    per-run views (a copy for a complex run that starts at an odd offset),
+    alpha [B, max_steps], beta [B, max_steps + 1])."""
     lib = _capi.load()
     B = len(ops)
     sizes = [op.rows() * (2 if op.is_complex else 1) for op in ops]
@@ -366,10 +369,11 @@ def lanczos_multi(ops: Sequence[Hubbard], max_steps: int, starts=None, ritz: boo
             v = evecs[int(offs[b]):int(offs[b + 1])]
             if op.is_complex:
                 if isinstance(v, np.ndarray):
-                    v = v.view(np.complex128)
+                    v = v.copy().view(np.complex128) if offs[b] % 2 else v.view(np.complex128)
                 else:
                     import torch
-                    v = v.view(torch.complex128)
+                    # a complex view needs an even offset; after a real run of odd length, a copy
+                    v = (v.clone() if offs[b] % 2 else v).view(torch.complex128)
             views.append(v)
     return np.array([r.e0 for r in res]), views, alpha, beta
 

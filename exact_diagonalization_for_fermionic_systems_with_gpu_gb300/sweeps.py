@@ -137,9 +137,18 @@ def flux_sweep(phis: Optional[Sequence[float]] = None, n_up: int = 6, n_dn: int 
     batch > 1 (fixed-step mode): up to `batch` (<= 16) twists share one
     persistent Lanczos launch for their ground states and one for their
     response solves (ed_lanczos_batch, ed_response_batch); the same start
-    vectors, so the same results bit for bit."""
+    vectors, so the same results bit for bit.  batch = 0: the size
+    tune_batch picks for this shape."""
     phis = flux_phis() if phis is None else phis
     t = timing if timing is not None else SweepTiming()
+    if batch == 0 and mode == "fixed":  # the autotuner's batch size for this shape
+        sample = []
+        for phi in list(phis)[:16]:
+            terms = L.kagome12(rand, flux=float(phi), peierls=True)
+            sample.append(Hubbard(H_TBq(12, n_up).extend(terms), H_TBq(12, n_dn).extend(terms), U))
+        batch = tune_batch(sample)
+        for op in sample:
+            op.close()
     if batch > 1 and mode == "fixed":
         t0 = time.perf_counter()
         out = _flux_batched(list(phis), n_up, n_dn, U, steps, response_steps, seed, rand, min(batch, 16), t)
@@ -307,6 +316,48 @@ def mbl_chain_terms(eps: Sequence[float], t: float = -1.0):
 MBL_SECTORS = ((6, 6), (7, 5), (8, 4))
 
 
+# Batch sizes chosen by tune_batch, per operator shape (n_sites, N_up, N_dn, complex).
+_BATCH_CHOICE: dict = {}
+
+
+def tune_batch(ops: Sequence[Hubbard], sizes=(1, 2, 4, 8, 16), steps: int = 20) -> int:
+    """The number of Lanczos runs per persistent launch (ed_lanczos_batch)
+    that gives the shortest time per run on these operators (one shape):
+    each candidate runs len(ops) short fixed-step solves in groups of that
+    size (a warm-up, then the better of two timed passes).  The choice is
+    kept per shape for the rest of the process."""
+    op0 = ops[0]
+    key = (op0.N, op0.dimUP, op0.dimDN, op0.is_complex, len(op0._up_terms))
+    if key in _BATCH_CHOICE:
+        return _BATCH_CHOICE[key]
+    best, pick = float("inf"), 1
+    for bsz in sizes:
+        if bsz > len(ops):
+            break
+        dt = float("inf")
+        for rep in range(3):
+            _sync()
+            t0 = time.perf_counter()
+            for g0 in range(0, len(ops), bsz):
+                grp = list(ops[g0:g0 + bsz])
+                if bsz == 1:
+                    Lanczos().eigen(grp[0], max_steps=steps, mode="fixed", ritz="none", seed=g0)
+                else:
+                    lanczos_multi(grp, steps, ritz=False, seed=g0)
+            _sync()
+            if rep:
+                dt = min(dt, time.perf_counter() - t0)
+        if dt < best:
+            best, pick = dt, bsz
+    _BATCH_CHOICE[key] = pick
+    return pick
+
+
+def batch_choices() -> dict:
+    """The batch sizes tune_batch has chosen so far, by shape."""
+    return {f"N={k[0]} {k[1]}x{k[2]}{' complex' if k[3] else ''}": v for k, v in _BATCH_CHOICE.items()}
+
+
 def _mbl_batched(reals, sectors, n_sites, W, U, steps, seed, a_sites, batch, t) -> List[MblPoint]:
     """mbl_sweep with the realisations of each sector in batches of `batch`
     Lanczos runs per persistent launch (ed_lanczos_batch); a sector the
@@ -318,8 +369,18 @@ def _mbl_batched(reals, sectors, n_sites, W, U, steps, seed, a_sites, batch, t) 
     out: List[MblPoint] = []
     reals = list(reals)
     for s, (qu, qd) in enumerate(sectors):
-        for g0 in range(0, len(reals), batch):
-            group = reals[g0:g0 + batch]
+        bsec = batch
+        if batch <= 0:  # the autotuner's batch size for this sector
+            sample = []
+            for r in reals[:8]:
+                eu, edn = mbl_disorder(r, n_sites, W, seed)
+                sample.append(Hubbard(H_TBq(n_sites, qu).extend(mbl_chain_terms(eu)),
+                                      H_TBq(n_sites, qd).extend(mbl_chain_terms(edn)), U))
+            bsec = tune_batch(sample, sizes=(1, 2, 4, 8))
+            for op in sample:
+                op.close()
+        for g0 in range(0, len(reals), bsec):
+            group = reals[g0:g0 + bsec]
             ti = time.perf_counter()
             ops = []
             for r in group:
@@ -373,12 +434,13 @@ def mbl_sweep(n_real: int = 64, sectors: Sequence[Tuple[int, int]] = MBL_SECTORS
               a_sites: Optional[Sequence[int]] = None, realisations: Optional[Sequence[int]] = None,
               timing: Optional[SweepTiming] = None, batch: int = 1) -> List[MblPoint]:
     """Ground-state sweep over disorder realisations and sectors; batch > 1
-    (fixed-step mode) runs up to 8 realisations of a sector per launch."""
+    (fixed-step mode) runs up to 8 realisations of a sector per launch, batch
+    = 0 the number tune_batch picks for each sector."""
     a_sites = list(range(n_sites // 2)) if a_sites is None else list(a_sites)
     reals = range(n_real) if realisations is None else realisations
     t = timing if timing is not None else SweepTiming()
     t0 = time.perf_counter()
-    if batch > 1 and mode == "fixed":
+    if (batch > 1 or batch == 0) and mode == "fixed":
         out = _mbl_batched(reals, sectors, n_sites, W, U, steps, seed, a_sites, min(batch, 8), t)
         t.total_s += time.perf_counter() - t0
         return out
@@ -453,11 +515,11 @@ FORM_ENV = {"tuned": {}, "plain": PLAIN_ENV, "plain_same_ee": PLAIN_SAME_EE_ENV}
 
 
 def run_form(what: str, n: int, form: str, steps: Optional[int] = None, mode: str = "fixed", seed: int = 0,
-             warmup: int = 1, batch: int = 8):
+             warmup: int = 1, batch: int = 0):
     """One sweep (what = "flux" | "mbl") in one form of FORM_ENV: the tuned
-    form batches twists (2 * batch per launch, at most 16) and disorder
-    realisations (batch per launch), the plain forms run one instance per
-    launch sequence.  steps: Lanczos steps per instance (None: FLUX_STEPS
+    form batches twists and disorder realisations (batch per launch; 0: the
+    autotuner's size for each shape, tune_batch), the plain forms run one
+    instance per launch sequence.  steps: Lanczos steps per instance (None: FLUX_STEPS
     for twists, 300 for disorder samples).  Returns (points, SweepTiming)."""
     if steps is None:
         steps = FLUX_STEPS if what == "flux" else 300
@@ -471,7 +533,7 @@ def run_form(what: str, n: int, form: str, steps: Optional[int] = None, mode: st
     try:
         tm = SweepTiming()
         if what == "flux":
-            fb = min(batch * 2, 16) if form == "tuned" else 1
+            fb = batch if form == "tuned" else 1
             if warmup:
                 flux_sweep(flux_phis(n)[:max(warmup, 2)], steps=steps, mode=mode, seed=seed, batch=fb)
             pts = flux_sweep(flux_phis(n), steps=steps, mode=mode, seed=seed, timing=tm, batch=fb)
@@ -502,8 +564,9 @@ def main(argv: Optional[Sequence[str]] = None) -> None:
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--warmup", type=int, default=1, help="instances run (untimed) before the sweep")
     ap.add_argument("--out", default=None, help="append the result rows to this .dat file")
-    ap.add_argument("--batch", type=int, default=8,
-                    help="disorder realisations per Lanczos launch in the tuned form (1: one launch per run)")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="runs per Lanczos launch in the tuned form (0: the autotuner's choice per shape, "
+                         "1: one launch per run)")
     ap.add_argument("--form", choices=["tuned", "plain", "plain_same_ee", "compare"], default="tuned",
                     help="plain: the per-instance form of PLAIN_ENV; plain_same_ee: the same with the tuned "
                          "entanglement path; compare: tuned and plain, with the largest differences of their "

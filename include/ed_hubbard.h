@@ -258,12 +258,16 @@ ed_status ed_lanczos_batch(ed_op* const* ops, int n_ops, const ed_lanczos_cfg* c
                            int start_mem, double* evecs, int evec_mem, double* alpha, double* beta,
                            ed_lanczos_result* res, void* stream);
 
-/* Autotuning of the Lanczos step for one operator: the per-step kernels and
- * the persistent kernel with three row-cost weights of its work queue
+/* Autotuning of the Lanczos step for one operator, over the knobs that set
+ * its speed per sector size: the per-step kernels against the persistent
+ * kernel; for the persistent kernel, the row-cost weight of its work queue
  * (the cost of a row taken as 1 + w len_up(u) / mean len_up, w = 0.4, 0.8,
- * 1.2) each run `steps` fixed Lanczos steps (one warm-up run, best of two
- * timed runs); with apply, the fastest becomes the operator's choice for
- * ed_lanczos_run and its users (the environment variable ED_LZ_FUSED still
+ * 1.2) and the rows each CTA takes (two 512-thread CTAs per SM, or one per SM
+ * taking twice the rows); for sectors on the two-pass matvec (rows beyond
+ * shared memory), the columns of a pass-D window (the chunk, largest that
+ * fits and half of it).  Each candidate runs `steps` fixed Lanczos steps (one
+ * warm-up run, best of two timed runs); with apply, the fastest becomes the
+ * operator's choice for ed_lanczos_run and its users (ED_LZ_FUSED still
  * overrides).  Every candidate computes the same coefficients bit for bit;
  * only the time differs.  Synchronous. */
 typedef struct {
@@ -278,6 +282,10 @@ typedef struct {
     double us_per_step;      /* the choice's time per step, host clock */
     double per_step_us;      /* per-step kernels */
     double persistent_us[3]; /* persistent kernel, w = 0.4, 0.8, 1.2 (0: no shared-memory plan) */
+    int32_t ctas_per_sm;     /* the choice's persistent CTAs per SM (2 or 1; 0 per-step) */
+    int32_t chunk;           /* the choice's pass-D window columns (two-pass sectors; else 0) */
+    double one_cta_us;       /* persistent kernel, one CTA per SM, the best weight (0: not timed) */
+    double chunk_us[2];      /* two-pass: per-step time at the largest chunk and at half of it */
 } ed_tune_result;
 
 ed_status ed_op_autotune(ed_op* op, const ed_tune_cfg* cfg, ed_tune_result* res, void* stream);

@@ -286,9 +286,9 @@ def test_lanczos_batch_rejects_other_tables(ed):
 @pytest.mark.parametrize("case", ["chain12_66", "kagome12_flux"])
 def test_autotune_keeps_results(ed, case):
     """ed_op_autotune times the per-step and persistent kernels (three queue
-    weights) and applies the fastest; the Lanczos coefficients afterwards are
-    the same bit for bit, and set_tuning carries the choice to a second
-    operator of the same shape."""
+    weights, two and one CTAs per SM) and applies the fastest; the Lanczos
+    coefficients afterwards are the same bit for bit, and set_tuning carries
+    the choice to a second operator of the same shape."""
     from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, sweeps
     if case == "chain12_66":
         eu, edn = sweeps.mbl_disorder(0, 12, 6.0)
@@ -302,7 +302,12 @@ def test_autotune_keeps_results(ed, case):
     lz0.eigen(op, max_steps=40, mode="fixed", ritz="none", seed=3)
     info = op.autotune(steps=20)
     assert info["per_step_us"] > 0 and all(v > 0 for v in info["persistent_us"])
-    assert info["us_per_step"] == min([info["per_step_us"]] + info["persistent_us"])
+    # the rows-per-CTA axis: one CTA per SM timed too where the plan has two,
+    # and the choice is the fastest of all
+    cands = [info["per_step_us"]] + info["persistent_us"] + ([info["one_cta_us"]] if info["one_cta_us"] > 0 else [])
+    assert info["candidates"] == len(cands)
+    assert info["us_per_step"] == min(cands)
+    assert info["ctas_per_sm"] in (1, 2) if info["persistent"] else info["ctas_per_sm"] == 0
     lz1 = ed.Lanczos()
     lz1.eigen(op, max_steps=40, mode="fixed", ritz="none", seed=3)
     assert lz1.a == lz0.a and lz1.b == lz0.b
@@ -357,3 +362,21 @@ def test_grid_barrier_timeout_is_reported_and_operator_recovers(ed, golden_energ
     g = golden_energies["kagome12_q66_U8"]["E0"]
     assert abs(e0 - g) < 1e-10 * abs(g)
     assert np.linalg.norm(op.matvec(v) - e0 * v) < 1e-6
+
+
+def test_autotune_two_pass_chunk_keeps_results(ed):
+    """The two-pass matvec's pass-D window (the tuner's chunk axis) on the
+    small Lieb18 case (4+9, 48,620 down columns): both chunks timed, and the
+    Lanczos coefficients under the chosen one equal the untuned run's."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    t = L.lieb18()
+    op = ed.Hubbard(ed.H_TBq(18, 4).extend(t), ed.H_TBq(18, 9).extend(t), 4.0)
+    assert op.matvec_kind == "two_pass"
+    lz0 = ed.Lanczos()
+    lz0.eigen(op, max_steps=6, mode="fixed", ritz="none", seed=2)
+    info = op.autotune(steps=3)
+    assert info["chunk"] > 0 and all(v > 0 for v in info["chunk_us"])
+    lz1 = ed.Lanczos()
+    lz1.eigen(op, max_steps=6, mode="fixed", ritz="none", seed=2)
+    assert lz1.a == lz0.a and lz1.b == lz0.b
+    op.close()
