@@ -43,12 +43,11 @@ constexpr int kDownThreads = 1024;
 constexpr int kUpThreads = 768;    // 24 warps (80 registers a thread): 24 rows of a stripe per item
 constexpr int kDownBatch = 8;      // pass-D schedule words loaded before their sums
 
-// One signed window word of the pass-D schedule: the sign mask (all ones
-// when bit 15 is set) by one byte permute that replicates the sign of byte 1,
-// then a conditional two's-complement negation.
+// One signed window word of the pass-D schedule: offset in bits 0..14, the
+// sign in bit 15 (m = 0 or -1, then a conditional two's-complement negation).
 __device__ __forceinline__ int64_t down_term(const int64_t* win, uint32_t e) {
     const int64_t v = win[e & 0x7FFFu];
-    const int64_t m = (int64_t)(int32_t)__byte_perm(e, 0u, 0x9999u);
+    const int64_t m = -(int64_t)((e >> 15) & 1u);
     return (v ^ m) - m;
 }
 

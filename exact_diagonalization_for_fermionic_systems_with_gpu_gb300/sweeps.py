@@ -143,7 +143,7 @@ def flux_sweep(phis: Optional[Sequence[float]] = None, n_up: int = 6, n_dn: int 
     t = timing if timing is not None else SweepTiming()
     if batch == 0 and mode == "fixed":  # the autotuner's batch size for this shape
         sample = []
-        for phi in list(phis)[:16]:
+        for phi in flux_phis(16):  # the sixteen-twist grid, whatever subset is swept
             terms = L.kagome12(rand, flux=float(phi), peierls=True)
             sample.append(Hubbard(H_TBq(12, n_up).extend(terms), H_TBq(12, n_dn).extend(terms), U))
         batch = tune_batch(sample)
@@ -320,7 +320,7 @@ MBL_SECTORS = ((6, 6), (7, 5), (8, 4))
 _BATCH_CHOICE: dict = {}
 
 
-def tune_batch(ops: Sequence[Hubbard], sizes=(1, 2, 4, 8, 16), steps: int = 20) -> int:
+def tune_batch(ops: Sequence[Hubbard], sizes=(1, 2, 4, 8, 16), steps: int = 60) -> int:
     """The number of Lanczos runs per persistent launch (ed_lanczos_batch)
     that gives the shortest time per run on these operators (one shape):
     each candidate runs len(ops) short fixed-step solves in groups of that
@@ -370,9 +370,9 @@ def _mbl_batched(reals, sectors, n_sites, W, U, steps, seed, a_sites, batch, t) 
     reals = list(reals)
     for s, (qu, qd) in enumerate(sectors):
         bsec = batch
-        if batch <= 0:  # the autotuner's batch size for this sector
+        if batch <= 0:  # the autotuner's batch size for this sector, from eight fixed realisations
             sample = []
-            for r in reals[:8]:
+            for r in range(8):
                 eu, edn = mbl_disorder(r, n_sites, W, seed)
                 sample.append(Hubbard(H_TBq(n_sites, qu).extend(mbl_chain_terms(eu)),
                                       H_TBq(n_sites, qd).extend(mbl_chain_terms(edn)), U))
