@@ -246,10 +246,29 @@ def c5_record(ed, lib, n_mv: int = 4) -> dict:
     prof = _profile_json("lieb18_matvec_traffic.json")
     kind = op.matvec_kind
     op.close()
+    # the gathers' own floor: every hop of every element loads one 8-byte
+    # neighbour value into the SM (up and down terms), at most 128 B per
+    # clock per SM through the L1/shared-memory path
+    import numpy as np
+    import torch
+    ax, _ = ed.H_TBq(18, 9).extend(t).ell()
+    nnz = int(np.count_nonzero(ax))
+    dim = ed.binom(18, 9)
+    gather_bytes = 8.0 * 2 * nnz * dim
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    try:
+        clk = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["sm_max_mhz"]) * 1e6
+    except (OSError, ValueError, KeyError):
+        clk = 2.07e9
+    floor_ms = gather_bytes / (sms * 128.0 * clk) * 1e3
     return {"workload": "lieb18_q99_U4_matvec", "dim": D, "matvecs": int(res.n_matvec), "matvec_kind": kind,
             "ms_per_matvec": ms, "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak,
             "bytes_per_matvec": 16.0 * D, "traffic_per_matvec": prof.get("dram_bytes_per_matvec"),
             "axpy_ms_per_step": axpy_ms, "min_bits": int(res.min_bits),
+            "gather_bytes_per_matvec": gather_bytes, "load_path_floor_ms": floor_ms,
+            "frac_of_load_path_floor": floor_ms / ms,
+            "load_path_note": "2 x nnz(spin table) x dim 8-byte neighbour loads at 128 B/clk/SM (L1/shared path), "
+                              "SM count and max SM clock of this GPU",
             "timing": "CUDA events on the launching stream around each matvec (both passes), vectors 18.9 GB "
                       "(no L2 flush needed)",
             "setup_s": round(time.perf_counter() - t0 - 0.0, 2), "build_s": round(build_s, 2)}

@@ -15,7 +15,9 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
 #include <functional>
+#include <thread>
 #include <vector>
 
 #include "ed_device.cuh"
@@ -415,6 +417,13 @@ struct Workspace {
     unsigned long long* cta_stamps = nullptr;  // per-CTA phase ends (profile 2)
     size_t cta_stamps_n = 0;
     std::vector<cudaEvent_t> events;  // profiling pool (pairs)
+    // host-mapped mirror of alpha and beta for the reference mode's stop test
+    unsigned char* mirror_base = nullptr;  // host address of the mapped block
+    HostMirror* mirror_h = nullptr;        // host view of its header
+    HostMirror* mirror_d = nullptr;        // device address of the header
+    double* mirror_alpha = nullptr;        // host views of the arrays
+    double* mirror_beta = nullptr;
+    int mirror_cap = 0;
 };
 
 #define LZ_CK(x)                                    \
@@ -435,7 +444,32 @@ void free_ws(Workspace* w) {
     cudaFree(w->ritz_part); cudaFree(w->ritz_ctr); cudaFree(w->inv_norm); cudaFree(w->gbar);
     cudaFree(w->stamps); cudaFree(w->fxbound); cudaFree(w->cta_stamps);
     for (cudaEvent_t e : w->events) cudaEventDestroy(e);
+    if (w->mirror_base) cudaFreeHost(w->mirror_base);
     *w = Workspace();
+}
+
+// The host-mapped mirror for runs of up to max_steps steps (grow-only).
+static cudaError_t ensure_mirror(Workspace* w, int max_steps) {
+    const int cap = max_steps + 2;
+    if (w->mirror_base && w->mirror_cap >= cap) return cudaSuccess;
+    if (w->mirror_base) cudaFreeHost(w->mirror_base);
+    w->mirror_base = nullptr;
+    w->mirror_cap = 0;
+    const size_t head = 64, bytes = head + 2 * sizeof(double) * (size_t)cap;
+    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&w->mirror_base), bytes, cudaHostAllocMapped);
+    if (e != cudaSuccess) return e;
+    std::memset(w->mirror_base, 0, bytes);
+    unsigned char* dbase = nullptr;
+    e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&dbase), w->mirror_base, 0);
+    if (e != cudaSuccess) return e;
+    w->mirror_h = reinterpret_cast<HostMirror*>(w->mirror_base);
+    w->mirror_d = reinterpret_cast<HostMirror*>(dbase);
+    w->mirror_alpha = reinterpret_cast<double*>(w->mirror_base + head);
+    w->mirror_beta = w->mirror_alpha + cap;
+    w->mirror_h->alpha = reinterpret_cast<double*>(dbase + head);  // device addresses, read by the kernel
+    w->mirror_h->beta = w->mirror_h->alpha + cap;
+    w->mirror_cap = cap;
+    return cudaSuccess;
 }
 
 constexpr int kDotChunks = 64;
@@ -606,11 +640,27 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     std::vector<double> tri(max_steps + 2);
     int status_dev = 0;
 
-    // Steps run in the persistent kernel (one launch per run of steps, ten at
-    // a time in the reference mode so the stop test keeps its cadence) for
-    // real single-class operators whose down table fits shared memory as a
-    // gather schedule, unless reorthogonalisation or per-step timing asks for
-    // the per-step kernels.  ED_LZ_FUSED=0 never uses it, ED_LZ_FUSED=1 also
+    // The reference stop test on steps 0 .. nn-1 (HubMatrix_GPU.cuh:585-597):
+    // the lowest Ritz pair of T_nn, converged when its residual estimate
+    // |beta_nn z_{nn-1}| is below tolconv * anorm.
+    auto ref_test = [&](int nn, const double* A, const double* Bv) -> bool {
+        double anorm = std::fabs(A[0] + Bv[1]);
+        for (int k = 1; k < nn; ++k) anorm = std::max(anorm, Bv[k] + std::fabs(A[k] + Bv[k + 1]));
+        tri[0] = tridiag_lowest_host(nn, A, Bv + 1, tri.data() + 1);
+        e0 = tri[0];
+        return std::fabs(Bv[nn] * tri[nn]) < tolconv * anorm && std::fabs(tri[1]) > tolconv * anorm;
+    };
+
+    // Steps run in the persistent kernel for real single-class operators
+    // whose down table fits shared memory as a gather schedule, unless
+    // reorthogonalisation or per-step timing asks for the per-step kernels.
+    // In the reference mode one launch runs every step while the host does
+    // the stop test every ten steps on the alpha and beta the kernel mirrors
+    // into mapped memory, and a host stop word ends the launch (a few steps
+    // after the test passes; T and the Ritz vector use the first n only).
+    // The tridiagonal eigensolve stays on the host: on this chip FP64 runs at
+    // 1/64 of the FP32 rate, and one device thread's Sturm bisection of a
+    // 300-step T takes milliseconds against ~0.1 ms on the host cores.  ED_LZ_FUSED=0 never uses it, ED_LZ_FUSED=1 also
     // for the other operators with a shared-memory plan (complex, several
     // classes), where the per-step kernels measured faster.
     const char* fz = std::getenv("ED_LZ_FUSED");
@@ -624,10 +674,17 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
     int j = 0;
     while (j < max_steps) {
         if (fused) {
-            const int j1 = (cfg->mode == ED_LANCZOS_REFERENCE || stop_beta >= 0.0)
+            const bool host_stop = cfg->mode == ED_LANCZOS_REFERENCE && stop_beta < 0.0 && j == 0;
+            const int j1 = (!host_stop && (cfg->mode == ED_LANCZOS_REFERENCE || stop_beta >= 0.0))
                                ? std::min(max_steps, (j / 10 + 1) * 10)
                                : max_steps;
             LZ_CK(cudaMemsetAsync(w->gbar, 0, kFusedSync, s));
+            if (host_stop) {
+                LZ_CK(ensure_mirror(w, max_steps));
+                w->mirror_h->done = 0;
+                w->mirror_h->stop = 0;
+                std::atomic_thread_fence(std::memory_order_seq_cst);
+            }
             LzRedSet* red = reinterpret_cast<LzRedSet*>(reinterpret_cast<char*>(w->gbar) + 32);
             if (stamps) {
                 const size_t need = (size_t)2 * max_steps * (op->lz_grid > 0 ? op->lz_grid : op->tma_grid);
@@ -640,8 +697,10 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
                 }
             }
             unsigned int* taken = reinterpret_cast<unsigned int*>(reinterpret_cast<char*>(w->gbar) + 160);
+            int* stop_word = reinterpret_cast<int*>(reinterpret_cast<char*>(w->gbar) + 176);
             LzFusedArgs fa{w->basis, w->stride, stored ? 1 : 0, j, j1, w->u, DW, lz, w->gbar, red, taken,
-                           stamps ? w->stamps : nullptr, stamps ? w->cta_stamps : nullptr, grid_wait_limits()};
+                           stamps ? w->stamps : nullptr, stamps ? w->cta_stamps : nullptr, grid_wait_limits(),
+                           host_stop ? w->mirror_d : nullptr, host_stop ? stop_word : nullptr};
             if (stamps) LZ_CK(cudaEventRecord(w->events[2 * n_fused], s));
             const cudaError_t e = launch_lz_fused(op, fa, s);
             if (e == cudaSuccess && stamps) LZ_CK(cudaEventRecord(w->events[2 * n_fused + 1], s));
@@ -653,6 +712,35 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             LZ_CK(e);
             ++launches;
             ++n_fused;
+            if (host_stop) {
+                // the stop test at every tenth step as the kernel's mirror
+                // reaches it; the first test that passes stops the launch
+                int checked = 0;
+                bool ended = false;
+                for (;;) {
+                    const int done = __atomic_load_n(&w->mirror_h->done, __ATOMIC_ACQUIRE);
+                    while (!converged && checked + 10 <= done && checked + 10 <= max_steps) {
+                        checked += 10;
+                        if (ref_test(checked, w->mirror_alpha, w->mirror_beta)) {
+                            converged = true;
+                            n = checked;
+                            __atomic_store_n(&w->mirror_h->stop, checked, __ATOMIC_RELEASE);
+                        }
+                    }
+                    if (converged || ended) break;
+                    const cudaError_t q = cudaStreamQuery(s);
+                    if (q == cudaSuccess) {
+                        ended = true;  // one more pass over the final count
+                        continue;
+                    }
+                    if (q != cudaErrorNotReady) LZ_CK(q);
+                    std::this_thread::yield();
+                }
+                LZ_CK(cudaStreamSynchronize(s));
+                steps_run = __atomic_load_n(&w->mirror_h->done, __ATOMIC_ACQUIRE);  // steps the launch ran
+                j = max_steps;
+                break;
+            }
             j = j1;
         } else {
             if (prof) LZ_CK(cudaEventRecord(w->events[4 * j], s));
@@ -712,11 +800,7 @@ ed_status lanczos_run(ed_op* op, void** ws_slot, const ed_lanczos_cfg* cfg, cons
             LZ_CK(cudaMemcpyAsync(&status_dev, &lz->status, sizeof(int), cudaMemcpyDeviceToHost, s));
             LZ_CK(cudaStreamSynchronize(s));
             if (status_dev != 0) { n = nn; break; }
-            double anorm = std::fabs(ha[0] + hb[1]);
-            for (int k = 1; k < nn; ++k) anorm = std::max(anorm, hb[k] + std::fabs(ha[k] + hb[k + 1]));
-            tri[0] = tridiag_lowest_host(nn, ha.data(), hb.data() + 1, tri.data() + 1);
-            e0 = tri[0];
-            if (std::fabs(hb[nn] * tri[nn]) < tolconv * anorm && std::fabs(tri[1]) > tolconv * anorm) {
+            if (ref_test(nn, ha.data(), hb.data())) {
                 converged = true;
                 n = nn;
                 break;

@@ -60,6 +60,15 @@ struct GridWait {
 // Defaults (2^26 polls, 4 s), or ED_GRID_WAIT="<ns>[,<extra arrivals>]".
 GridWait grid_wait_limits();
 
+// Host-mapped mirror of the Lanczos scalars for the host-side stop test.
+struct HostMirror {
+    int done;     // alpha[0 .. done-1] and beta[0 .. done] are written
+    int stop;     // host: nonzero n ends the run once n steps are done
+    int pad_[2];
+    double* alpha;  // device addresses of mapped arrays (max_steps + 2 each)
+    double* beta;
+};
+
 struct LzFusedArgs {
     int64_t* basis;
     int64_t stride;      // slot stride in elements
@@ -76,6 +85,13 @@ struct LzFusedArgs {
     unsigned long long* cta_stamps;  // optional: every CTA's rows-done and axpy-done
                                      // times, [step][2][gridDim.x]
     GridWait wait;
+    // Stop test on the host while the launch runs (reference mode): block 0
+    // mirrors alpha and beta into host-mapped memory and counts the slots
+    // done; a nonzero host stop word s ends the launch at the first step end
+    // with j + 1 >= s (the decision passed to every CTA through stop_word,
+    // read after the step's last grid barrier).  All null when unused.
+    HostMirror* mirror;  // device address of the mapped mirror
+    int* stop_word;      // device word, zero at launch
 };
 
 // One instance of a batched run (k_lz_batch): instances share the hopping

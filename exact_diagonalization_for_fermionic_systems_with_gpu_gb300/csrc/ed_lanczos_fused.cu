@@ -65,6 +65,22 @@ __device__ __forceinline__ void red_release_gpu_add(unsigned int* p, unsigned in
 
 __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 
+// A word of host-mapped memory written by the host (system scope).
+__device__ __forceinline__ int ld_relaxed_sys(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.sys.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Block 0: slot k of the host mirror complete (alpha[k-1], beta[k]), the
+// data before the count (system-scope fence).
+__device__ __forceinline__ void mirror_slot(HostMirror* hm, const LzState* lz, int k) {
+    if (k > 0) hm->alpha[k - 1] = lz->alpha[k - 1];
+    hm->beta[k] = lz->beta[k];
+    __threadfence_system();
+    *(volatile int*)&hm->done = k;
+}
+
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -181,6 +197,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
         else sP = {0, 0, 0.0, 0.0};
         s_status = lz->status;
         s_min_bits = lz->min_bits;
+        if (f.mirror && blockIdx.x == 0 && j == 0) mirror_slot(f.mirror, lz, 0);
     }
     if (SCHED) tma_zero_slots(a, S);
     __syncthreads();
@@ -230,6 +247,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
             uint64_t mw;
             red_pull(&f.red[(rM - 1) % 4], ss, mw);
             slot_done(lz, j, s_coef.e_w, ss, mw, sX, sP, s_status, s_min_bits, blockIdx.x == 0);
+            if (f.mirror && blockIdx.x == 0) mirror_slot(f.mirror, lz, j);
         }
         {
             i128 dot = 0;
@@ -244,6 +262,10 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
             if (stamp) st[2] = global_ns();
         }
         if (!grid_sync(f.gbar, target, &give_up, a.err, f.wait)) return;
+        // block 0 reads the host's stop word now and passes it on before the
+        // step's last barrier (the load's latency hides behind the axpy)
+        int host_stop = 0;
+        if (f.mirror && blockIdx.x == 0 && tid == 0) host_stop = ld_relaxed_sys(&f.mirror->stop);
         if (tid == 0) {
             if (stamp) st[3] = global_ns();
             i128 s;
@@ -311,23 +333,29 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
             }
             block_sum_max(ss, mw, s128, s64);
             if (tid == 0) red_push(&f.red[rA % 4], ss, mw);
+            if (f.mirror && blockIdx.x == 0 && tid == 0) *(volatile int*)f.stop_word = host_stop;
             if (stamp) st[6] = global_ns();
         }
         // a data barrier: the next matvec gathers w_{j+1} from every CTA; the
         // norm and max of w_{j+1} are read at the next step's reduction
         if (!grid_sync(f.gbar, target, &give_up, a.err, f.wait)) return;
+        // the same stop decision in every CTA: the word block 0 wrote before the barrier
+        const int stop_at = f.mirror ? *(volatile int*)f.stop_word : 0;
+        const bool last = j + 1 == f.j1 || (stop_at > 0 && j + 1 >= stop_at);
         if (tid == 0) {
             if (blockIdx.x == 0 && rA >= 2) f.red[(rA - 2) % 4] = LzRedSet{0, 0, 0, 0};
             if (stamp) st[7] = st[8] = global_ns();
-            if (j + 1 == f.j1 && blockIdx.x == 0) {
+            if (last && blockIdx.x == 0) {
                 // the last slot of this launch: block 0 stores its scalars
                 i128 ss;
                 uint64_t mw;
                 red_pull(&f.red[rA % 4], ss, mw);
                 slot_done(lz, j + 1, s_coef.e_w, ss, mw, sX, sP, s_status, s_min_bits, true);
+                if (f.mirror) mirror_slot(f.mirror, lz, j + 1);
             }
         }
         __syncthreads();
+        if (last) break;
     }
 }
 

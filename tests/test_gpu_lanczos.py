@@ -54,6 +54,31 @@ def test_reference_mode_matches_oracle(ed, orc, golden_energies):
     assert abs(abs(v @ v_o) - 1.0) < 1e-8
 
 
+def test_reference_mode_kagome12_one_launch(ed, golden_energies, monkeypatch):
+    """The reference stop test on Kagome12 6+6, U=8: the persistent kernel
+    runs every step in one launch while the host tests T every ten steps on
+    the mirrored alpha and beta, and the launch stops a few steps after the
+    test passes.  Against the per-step kernels, which stop at the test's
+    step with a host round trip every ten steps: the same step count, alpha,
+    beta and E0 bit for bit; the golden E0 to 1e-10; six kernel launches in
+    all (start vector three, one persistent, Ritz sum two)."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    g = golden_energies["kagome12_q66_U8"]["E0"]
+    op = op_for(ed, 12, 6, 6, L.kagome12(), L.kagome12(), 8.0)
+    lz = ed.Lanczos()
+    e0, v = lz.eigen(op, max_steps=1000, mode="reference", seed=4)
+    assert lz.result.converged == 1 and lz.result.steps % 10 == 0
+    assert lz.result.launches == 6, lz.result.launches
+    assert lz.result.n_matvec >= lz.result.steps
+    assert abs(e0 - g) < 1e-10 * abs(g)
+    monkeypatch.setenv("ED_LZ_FUSED", "0")
+    lz2 = ed.Lanczos()
+    e2, v2 = lz2.eigen(op, max_steps=1000, mode="reference", seed=4)
+    assert lz2.result.steps == lz.result.steps and lz2.result.n_matvec == lz2.result.steps
+    assert lz2.a == lz.a and lz2.b == lz.b and e2 == e0
+    assert np.array_equal(v2, v)
+
+
 def test_kagome12_300_steps(ed, golden_energies):
     """Kagome 12-site, 6+6, U=8, 300 fixed steps: E0 to 1e-10 and the Ritz vector."""
     from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
@@ -275,12 +300,17 @@ def test_lanczos_batch_matches_single_runs(ed):
             assert np.array_equal(ev[b], v)
 
 
-def test_lanczos_batch_rejects_other_tables(ed):
+def test_lanczos_batch_of_different_tables_runs_each_as_alone(ed):
+    """Operators with different hopping tables (open and periodic chain)
+    share a launch in the general batch kernel; each run equals its own."""
     from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
     a = ed.Hubbard(ed.H_TBq(12, 6).extend(L.chain(12, periodic=False)), ed.H_TBq(12, 6).extend(L.chain(12, periodic=False)), 1.0)
     b = ed.Hubbard(ed.H_TBq(12, 6).extend(L.chain(12)), ed.H_TBq(12, 6).extend(L.chain(12)), 1.0)
-    with pytest.raises(ed.EdError):
-        ed.lanczos_batch([a, b], 10)
+    e0, ev, al, be = ed.lanczos_batch([a, b], 40, seed=5)
+    for k, op in enumerate((a, b)):
+        lz = ed.Lanczos()
+        e, v = lz.eigen(op, max_steps=40, mode="fixed", seed=5 + k)
+        assert e0[k] == e and np.array_equal(al[k], np.array(lz.a)) and np.array_equal(ev[k], v)
 
 
 @pytest.mark.parametrize("case", ["chain12_66", "kagome12_flux"])
