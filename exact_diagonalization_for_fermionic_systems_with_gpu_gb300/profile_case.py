@@ -10,6 +10,10 @@
 --what perform : --steps operator applies through the FP64 C-ABI path
 --what adjoint : a --steps Lanczos solve with the Ritz vector regenerated in a
                  second pass, then dE0/dU and dE0/dt (the Lieb18 9+9 workload)
+--what tune    : ed_op_autotune's timings and choice for the case's operator
+                 (--steps per candidate) and, for sectors with a persistent plan,
+                 the batch size sweeps.tune_batch picks (eight samples of the
+                 case's shape); one JSON line
 Cases: kagome12 (6+6, dim 853,776, L2-resident vectors), kagome12_flux
 (complex, Peierls phases), chain12_66 / chain12_75 / chain12_84 (open L=12
 chain, W=6 disorder, the three sectors of the MBL sweep), chain14 (7+7 open
@@ -98,7 +102,7 @@ def adjoint_run(name: str, op: Hubbard, steps: int) -> None:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default="kagome12")
-    ap.add_argument("--what", default="lanczos", choices=["lanczos", "fused", "solve", "perform", "adjoint"])
+    ap.add_argument("--what", default="lanczos", choices=["lanczos", "fused", "solve", "perform", "adjoint", "tune"])
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--ritz", default="none", choices=["none", "stored"],
                     help="stored: keep the Krylov basis and form the Ritz vector, as the bench does")
@@ -109,6 +113,28 @@ def main():
     t0 = time.perf_counter()
     if args.what == "adjoint":
         adjoint_run(args.case, op, args.steps)
+    elif args.what == "tune":
+        import json
+        from . import sweeps
+        info = op.autotune(steps=args.steps)
+        info.pop("result")
+        out = {"case": args.case, "dim": op.rows(), "matvec_kind": op.matvec_kind, "autotune": info}
+        if op.matvec_kind != "two_pass":
+            sample = [build_case(args.case) for _ in range(8)]
+            if args.case.startswith("chain12_"):
+                # eight disorder realisations of the sector (different on-site terms, same hops)
+                qu, qd = int(args.case[-2]), int(args.case[-1])
+                for o in sample:
+                    o.close()
+                sample = []
+                for r in range(8):
+                    eu, edn = sweeps.mbl_disorder(r, 12, 6.0)
+                    sample.append(Hubbard(H_TBq(12, qu).extend(sweeps.mbl_chain_terms(eu)),
+                                          H_TBq(12, qd).extend(sweeps.mbl_chain_terms(edn)), 1.0))
+            out["batch_size"] = sweeps.tune_batch(sample)
+            for o in sample:
+                o.close()
+        print(json.dumps(out))
     elif args.what in ("lanczos", "fused", "solve"):
         ritz = _capi.ED_RITZ_STORED if args.ritz == "stored" else _capi.ED_RITZ_NONE
         cfg = _capi.ed_lanczos_cfg(max_steps=args.steps, mode=_capi.ED_LANCZOS_FIXED, reorth=0,
