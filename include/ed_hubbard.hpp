@@ -177,6 +177,57 @@ inline void entanglement_entropy_batch(Hubbard& h, int n, const std::vector<doub
           "ed_entanglement_entropy_batch");
 }
 
+// Fixed-step Lanczos runs of up to 16 operators (any sectors, real or complex)
+// in one persistent launch: the drivers' loops over disorder samples, sectors
+// and twists.  starts (host, the runs one after another: rows values each, 2
+// rows for complex operators; empty for seeded starts seed + b); evecs (host)
+// receives the normalised Ritz vectors in the same layout; returns E0 per run.
+inline std::vector<double> lanczos_batch(const std::vector<Hubbard*>& ops, int steps,
+                                         const std::vector<double>& starts, std::vector<double>& evecs,
+                                         uint64_t seed = 0) {
+    const int n = (int)ops.size();
+    std::vector<ed_op*> h(n);
+    size_t total = 0;
+    for (int b = 0; b < n; ++b) {
+        h[b] = ops[b]->handle();
+        total += (size_t)ops[b]->rows() * (ed_op_is_complex(h[b]) ? 2 : 1);
+    }
+    ed_lanczos_cfg cfg{};
+    cfg.max_steps = steps;
+    cfg.mode = ED_LANCZOS_FIXED;
+    cfg.ritz = ED_RITZ_STORED;
+    cfg.start = starts.empty() ? ED_START_RANDOM : ED_START_USER;
+    cfg.seed = seed;
+    evecs.resize(total);
+    std::vector<ed_lanczos_result> res(n);
+    check(ed_lanczos_batch(h.data(), n, &cfg, starts.empty() ? nullptr : starts.data(), ED_MEM_HOST, evecs.data(),
+                           ED_MEM_HOST, nullptr, nullptr, res.data(), nullptr),
+          "ed_lanczos_batch");
+    std::vector<double> e0(n);
+    for (int b = 0; b < n; ++b) e0[b] = res[b].e0;
+    return e0;
+}
+
+// dE0/dtheta and d2E0/dtheta2 for n operators in one batched linear-response
+// launch (ed_response_batch); psis_device holds the n normalised ground states
+// one after another in device memory.
+inline void response_batch(const std::vector<Hubbard*>& H, const std::vector<Hubbard*>& dH,
+                           const std::vector<Hubbard*>& d2H, const double* psis_device, const std::vector<double>& e0,
+                           int steps, std::vector<double>& first, std::vector<double>& second) {
+    const int n = (int)H.size();
+    std::vector<ed_op*> h(n), d(n), d2(n);
+    for (int b = 0; b < n; ++b) {
+        h[b] = H[b]->handle();
+        d[b] = dH[b]->handle();
+        d2[b] = d2H[b]->handle();
+    }
+    first.assign(n, 0.0);
+    second.assign(n, 0.0);
+    check(ed_response_batch(h.data(), d.data(), d2.data(), n, psis_device, e0.data(), steps, first.data(),
+                            second.data(), nullptr),
+          "ed_response_batch");
+}
+
 // Spectra::SymEigsSolver<OpType>(op, nev, ncv) with SortRule::SmallestAlge;
 // eigenvectors() is rows x nev column-major (Eigen's MatrixXd layout).
 class SymEigsSolver {

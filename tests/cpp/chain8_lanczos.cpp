@@ -5,6 +5,7 @@
 // (Time_evol_test.cu).
 // Argument "--basis-only" exercises the host-side part without a GPU.
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -38,6 +39,24 @@ int main(int argc, char** argv) {
         ed::entanglement_entropy_batch(h, 2, two, 0x0Fu, bvn, bref);
         std::printf("EE %.15f %.15f %d %d\n", ee.first, ee.second, (int)(bvn[0] == ee.first && bvn[1] == ee.first),
                     h.matvec_kind());
+        // the drivers' loop over samples and sectors as one batched launch: the
+        // 4+4 operator and a 5+3 one, each run equal to its own
+        ed::H_TBq up5(N, 5), dn3(N, 3);
+        for (int i = 0; i < N; ++i) {
+            up5.Make_H(i, (i + 1) % N, -1.0);
+            dn3.Make_H(i, (i + 1) % N, -1.0);
+        }
+        ed::Hubbard h53(up5, dn3, 4.0);
+        std::vector<double> bev;
+        const std::vector<double> be0 = ed::lanczos_batch({&h, &h53}, 60, {}, bev, 11);
+        ed::Lanczos l0, l1;
+        std::vector<double> v0, v1;
+        l0.eigen(h, {}, v0, 60, ED_LANCZOS_FIXED, false, 11);
+        l1.eigen(h53, {}, v1, 60, ED_LANCZOS_FIXED, false, 12);
+        const bool same = be0[0] == l0.result.e0 && be0[1] == l1.result.e0 &&
+                          std::equal(v0.begin(), v0.end(), bev.begin()) &&
+                          std::equal(v1.begin(), v1.end(), bev.begin() + v0.size());
+        std::printf("BATCH %.15f %.15f %d\n", be0[0], be0[1], (int)same);
         // TotalSpinExcited_*: the lowest pairs through the Spectra-shaped solver
         ed::SymEigsSolver eigs(h, 3, 4 * (3 + 1));
         eigs.init();

@@ -41,6 +41,8 @@ def test_cpp_header_lanczos_on_gpu(tmp_path, edlib, golden_energies):
     assert ee[2] == "1" and int(ee[3]) in (0, 1, 2)
     kry = out.split("KRYLOV ")[1].split()
     assert abs(float(kry[3]) - 1.0) < 1e-12
+    bat = out.split("BATCH ")[1].split()
+    assert bat[2] == "1" and abs(float(bat[0]) - g) < 1e-9 * abs(g)
 
 
 def test_gather_schedule_host_check(tmp_path):
