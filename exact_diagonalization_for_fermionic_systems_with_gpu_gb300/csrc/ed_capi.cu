@@ -232,7 +232,7 @@ static ed_status plan_striped(ed_op* op, bool forced, int64_t chunk_cap = 16384)
     int64_t zbase = 0;
     if (!ed::window_schedule16(g, op->dimDN, chunk, bw, &s16, &zbase)) return ED_OK;
     const int64_t sched_steps = std::max(g.steps, 1);
-    const std::vector<uint16_t> s16bm = ed::block_major16(s16, g.count_pad, sched_steps);
+    const std::vector<uint16_t> s16bm = ed::lane_packed16(s16, g.count_pad, sched_steps, zbase);
     const int Fc = op->mv.Fc;
     std::vector<int64_t> dq((size_t)op->dimDN);
     std::vector<uint64_t> st((size_t)op->dimDN);
@@ -260,7 +260,7 @@ static ed_status plan_striped(ed_op* op, bool forced, int64_t chunk_cap = 16384)
     op->st_win = (int)(zbase + 16);
     op->st_zbase = (int)zbase;
     op->st_cpad = g.count_pad;
-    op->st_smax = (int)sched_steps;
+    op->st_s8 = (int)((sched_steps + 7) / 8);
     return ED_OK;
 }
 

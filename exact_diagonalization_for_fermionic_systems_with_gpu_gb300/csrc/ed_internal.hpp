@@ -88,10 +88,10 @@ struct StripedArgs {
     const int64_t* xq;        // FX input, permuted order
     int64_t* sdn;             // int64 down sums (pass D out, pass U in / FP64 out)
     int64_t dimUP, dimDN;
-    const uint16_t* sched16;  // [cpad / 32][smax][32] offset in the chunk's window | sign << 15; idle: a zero slot
+    const uint16_t* sched16;  // [cpad / 32][s8][32][8] offset in the chunk's window | sign << 15; idle: a zero slot
     const uint8_t* steps32;   // steps the warp of 32-column block k runs
     int64_t cpad;
-    int smax;                 // schedule steps (rows of a 32-column block)
+    int s8;                   // groups of eight schedule steps
     int64_t bw;               // bandwidth of the permuted down index
     int chunk;                // columns per pass-D item
     int zbase;                // first of the 16 zero slots after the window
@@ -141,7 +141,7 @@ struct ed_op {
     // two-pass matvec (striped): down index permuted by perm (new -> old)
     bool striped = false;
     int st_grid = 0, st_win = 0, st_chunk = 0, st_zbase = 0;
-    int st_smax = 0;            // steps of pass D's schedule (block-major layout)
+    int st_s8 = 0;              // groups of eight steps of pass D's schedule (lane-packed layout)
     // tuning (ed_op_autotune): Lanczos kernels 0 by the default rule, 1 per
     // step, 2 persistent; weight of the persistent kernel's row queue
     int lz_mode = 0;

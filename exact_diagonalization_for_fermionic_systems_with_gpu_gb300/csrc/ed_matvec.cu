@@ -290,7 +290,7 @@ cudaError_t striped_args(ed_op* op, const int64_t* xq, StripedArgs* g) {
     g->sched16 = op->d_sched16;
     g->steps32 = op->d_steps32;
     g->cpad = op->st_cpad;
-    g->smax = op->st_smax;
+    g->s8 = op->st_s8;
     g->bw = op->st_bw;
     g->chunk = op->st_chunk;
     g->zbase = op->st_zbase;

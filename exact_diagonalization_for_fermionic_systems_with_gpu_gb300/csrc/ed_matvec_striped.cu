@@ -14,8 +14,9 @@
 //   chunk's window | sign << 15; at most two targets per bank pair in a
 //   step, idle lanes on a zero slot; the columns are ordered by hop count
 //   within blocks of 256 so that a warp's lanes have similar step counts; the
-//   schedule is the same for every row and is read from L2, eight steps'
-//   words in flight per thread).  Output: the exact int64 down sums S_dn.
+//   schedule is the same for every row and is read from L2, eight steps of
+//   a column packed in one 16-byte load).  Output: the exact int64 down sums
+//   S_dn.
 // Pass U (k_mv_up): column stripes of kStripe columns, stripe-major over all
 //   rows so that the stripe of x (dim_up x kStripe x 8 B) stays in L2 while
 //   every row's up neighbours gather from it; a warp computes one row of a
@@ -41,7 +42,6 @@ using namespace dev;
 constexpr int kStripe = 128;       // columns of a pass-U stripe (32 lanes x 4)
 constexpr int kDownThreads = 1024;
 constexpr int kUpThreads = 768;    // 24 warps (80 registers a thread): 24 rows of a stripe per item
-constexpr int kDownBatch = 8;      // pass-D schedule words loaded before their sums
 
 // One signed window word of the pass-D schedule: offset in bits 0..14, the
 // sign in bit 15 (m = 0 or -1, then a conditional two's-complement negation).
@@ -51,20 +51,26 @@ __device__ __forceinline__ int64_t down_term(const int64_t* win, uint32_t e) {
     return (v ^ m) - m;
 }
 
-// Steps s0 .. n-1 of one column's schedule (block-major: a lane's steps 32
-// words apart): kDownBatch at a time, then singly.
-__device__ __forceinline__ int64_t down_tail(const int64_t* win, const uint16_t* sc, int s0, int n) {
+// The steps of one lane-packed 16-byte schedule word (eight 16-bit words);
+// GUARD: only the first rem of them (the last, partial group of a column).
+template <bool GUARD>
+__device__ __forceinline__ int64_t down_group(const int64_t* win, const uint4 w, int rem) {
+    const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
     int64_t acc = 0;
-    int s = s0;
-    for (; s + kDownBatch <= n; s += kDownBatch) {
-        const uint16_t* p = sc + 32 * s;
-        uint32_t e[kDownBatch];
 #pragma unroll
-        for (int t = 0; t < kDownBatch; ++t) e[t] = __ldg(p + 32 * t);
-#pragma unroll
-        for (int t = 0; t < kDownBatch; ++t) acc += down_term(win, e[t]);
+    for (int t = 0; t < 8; ++t) {
+        if (GUARD && t >= rem) break;
+        acc += down_term(win, (t & 1) ? ws[t >> 1] >> 16 : ws[t >> 1] & 0xFFFFu);
     }
-    for (; s < n; ++s) acc += down_term(win, __ldg(sc + 32 * s));
+    return acc;
+}
+
+// Groups q0 .. of one column's n steps: whole groups, then the partial one.
+__device__ __forceinline__ int64_t down_tail(const int64_t* win, const uint4* p, int q0, int n) {
+    int64_t acc = 0;
+    int q = q0;
+    for (; q < (n >> 3); ++q) acc += down_group<false>(win, __ldg(p + 32 * q), 0);
+    if (n & 7) acc += down_group<true>(win, __ldg(p + 32 * q), n & 7);
     return acc;
 }
 
@@ -110,34 +116,26 @@ __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g
             return;
         }
         // two columns per iteration (c and c + 1024): their schedule words are
-        // loaded together, kDownBatch steps of each in flight
+        // loaded together
         for (int64_t c = c0 + tid; c < c1; c += 2 * kDownThreads) {
             const int64_t cb = c + kDownThreads;
             const bool hb = cb < c1;
             const int na = __ldg(g.steps32 + (c >> 5)), nb = hb ? __ldg(g.steps32 + (cb >> 5)) : 0;
             const int64_t cbb = hb ? cb : c;
-            const uint16_t* sa = g.sched16 + (size_t)(c >> 5) * (size_t)g.smax * 32 + (c & 31);
-            const uint16_t* sb = g.sched16 + (size_t)(cbb >> 5) * (size_t)g.smax * 32 + (cbb & 31);
+            const uint4* sa = reinterpret_cast<const uint4*>(g.sched16) + (size_t)(c >> 5) * (size_t)g.s8 * 32 + (c & 31);
+            const uint4* sb = reinterpret_cast<const uint4*>(g.sched16) + (size_t)(cbb >> 5) * (size_t)g.s8 * 32 + (cbb & 31);
             int64_t acca = 0, accb = 0;
-            const int nm = na < nb ? na : nb;
-            int s = 0;
-            for (; s + kDownBatch <= nm; s += kDownBatch) {
-                const uint16_t* pa = sa + 32 * s;
-                const uint16_t* pb = sb + 32 * s;
-                uint32_t ea[kDownBatch], eb[kDownBatch];
-#pragma unroll
-                for (int t = 0; t < kDownBatch; ++t) {
-                    ea[t] = __ldg(pa + 32 * t);
-                    eb[t] = __ldg(pb + 32 * t);
-                }
-#pragma unroll
-                for (int t = 0; t < kDownBatch; ++t) {
-                    acca += down_term(win, ea[t]);
-                    accb += down_term(win, eb[t]);
-                }
+            // whole groups of eight steps of both columns, one 16-byte
+            // schedule load per column and group
+            const int gm = (na < nb ? na : nb) >> 3;
+            int q = 0;
+            for (; q < gm; ++q) {
+                const uint4 wa = __ldg(sa + 32 * q), wb = __ldg(sb + 32 * q);
+                acca += down_group<false>(win, wa, 0);
+                accb += down_group<false>(win, wb, 0);
             }
-            acca += down_tail(win, sa, s, na);
-            if (hb) accb += down_tail(win, sb, s, nb);
+            acca += down_tail(win, sa, q, na);
+            if (hb) accb += down_tail(win, sb, q, nb);
             g.sdn[u * dimDN + c] = acca;
             if (hb) g.sdn[u * dimDN + cb] = accb;
         }

@@ -414,8 +414,10 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
 #pragma unroll 1
                 for (int cc = 0; cc < 2; ++cc) {
                     const uint32_t d = cc ? d1c : d0;
-                    i128& ar = cc ? ar1 : ar0;
-                    i128& ai = cc ? ai1 : ai0;
+                    // this column's accumulators, stored into ar0/ai0 or
+                    // ar1/ai1 at the end (not a reference chosen at run time,
+                    // which would put all four in local memory)
+                    i128 ar = 0, ai = 0;
                     const uint32_t se = __ldg(a.dnSegE + d), sp = __ldg(a.dnSegP + d);
                     const uint32_t q0 = S.dptr[d];
                     uint32_t ub = 0, b = 0;
@@ -458,6 +460,13 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                         } else if (a.mergeMC) {
                             apply_class<CPLX>(ar, ai, r, i, a.coefUP, c, unitU, a.Fc);
                         }
+                    }
+                    if (cc) {
+                        ar1 = ar;
+                        ai1 = ai;
+                    } else {
+                        ar0 = ar;
+                        ai0 = ai;
                     }
                 }
             } else {

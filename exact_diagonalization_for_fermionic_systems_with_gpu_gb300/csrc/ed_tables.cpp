@@ -620,12 +620,12 @@ bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& pe
     return true;
 }
 
-std::vector<uint16_t> block_major16(const std::vector<uint16_t>& s16, int64_t cpad, int64_t steps) {
-    std::vector<uint16_t> out(s16.size());
-    for (int64_t blk = 0; blk < cpad / 32; ++blk)
+std::vector<uint16_t> lane_packed16(const std::vector<uint16_t>& s16, int64_t cpad, int64_t steps, int64_t zbase) {
+    const int64_t groups = (steps + 7) / 8;
+    std::vector<uint16_t> out((size_t)((cpad / 32) * groups * 256), (uint16_t)zbase);
+    for (int64_t c = 0; c < cpad; ++c)
         for (int64_t st = 0; st < steps; ++st)
-            for (int64_t l = 0; l < 32; ++l)
-                out[(size_t)((blk * steps + st) * 32 + l)] = s16[(size_t)(st * cpad + blk * 32 + l)];
+            out[(size_t)((((c / 32) * groups + st / 8) * 32 + c % 32) * 8 + st % 8)] = s16[(size_t)(st * cpad + c)];
     return out;
 }
 

@@ -150,10 +150,12 @@ bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& pe
 bool window_schedule16(const GatherSchedule32& g, int64_t count, int64_t chunk, int64_t bw, std::vector<uint16_t>* out,
                        int64_t* zbase);
 
-// The [steps][cpad] window schedule rearranged block-major, [cpad / 32]
-// [steps][32]: the steps of one 32-column block 64 bytes apart, so that a
-// lane's successive schedule words sit at constant offsets.
-std::vector<uint16_t> block_major16(const std::vector<uint16_t>& s16, int64_t cpad, int64_t steps);
+// The [steps][cpad] window schedule rearranged lane-packed, [cpad / 32]
+// [ceil(steps / 8)][32][8]: eight successive steps of a column in one
+// 16-byte word, so that one load serves eight steps and a warp's load is
+// one contiguous 512-byte segment.  Steps past the last are padded with the
+// zero slot zbase (offset zbase, + sign).
+std::vector<uint16_t> lane_packed16(const std::vector<uint16_t>& s16, int64_t cpad, int64_t steps, int64_t zbase);
 
 // Build both layouts for one spin from a term list.  Returns ED_OK or an
 // error (bad site, table overflow, complex term in a real operator when

@@ -235,14 +235,23 @@ static int check(const char* name, int n, int q, const std::vector<ed_term>& ter
                 std::printf("%s window schedule shape\n", name);
                 return 1;
             }
-            // the block-major copy k_mv_down reads: word (c, st) at ((c / 32) nst + st) 32 + c % 32
-            const std::vector<uint16_t> bm = block_major16(s16, cpd, nst);
+            // the lane-packed copy k_mv_down reads: word (c, st) at
+            // (((c / 32) g8 + st / 8) 32 + c % 32) 8 + st % 8, the steps past
+            // the last on the zero slot zb16
+            const int64_t g8 = (nst + 7) / 8;
+            const std::vector<uint16_t> bm = lane_packed16(s16, cpd, nst, zb16);
+            if ((int64_t)bm.size() != (cpd / 32) * g8 * 256) {
+                std::printf("%s lane-packed schedule size\n", name);
+                return 1;
+            }
             for (int64_t c = 0; c < cpd; ++c)
-                for (int64_t st = 0; st < nst; ++st)
-                    if (bm[(size_t)(((c / 32) * nst + st) * 32 + c % 32)] != s16[(size_t)(st * cpd + c)]) {
-                        std::printf("%s block-major schedule\n", name);
+                for (int64_t st = 0; st < g8 * 8; ++st) {
+                    const uint16_t want = st < nst ? s16[(size_t)(st * cpd + c)] : (uint16_t)zb16;
+                    if (bm[(size_t)((((c / 32) * g8 + st / 8) * 32 + c % 32) * 8 + st % 8)] != want) {
+                        std::printf("%s lane-packed schedule\n", name);
                         return 1;
                     }
+                }
             for (int64_t c = 0; c < cpd; ++c) {
                 const int64_t k = c / chunk;
                 const int64_t w0 = std::max<int64_t>(0, k * chunk - bw2) & ~(int64_t)15;
