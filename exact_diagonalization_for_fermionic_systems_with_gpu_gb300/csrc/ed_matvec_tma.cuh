@@ -319,9 +319,12 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
         const int64_t du = __ldg(a.dUPq + u);
         const uint32_t ubase = u * dimDN;
 
-        for (uint32_t d0 = tid; d0 < dimDN; d0 += 2 * T) {
+        // two columns (d0, d0 + T) per iteration; one in the class-segmented
+        // path, which takes its columns one after the other anyway (fewer
+        // live 128-bit accumulators)
+        for (uint32_t d0 = tid; d0 < dimDN; d0 += (SEG ? 1u : 2u) * T) {
             const uint32_t d1 = d0 + T;
-            const bool v1 = d1 < dimDN;
+            const bool v1 = !SEG && d1 < dimDN;
             const uint32_t d1c = v1 ? d1 : d0;  // clamp: the second column repeats d0 and is not stored
             i128 ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;
             if (FAST) {
@@ -408,11 +411,10 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                 // from the rows' class-end bytes (+ entries first), the same
                 // loop bounds for every lane in the up row; with equal class
                 // lists the up and down sums of a class share one product.
-                // The two columns one after the other (register budget).
                 const uint32_t se_u = __ldg(a.upSegE + u), sp_u = __ldg(a.upSegP + u);
                 const int ncl = max(a.nclsUP, a.nclsDN);
 #pragma unroll 1
-                for (int cc = 0; cc < 2; ++cc) {
+                for (int cc = 0; cc < (v1 ? 2 : 1); ++cc) {
                     const uint32_t d = cc ? d1c : d0;
                     // this column's accumulators, stored into ar0/ai0 or
                     // ar1/ai1 at the end (not a reference chosen at run time,
