@@ -957,8 +957,6 @@ cudaError_t launch_lz_multi(int device, int kinds, const LzMultiArgs& f, cudaStr
 
 // Cooperative launch of the batch: grid and shared memory of the first
 // operator's plan.
-// Cooperative launch of the batch: grid and shared memory of the first
-// operator's plan.
 cudaError_t launch_lz_batch(const ed_op* op, const LzBatchArgs& f, cudaStream_t s) {
     if (op->tma_smem <= 0 || op->cplx || !op->mv_fast || !op->mv.dnSched) return cudaErrorNotSupported;
     const void* fn = (const void*)k_lz_batch;

@@ -264,28 +264,18 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
     const bool unitD = a.unitDN != 0 && a.nclsDN == 1;
     const uint32_t nq = (uint32_t)a.dimUP;
 
-    bool issued_next = false;  // thread 0: a copy for the next row is in flight
+    // The next row is taken and its copy issued by the last thread (with
+    // rows shorter than 2T it has the fewest columns) after the barrier below:
+    // the queue atomic, issued at the row start, and the row-index lookup
+    // then keep no thread from that barrier.
+    const int qt = T - 1;
     const uint32_t r1 = DYN ? nq : __ldg(a.rowStart + blockIdx.x + 1);
     for (uint32_t r = DYN ? blockIdx.x : __ldg(a.rowStart + blockIdx.x); r < r1; ++rc) {
         const uint32_t u = DYN ? __ldg(a.rowQueue + r) : __ldg(a.rowList + r);
         const int buf = rc & 1;
         const uint32_t parity = (rc >> 1) & 1;
-        // prefetch the next row into the other buffer (its readers finished
-        // at the barrier that closed the previous iteration)
-        issued_next = false;
-        if (tid == 0) {
-            uint32_t rn = r + 1;
-            if (DYN) {
-                rn = gridDim.x + atomicAdd(taken, 1u);
-                *snext = rn;
-            }
-            if (rn < r1) {
-                const uint32_t un = DYN ? __ldg(a.rowQueue + rn) : __ldg(a.rowList + rn);
-                tma::fence_proxy_async_smem();
-                tma_issue_row<CPLX>(a, S, xq, un, buf ^ 1);
-                issued_next = true;
-            }
-        }
+        uint32_t taken_at = 0;
+        if (DYN && tid == qt) taken_at = atomicAdd(taken, 1u);  // consumed after the barrier
         const uint32_t p0 = __ldg(a.upPtr + u), lenU = __ldg(a.upPtr + u + 1) - p0;
         const int nposU = FAST ? (int)__ldg(a.upNpos + u) : 0;
         for (uint32_t k = tid; k < lenU; k += T) {
@@ -303,17 +293,24 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
         }
         __syncthreads();
         if (*S.give_up) {
-            // every copy still counted on a barrier must land before the CTA
-            // leaves and its shared memory is reassigned: the current row's
-            // (the wait that gave up, once more) and the next row's, each
-            // wait bounded; if one gives up again the rows are undefined
-            if (tid == 0) {
-                tma::mbar_wait(&S.bar[buf], parity);
-                if (issued_next) tma::mbar_wait(&S.bar[buf ^ 1], ((rc + 1) >> 1) & 1);
-            }
+            // the current row's copy (the wait that gave up) is the only one
+            // counted on a barrier: it must land before the CTA leaves and its
+            // shared memory is reassigned (bounded; if it gives up again the
+            // rows are undefined)
+            if (tid == 0) tma::mbar_wait(&S.bar[buf], parity);
             return;
         }
-        const uint32_t r_next = DYN ? *snext : r + 1;  // written by thread 0 before the barrier above
+        // prefetch the next row into the other buffer (its readers finished
+        // at the barrier that closed the previous iteration)
+        if (tid == qt) {
+            const uint32_t rn = DYN ? gridDim.x + taken_at : r + 1;
+            if (DYN) *snext = rn;
+            if (rn < r1) {
+                const uint32_t un = DYN ? __ldg(a.rowQueue + rn) : __ldg(a.rowList + rn);
+                tma::fence_proxy_async_smem();
+                tma_issue_row<CPLX>(a, S, xq, un, buf ^ 1);
+            }
+        }
         const int64_t* xrow = (buf ? S.row1 : S.row0) + tma_row_off<CPLX>(a, u);
         const uint64_t stu = __ldg(a.stUP + u);
         const int64_t du = __ldg(a.dUPq + u);
@@ -550,8 +547,8 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                 }
             }
         }
-        __syncthreads();  // row buffer and uoff are free for the next iteration
-        r = r_next;
+        __syncthreads();  // row buffer and uoff are free for the next iteration; *snext is written
+        r = DYN ? *snext : r + 1;
     }
 }
 
