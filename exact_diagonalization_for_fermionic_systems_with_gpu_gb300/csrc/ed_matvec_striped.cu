@@ -41,7 +41,7 @@ using namespace dev;
 
 constexpr int kStripe = 128;       // columns of a pass-U stripe (32 lanes x 4)
 constexpr int kDownThreads = 1024;
-constexpr int kUpThreads = 768;    // 24 warps (80 registers a thread): 24 rows of a stripe per item
+constexpr int kUpThreads = 896;    // 28 warps (71 registers a thread): 28 rows of a stripe per item
 
 // One signed window word of the pass-D schedule: offset in bits 0..14, the
 // sign in bit 15 (m = 0 or -1, then a conditional two's-complement negation).
@@ -145,7 +145,7 @@ __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g
 
 // ---------------------------------------------------------------- pass U --
 // Column-stripe-major items: item = stripe * dim_up + row, one warp each;
-// warp w of CTA b takes items b * 24 + w, + 24 * gridDim.x, ...  A lane
+// warp w of CTA b takes items b * 28 + w, + 28 * gridDim.x, ...  A lane
 // holds two column pairs 64 columns apart (c, c + 1 and c + 64, c + 65), so
 // each 16-byte load instruction of the warp reads one contiguous 512-byte
 // segment; the second pair is absent past the end of the row.  Row offsets
@@ -177,16 +177,17 @@ __global__ void __launch_bounds__(kUpThreads, 1) k_mv_up(const MvArgs a, const S
         if (c >= dn32) continue;
         const bool two = c + 64u < dn32;  // the second pair of columns exists
         const uint32_t rowu = (uint32_t)u * dn32 + c;
-        // the row's own values and down sums first: their HBM latency overlaps the gathers
-        longlong2 dsv[2], xs[2];
-        dsv[0] = __ldcs(reinterpret_cast<const longlong2*>(g.sdn + rowu));
-        xs[0] = __ldcg(reinterpret_cast<const longlong2*>(xq + rowu));
-        if (two) {
-            dsv[1] = __ldcs(reinterpret_cast<const longlong2*>(g.sdn + rowu + 64u));
-            xs[1] = __ldcg(reinterpret_cast<const longlong2*>(xq + rowu + 64u));
-        } else {
-            dsv[1] = make_longlong2(0, 0);
-            xs[1] = dsv[1];
+        // the row's down sums (streamed from HBM) are prefetched into L2 by one
+        // bulk prefetch now and read after the gathers, with the row's own
+        // values (in the L2-resident stripe): no registers held across the
+        // gathers for them, which leaves room for 28 warps per SM
+        if (lane == 0) {
+            const uint32_t c0 = (uint32_t)(st * kStripe);
+            const uint32_t nb = ((dn32 - c0 < (uint32_t)kStripe ? dn32 - c0 : (uint32_t)kStripe) * 8u) & ~15u;
+            if (nb)
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(g.sdn + (uint32_t)u * dn32 + c0),
+                             "r"(nb)
+                             : "memory");
         }
         const uint32_t p0 = __ldg(a.upPtr + u), len = __ldg(a.upPtr + u + 1) - p0;
         const int npos = (int)__ldg(a.upNpos + u);
@@ -211,6 +212,16 @@ __global__ void __launch_bounds__(kUpThreads, 1) k_mv_up(const MvArgs a, const S
             sp[1] -= v0.y;
             sp[2] -= v1.x;
             sp[3] -= v1.y;
+        }
+        longlong2 dsv[2], xs[2];
+        dsv[0] = __ldcs(reinterpret_cast<const longlong2*>(g.sdn + rowu));
+        xs[0] = __ldcg(reinterpret_cast<const longlong2*>(xq + rowu));
+        if (two) {
+            dsv[1] = __ldcs(reinterpret_cast<const longlong2*>(g.sdn + rowu + 64u));
+            xs[1] = __ldcg(reinterpret_cast<const longlong2*>(xq + rowu + 64u));
+        } else {
+            dsv[1] = make_longlong2(0, 0);
+            xs[1] = dsv[1];
         }
         const uint64_t stu = __ldg(a.stUP + u);
         const int64_t du = __ldg(a.dUPq + u);
