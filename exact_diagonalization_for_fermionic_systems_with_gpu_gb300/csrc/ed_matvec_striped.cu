@@ -115,6 +115,18 @@ __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g
             if (tid == 0) tma::mbar_wait(&bar, phase);
             return;
         }
+        if (tid == 32 && it + gridDim.x < nitems) {
+            // the next item's window into L2 while this one is summed, so
+            // that its copy into shared memory does not wait on HBM
+            const int64_t itn = it + gridDim.x, un = itn / nchunk, kn = itn - un * nchunk;
+            const int64_t c0n = kn * g.chunk, c1n = min(c0n + (int64_t)g.chunk, dimDN);
+            const int64_t w0n = max((int64_t)0, c0n - g.bw) & ~(int64_t)15;
+            int64_t w1n = min(dimDN, c1n + g.bw);
+            w1n = (w1n + 1) & ~(int64_t)1;
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(g.xq + un * dimDN + w0n),
+                         "r"((uint32_t)((w1n - w0n) * 8))
+                         : "memory");
+        }
         // two columns per iteration (c and c + 1024): their schedule words are
         // loaded together
         for (int64_t c = c0 + tid; c < c1; c += 2 * kDownThreads) {
