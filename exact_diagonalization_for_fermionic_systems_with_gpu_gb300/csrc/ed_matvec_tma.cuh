@@ -312,8 +312,6 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
             }
         }
         const int64_t* xrow = (buf ? S.row1 : S.row0) + tma_row_off<CPLX>(a, u);
-        const uint64_t stu = __ldg(a.stUP + u);
-        const int64_t du = __ldg(a.dUPq + u);
         const uint32_t ubase = u * dimDN;
 
         // two columns (d0, d0 + T) per iteration; one in the class-segmented
@@ -515,6 +513,9 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
                     }
                 }
             }
+            // the row's diagonal terms, read here rather than held across the sums
+            const uint64_t stu = __ldg(a.stUP + u);
+            const int64_t du = __ldg(a.dUPq + u);
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
                 if (c == 1 && !v1) break;
