@@ -43,26 +43,24 @@ constexpr int kStripe = 128;       // columns of a pass-U stripe (32 lanes x 4)
 constexpr int kDownThreads = 1024;
 constexpr int kUpThreads = 896;    // 28 warps (71 registers a thread): 28 rows of a stripe per item
 
-// One signed window word of the pass-D schedule: offset in bits 0..14, the
-// sign in bit 15 (m = 0 or -1, then a conditional two's-complement negation).
-__device__ __forceinline__ int64_t down_term(const int64_t* win, uint32_t e) {
-    const int64_t v = win[e & 0x7FFFu];
-    const int64_t m = -(int64_t)((e >> 15) & 1u);
-    return (v ^ m) - m;
-}
-
-// The steps of one lane-packed 16-byte schedule word (eight 16-bit words);
-// GUARD: only the first rem of them (the last, partial group of a column).
+// The steps of one lane-packed 16-byte schedule word (eight 16-bit words:
+// window offset in bits 0..14, the sign in bit 15); GUARD: only the first rem
+// of them (the last, partial group of a column).  A term is (v ^ m) - m with
+// m = 0 or -1 from the sign bit; the -m parts are summed apart as a count.
 template <bool GUARD>
 __device__ __forceinline__ int64_t down_group(const int64_t* win, const uint4 w, int rem) {
     const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
     int64_t acc = 0;
+    int32_t cnt = 0;
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
         if (GUARD && t >= rem) break;
-        acc += down_term(win, (t & 1) ? ws[t >> 1] >> 16 : ws[t >> 1] & 0xFFFFu);
+        const uint32_t e = (t & 1) ? ws[t >> 1] >> 16 : ws[t >> 1] & 0xFFFFu;
+        const int32_t m = (t & 1) ? ((int32_t)ws[t >> 1] >> 31) : ((int32_t)(ws[t >> 1] << 16) >> 31);
+        acc += win[e & 0x7FFFu] ^ (int64_t)m;
+        cnt -= m;
     }
-    return acc;
+    return acc + cnt;
 }
 
 // Groups q0 .. of one column's n steps: whole groups, then the partial one.
