@@ -57,6 +57,53 @@ def test_matvec_real_vs_oracle(ed, orc, case):
         assert rel_err(y, yo) < TOL, (name, rel_err(y, yo))
 
 
+def degenerate_cases():
+    """Sectors with an empty or a full spin species (a one-dimensional spin
+    space: one row of the product basis, or rows of one element), a sector
+    with no particle at all, and a small square one: the row engine's edge
+    shapes (grid larger than the row count, odd one-element rows, empty hop
+    tables)."""
+    return [
+        ("chain8_04", 8, 0, 4), ("chain8_40", 8, 4, 0), ("chain8_84", 8, 8, 4), ("chain8_48", 8, 4, 8),
+        ("chain8_00", 8, 0, 0), ("chain8_17", 8, 1, 7), ("chain12_06", 12, 0, 6),
+    ]
+
+
+@pytest.mark.parametrize("case", degenerate_cases(), ids=lambda c: c[0])
+def test_matvec_degenerate_sectors_vs_oracle(ed, orc, case):
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    name, N, qu, qd = case
+    t = L.chain(N, eps=list(philox_uniform(5, N, 1.5)))
+    op = make_op(ed, N, qu, qd, t, t, 4.0)
+    tu, td = orc.Tables(N, qu, t), orc.Tables(N, qd, t)
+    assert op.rows() == tu.count * td.count
+    x = np.random.default_rng(3).standard_normal(op.rows())
+    y = op.matvec(x)
+    yo = orc.matvec(tu, td, 4.0, x)
+    if not np.any(yo):
+        assert not np.any(y), name  # the empty sector's operator is zero
+    else:
+        assert rel_err(y, yo) < TOL, (name, rel_err(y, yo))
+    op.close()
+
+
+@pytest.mark.parametrize("case", degenerate_cases(), ids=lambda c: c[0])
+def test_lanczos_degenerate_sectors_vs_dense(ed, orc, case):
+    """Lanczos on the same sectors (fixed steps, up to the dimension: the
+    one-row sectors break down after the first step and T stops there)
+    against the lowest eigenvalue of the oracle's dense Hamiltonian."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    name, N, qu, qd = case
+    t = L.chain(N, eps=list(philox_uniform(5, N, 1.5)))
+    op = make_op(ed, N, qu, qd, t, t, 4.0)
+    e0, _ = ed.Lanczos().eigen(op, max_steps=min(200, op.rows()), mode="fixed", ritz="none", seed=0)
+    H = orc.hamiltonian(N, qu, qd, t, t, 4.0)
+    H = H.toarray() if hasattr(H, "toarray") else np.asarray(H)
+    e_ref = float(np.linalg.eigvalsh(H)[0])
+    assert abs(e0 - e_ref) < 1e-10 * max(1.0, abs(e_ref)), (name, e0, e_ref)
+    op.close()
+
+
 def test_matvec_device_path_matches_host_path(ed):
     import torch
     from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
