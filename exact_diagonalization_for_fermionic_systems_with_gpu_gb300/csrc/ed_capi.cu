@@ -231,6 +231,7 @@ static ed_status plan_striped(ed_op* op, bool forced, int64_t chunk_cap = 16384)
     std::vector<uint16_t> s16;
     int64_t zbase = 0;
     if (!ed::window_schedule16(g, op->dimDN, chunk, bw, &s16, &zbase)) return ED_OK;
+    const std::vector<uint8_t> negc = ed::schedule_negcount(g);
     const int64_t sched_steps = std::max(g.steps, 1);
     const std::vector<uint16_t> s16bm = ed::lane_packed16(s16, g.count_pad, sched_steps, zbase);
     const int Fc = op->mv.Fc;
@@ -242,12 +243,13 @@ static ed_status plan_striped(ed_op* op, bool forced, int64_t chunk_cap = 16384)
     }
     // a re-plan (the autotuner's chunk axis) replaces the previous tables
     cudaFree(op->d_permDN); cudaFree(op->d_sched16); cudaFree(op->d_steps32); cudaFree(op->d_dDNqP);
-    cudaFree(op->d_stDNp);
+    cudaFree(op->d_stDNp); cudaFree(op->d_negDN);
     op->d_permDN = nullptr; op->d_sched16 = nullptr; op->d_steps32 = nullptr; op->d_dDNqP = nullptr;
-    op->d_stDNp = nullptr;
+    op->d_stDNp = nullptr; op->d_negDN = nullptr;
     if (upload(&op->d_permDN, perm.data(), perm.size()) != cudaSuccess ||
         upload(&op->d_sched16, s16bm.data(), s16bm.size()) != cudaSuccess ||
         upload(&op->d_steps32, g.steps32.data(), g.steps32.size()) != cudaSuccess ||
+        upload(&op->d_negDN, negc.data(), negc.size()) != cudaSuccess ||
         upload(&op->d_dDNqP, dq.data(), dq.size()) != cudaSuccess ||
         upload(&op->d_stDNp, st.data(), st.size()) != cudaSuccess)
         return ED_ERR_ALLOC;
@@ -618,7 +620,7 @@ ed_status ed_op_destroy(ed_op* op) {
     cudaFree(op->d_dnSched); cudaFree(op->d_dnSteps); cudaFree(op->d_rowStart); cudaFree(op->d_rowList); cudaFree(op->d_rowQueue);
     cudaFree(op->d_upSegE); cudaFree(op->d_upSegP); cudaFree(op->d_dnSegE); cudaFree(op->d_dnSegP);
     cudaFree(op->d_permDN); cudaFree(op->d_sched16); cudaFree(op->d_steps32); cudaFree(op->d_dDNqP);
-    cudaFree(op->d_stDNp); cudaFree(op->d_sdn);
+    cudaFree(op->d_stDNp); cudaFree(op->d_sdn); cudaFree(op->d_negDN);
     cudaFree(op->d_err);
     cudaFree(op->d_dUPq); cudaFree(op->d_dDNq); cudaFree(op->d_stUP); cudaFree(op->d_stDN);
     cudaFree(op->d_xq); cudaFree(op->d_emax); cudaFree(op->d_flag); cudaFree(op->d_io);

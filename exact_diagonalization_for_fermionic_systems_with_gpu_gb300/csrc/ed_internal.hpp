@@ -90,6 +90,7 @@ struct StripedArgs {
     int64_t dimUP, dimDN;
     const uint16_t* sched16;  // [cpad / 32][s8][32][8] offset in the chunk's window | sign << 15; idle: a zero slot
     const uint8_t* steps32;   // steps the warp of 32-column block k runs
+    const uint8_t* negcnt;    // negative entries of each (permuted) column
     int64_t cpad;
     int s8;                   // groups of eight schedule steps
     int64_t bw;               // bandwidth of the permuted down index
@@ -151,6 +152,7 @@ struct ed_op {
     uint32_t* d_permDN = nullptr;
     uint16_t* d_sched16 = nullptr;
     uint8_t* d_steps32 = nullptr;
+    uint8_t* d_negDN = nullptr;   // negative entries per permuted down column
     int64_t* d_dDNqP = nullptr;
     uint64_t* d_stDNp = nullptr;
     int64_t* d_sdn = nullptr;   // D down sums, allocated on first use

@@ -289,6 +289,7 @@ cudaError_t striped_args(ed_op* op, const int64_t* xq, StripedArgs* g) {
     g->dimDN = op->dimDN;
     g->sched16 = op->d_sched16;
     g->steps32 = op->d_steps32;
+    g->negcnt = op->d_negDN;
     g->cpad = op->st_cpad;
     g->s8 = op->st_s8;
     g->bw = op->st_bw;

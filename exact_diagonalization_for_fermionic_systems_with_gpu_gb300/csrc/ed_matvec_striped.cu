@@ -43,32 +43,52 @@ constexpr int kStripe = 128;       // columns of a pass-U stripe (32 lanes x 4)
 constexpr int kDownThreads = 1024;
 constexpr int kUpThreads = 896;    // 28 warps (71 registers a thread): 28 rows of a stripe per item
 
-// The steps of one lane-packed 16-byte schedule word (eight 16-bit words:
-// window offset in bits 0..14, the sign in bit 15); GUARD: only the first rem
-// of them (the last, partial group of a column).  A term is (v ^ m) - m with
-// m = 0 or -1 from the sign bit; the -m parts are summed apart as a count.
-template <bool GUARD>
-__device__ __forceinline__ int64_t down_group(const int64_t* win, const uint4 w, int rem) {
-    const uint32_t ws[4] = {w.x, w.y, w.z, w.w};
-    int64_t acc = 0;
-    int32_t cnt = 0;
-#pragma unroll
-    for (int t = 0; t < 8; ++t) {
-        if (GUARD && t >= rem) break;
-        const uint32_t e = (t & 1) ? ws[t >> 1] >> 16 : ws[t >> 1] & 0xFFFFu;
-        const int32_t m = (t & 1) ? ((int32_t)ws[t >> 1] >> 31) : ((int32_t)(ws[t >> 1] << 16) >> 31);
-        acc += win[e & 0x7FFFu] ^ (int64_t)m;
-        cnt -= m;
-    }
-    return acc + cnt;
+// One schedule word holds two steps (16 bits each: window offset in bits
+// 0..14, sign in bit 15; the even step in the low half).  A step adds
+// (v ^ m) with m = 0 or -1 from its sign bit; the -m parts of a column, the
+// number of its negative entries, are added once per column (g.negcnt).
+// Byte offsets come out of a word in two operations and the sign mask in one
+// (prmt replicating bit 15 or bit 31 over the word).
+__device__ __forceinline__ uint32_t off_lo(uint32_t w) { return (w << 3) & 0x3FFF8u; }
+__device__ __forceinline__ uint32_t off_hi(uint32_t w) { return (w >> 13) & 0x3FFF8u; }
+__device__ __forceinline__ uint32_t sgn_lo(uint32_t w) {
+    uint32_t m;
+    asm("prmt.b32 %0, %1, 0, 0x9999;" : "=r"(m) : "r"(w));
+    return m;
+}
+__device__ __forceinline__ uint32_t sgn_hi(uint32_t w) { return (uint32_t)((int32_t)w >> 31); }
+
+// v ^ (m, m): the 64-bit term of one step
+__device__ __forceinline__ uint64_t dterm(const unsigned char* winb, uint32_t off, uint32_t m) {
+    const uint64_t v = *reinterpret_cast<const uint64_t*>(winb + off);
+    uint64_t mm;
+    asm("mov.b64 %0, {%1, %1};" : "=l"(mm) : "r"(m));
+    return v ^ mm;
 }
 
-// Groups q0 .. of one column's n steps: whole groups, then the partial one.
-__device__ __forceinline__ int64_t down_tail(const int64_t* win, const uint4* p, int q0, int n) {
-    int64_t acc = 0;
-    int q = q0;
-    for (; q < (n >> 3); ++q) acc += down_group<false>(win, __ldg(p + 32 * q), 0);
-    if (n & 7) acc += down_group<true>(win, __ldg(p + 32 * q), n & 7);
+// The eight steps of one lane-packed 16-byte schedule group.
+__device__ __forceinline__ uint64_t dgroup8(const unsigned char* winb, const uint4 w) {
+    const uint64_t a = dterm(winb, off_lo(w.x), sgn_lo(w.x)) + dterm(winb, off_hi(w.x), sgn_hi(w.x));
+    const uint64_t b = dterm(winb, off_lo(w.y), sgn_lo(w.y)) + dterm(winb, off_hi(w.y), sgn_hi(w.y));
+    const uint64_t c = dterm(winb, off_lo(w.z), sgn_lo(w.z)) + dterm(winb, off_hi(w.z), sgn_hi(w.z));
+    const uint64_t d = dterm(winb, off_lo(w.w), sgn_lo(w.w)) + dterm(winb, off_hi(w.w), sgn_hi(w.w));
+    return (a + b) + (c + d);
+}
+
+// The first rem (0..7) steps of a group: one jump into the unrolled steps
+// (rem is the same for the 32 lanes of a warp).
+__device__ __forceinline__ uint64_t dtail(const unsigned char* winb, const uint4 w, int rem) {
+    uint64_t acc = 0;
+    switch (rem) {
+        case 7: acc += dterm(winb, off_lo(w.w), sgn_lo(w.w)); [[fallthrough]];
+        case 6: acc += dterm(winb, off_hi(w.z), sgn_hi(w.z)); [[fallthrough]];
+        case 5: acc += dterm(winb, off_lo(w.z), sgn_lo(w.z)); [[fallthrough]];
+        case 4: acc += dterm(winb, off_hi(w.y), sgn_hi(w.y)); [[fallthrough]];
+        case 3: acc += dterm(winb, off_lo(w.y), sgn_lo(w.y)); [[fallthrough]];
+        case 2: acc += dterm(winb, off_hi(w.x), sgn_hi(w.x)); [[fallthrough]];
+        case 1: acc += dterm(winb, off_lo(w.x), sgn_lo(w.x)); [[fallthrough]];
+        default: break;
+    }
     return acc;
 }
 
@@ -125,29 +145,25 @@ __global__ void __launch_bounds__(kDownThreads, 1) k_mv_down(const StripedArgs g
                          "r"((uint32_t)((w1n - w0n) * 8))
                          : "memory");
         }
-        // two columns per iteration (c and c + 1024): their schedule words are
-        // loaded together
-        for (int64_t c = c0 + tid; c < c1; c += 2 * kDownThreads) {
-            const int64_t cb = c + kDownThreads;
-            const bool hb = cb < c1;
-            const int na = __ldg(g.steps32 + (c >> 5)), nb = hb ? __ldg(g.steps32 + (cb >> 5)) : 0;
-            const int64_t cbb = hb ? cb : c;
-            const uint4* sa = reinterpret_cast<const uint4*>(g.sched16) + (size_t)(c >> 5) * (size_t)g.s8 * 32 + (c & 31);
-            const uint4* sb = reinterpret_cast<const uint4*>(g.sched16) + (size_t)(cbb >> 5) * (size_t)g.s8 * 32 + (cbb & 31);
-            int64_t acca = 0, accb = 0;
-            // whole groups of eight steps of both columns, one 16-byte
-            // schedule load per column and group
-            const int gm = (na < nb ? na : nb) >> 3;
-            int q = 0;
-            for (; q < gm; ++q) {
-                const uint4 wa = __ldg(sa + 32 * q), wb = __ldg(sb + 32 * q);
-                acca += down_group<false>(win, wa, 0);
-                accb += down_group<false>(win, wb, 0);
+        // one column per iteration: its step count, negative-entry count and
+        // first two schedule groups are loaded together, each later group one
+        // group ahead of its use
+        const unsigned char* winb = sm;
+        const uint4* sched = reinterpret_cast<const uint4*>(g.sched16);
+        for (int64_t c = c0 + tid; c < c1; c += kDownThreads) {
+            const uint4* sp = sched + (size_t)(c >> 5) * (size_t)g.s8 * 32 + (c & 31);
+            const int n = __ldg(g.steps32 + (c >> 5));
+            uint64_t acc = __ldg(g.negcnt + c);
+            uint4 cur = __ldg(sp), nxt = make_uint4(0u, 0u, 0u, 0u);
+            if (g.s8 > 1) nxt = __ldg(sp + 32);
+            const int full = n >> 3;
+            for (int q = 0; q < full; ++q) {
+                acc += dgroup8(winb, cur);
+                cur = nxt;
+                if (q + 2 < g.s8) nxt = __ldg(sp + 32 * (q + 2));
             }
-            acca += down_tail(win, sa, q, na);
-            if (hb) accb += down_tail(win, sb, q, nb);
-            g.sdn[u * dimDN + c] = acca;
-            if (hb) g.sdn[u * dimDN + cb] = accb;
+            acc += dtail(winb, cur, n & 7);
+            g.sdn[u * dimDN + c] = (int64_t)acc;
         }
         __syncthreads();  // the window is free for the next copy
     }

@@ -620,6 +620,16 @@ bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& pe
     return true;
 }
 
+std::vector<uint8_t> schedule_negcount(const GatherSchedule32& g) {
+    std::vector<uint8_t> neg((size_t)g.count_pad, 0);
+    for (int st = 0; st < g.steps; ++st)
+        for (int64_t c = 0; c < g.count_pad; ++c) {
+            const uint32_t w = g.ent[(size_t)st * g.count_pad + c];
+            if (w != kSched32None && (w & kSignBit)) ++neg[(size_t)c];
+        }
+    return neg;
+}
+
 std::vector<uint16_t> lane_packed16(const std::vector<uint16_t>& s16, int64_t cpad, int64_t steps, int64_t zbase) {
     const int64_t groups = (steps + 7) / 8;
     std::vector<uint16_t> out((size_t)((cpad / 32) * groups * 256), (uint16_t)zbase);

@@ -137,6 +137,11 @@ struct GatherSchedule32 {
 bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
                              GatherSchedule32* g, std::string* err, int sign_filter = -1, int bank_cap = 1);
 
+// Negative entries of each column of a schedule (count_pad values, idle
+// lanes not counted).  Pass D adds v ^ m per step (m = -1 for a negative
+// entry: v ^ -1 = -v - 1) and this count once per column.
+std::vector<uint8_t> schedule_negcount(const GatherSchedule32& g);
+
 // Pass D's schedule (two-pass matvec): the permuted schedule g as 16-bit
 // words, step-major ([step][count_pad]), each the offset of the target in the
 // window of its column's chunk, x[w0 .. w1) with w0 = (k chunk - bw) rounded

@@ -223,6 +223,22 @@ static int check(const char* name, int n, int q, const std::vector<ed_term>& ter
     {
         GatherSchedule32 gc;
         build_gather_schedule32(t, perm2, inv2, &gc, &err, -1, 2);
+        // the per-column count of negative entries that k_mv_down adds once
+        const std::vector<uint8_t> neg = schedule_negcount(gc);
+        if ((int64_t)neg.size() != gc.count_pad) {
+            std::printf("%s negative counts: size\n", name);
+            return 1;
+        }
+        for (int64_t c = 0; c < gc.count_pad; ++c) {
+            int want = 0;
+            if (c < cnt)
+                for (int k = 0; k < t.len[perm2[c]]; ++k)
+                    want += (t.ent[(size_t)k * cnt + perm2[c]] & kSignBit) ? 1 : 0;
+            if (neg[(size_t)c] != want) {
+                std::printf("%s negative count of column %lld\n", name, (long long)c);
+                return 1;
+            }
+        }
         for (int64_t chunk : {(int64_t)1024, (int64_t)2048}) {
             std::vector<uint16_t> s16;
             int64_t zb16 = 0;
