@@ -35,12 +35,13 @@ cudaError_t launch_lz_multi(int device, int kinds, const LzMultiArgs& f, cudaStr
 
 constexpr int kLzThreads = 256;
 
-// Element-wise Lanczos kernels: about 8 elements per thread and at most four
-// 256-thread CTAs per SM, so each thread keeps several loads in flight and
-// the last-block reduction has few partials.
+// Element-wise Lanczos kernels: about 8 elements per thread and at most five
+// 256-thread CTAs per SM (all resident: these kernels take at most 48
+// registers a thread), so each thread keeps several loads in flight and the
+// last-block reduction has few partials.
 static int lz_grid(int64_t n) {
     int64_t g = (n + 8 * kLzThreads - 1) / (8 * kLzThreads);
-    if (g > 152 * 4) g = 152 * 4;
+    if (g > 152 * 5) g = 152 * 5;
     return (int)(g < 1 ? 1 : g);
 }
 
