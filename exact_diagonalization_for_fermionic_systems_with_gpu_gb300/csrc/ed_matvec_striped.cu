@@ -4,7 +4,8 @@
 //
 // Inside this path the down index is in reverse Cuthill-McKee order (the
 // vectors are permuted on the way in and out), so the down hops of column c
-// stay within +-B of c (B = the order's bandwidth, 8,672 at Lieb18).
+// stay within +-B of c (B = the order's bandwidth, 8,875 at Lieb18 after the
+// hop-count sort below).
 //
 // Pass D (k_mv_down): row-major.  A work item is (row u, chunk of C columns);
 //   the CTA copies the window x[u, c0-B .. c0+C+B) of the row into shared
@@ -15,8 +16,9 @@
 //   step, idle lanes on a zero slot; the columns are ordered by hop count
 //   within blocks of 256 so that a warp's lanes have similar step counts; the
 //   schedule is the same for every row and is read from L2, eight steps of
-//   a column packed in one 16-byte load).  Output: the exact int64 down sums
-//   S_dn.
+//   a column packed in one 16-byte load; a step adds the window value xor-ed
+//   with its sign mask, and a column's count of negative entries is added
+//   once).  Output: the exact int64 down sums S_dn.
 // Pass U (k_mv_up): column stripes of kStripe columns, stripe-major over all
 //   rows so that the stripe of x (dim_up x kStripe x 8 B) stays in L2 while
 //   every row's up neighbours gather from it; a warp computes one row of a
