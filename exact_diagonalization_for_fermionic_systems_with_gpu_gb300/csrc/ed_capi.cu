@@ -595,15 +595,21 @@ ed_status ed_op_create(ed_op** out, const ed_model_desc* desc, int device) {
         op->tma_grid = ed::tma_grid(op);
         std::vector<uint32_t> rs, rl, rq;
         ed::row_plan(op->tup, op->tma_grid, &rs, &rl, &rq);
+        const std::vector<uint32_t> uq = ed::unit_queue(rq, op->dimDN, op->tma_grid);
+        // room for the unit queue at any row plan (at most 4 units a row)
         if (upload(&op->d_rowStart, rs.data(), rs.size()) != cudaSuccess ||
             upload(&op->d_rowList, rl.data(), rl.size()) != cudaSuccess ||
-            upload(&op->d_rowQueue, rq.data(), rq.size()) != cudaSuccess) {
+            upload(&op->d_rowQueue, rq.data(), rq.size()) != cudaSuccess ||
+            cudaMalloc(&op->d_unitQueue, sizeof(uint32_t) * (rq.size() + 3 * (size_t)op->tma_grid + 4)) != cudaSuccess ||
+            cudaMemcpy(op->d_unitQueue, uq.data(), sizeof(uint32_t) * uq.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
             ed_op_destroy(op);
             return ED_ERR_ALLOC;
         }
         op->mv.rowStart = op->d_rowStart;
         op->mv.rowList = op->d_rowList;
         op->mv.rowQueue = op->d_rowQueue;
+        op->mv.unitQueue = op->d_unitQueue;
+        op->mv.nunits = (uint32_t)uq.size();
     }
     *out = op;
     return ED_OK;
@@ -618,6 +624,7 @@ ed_status ed_op_destroy(ed_op* op) {
     cudaFree(op->d_upNpos); cudaFree(op->d_dnNpos);
     cudaFree(op->d_upPtr); cudaFree(op->d_upEntC); cudaFree(op->d_dnPtr); cudaFree(op->d_dnEntC);
     cudaFree(op->d_dnSched); cudaFree(op->d_dnSteps); cudaFree(op->d_rowStart); cudaFree(op->d_rowList); cudaFree(op->d_rowQueue);
+    cudaFree(op->d_unitQueue);
     cudaFree(op->d_upSegE); cudaFree(op->d_upSegP); cudaFree(op->d_dnSegE); cudaFree(op->d_dnSegP);
     cudaFree(op->d_permDN); cudaFree(op->d_sched16); cudaFree(op->d_steps32); cudaFree(op->d_dDNqP);
     cudaFree(op->d_stDNp); cudaFree(op->d_sdn); cudaFree(op->d_negDN);
@@ -707,10 +714,13 @@ ed_status ed_lanczos_batch(ed_op* const* ops, int n_ops, const ed_lanczos_cfg* c
 static ed_status set_row_plan(ed_op* op, double w) {
     std::vector<uint32_t> rs, rl, rq;
     ed::row_plan(op->tup, op->tma_grid, &rs, &rl, &rq, w);
+    const std::vector<uint32_t> uq = ed::unit_queue(rq, op->dimDN, op->lz_grid > 0 ? op->lz_grid : op->tma_grid);
     if (cudaMemcpy(op->d_rowStart, rs.data(), sizeof(uint32_t) * rs.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(op->d_rowList, rl.data(), sizeof(uint32_t) * rl.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(op->d_rowQueue, rq.data(), sizeof(uint32_t) * rq.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+        cudaMemcpy(op->d_rowQueue, rq.data(), sizeof(uint32_t) * rq.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(op->d_unitQueue, uq.data(), sizeof(uint32_t) * uq.size(), cudaMemcpyHostToDevice) != cudaSuccess)
         return ED_ERR_CUDA;
+    op->mv.nunits = (uint32_t)uq.size();
     op->row_cost = w;
     return ED_OK;
 }

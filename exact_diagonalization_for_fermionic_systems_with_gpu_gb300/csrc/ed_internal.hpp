@@ -56,6 +56,11 @@ struct MvArgs {
     const uint32_t* rowStart;
     const uint32_t* rowList;
     const uint32_t* rowQueue;  // all rows in decreasing order of cost (dynamic distribution)
+    // The single-run persistent kernel's queue: rowQueue with its last rows
+    // (those past the last full wave of CTAs) split into column ranges.  An
+    // entry is a row, or row | part << 24 | log2(parts) << 28 for a range.
+    const uint32_t* unitQueue;
+    uint32_t nunits;           // entries of unitQueue
     int* err;             // device word set when a bounded wait gives up
     // shared-memory plan of the TMA kernel (byte offsets)
     int sm_row0, sm_row1, sm_dnptr, sm_dnent, sm_dnnpos, sm_ddnq, sm_stdn;
@@ -120,7 +125,7 @@ struct ed_op {
     uint32_t *d_upPtr = nullptr, *d_upEntC = nullptr, *d_dnPtr = nullptr, *d_dnEntC = nullptr;
     uint16_t* d_dnSched = nullptr;
     uint8_t* d_dnSteps = nullptr;
-    uint32_t *d_rowStart = nullptr, *d_rowList = nullptr, *d_rowQueue = nullptr;
+    uint32_t *d_rowStart = nullptr, *d_rowList = nullptr, *d_rowQueue = nullptr, *d_unitQueue = nullptr;
     uint32_t *d_upSegE = nullptr, *d_upSegP = nullptr, *d_dnSegE = nullptr, *d_dnSegP = nullptr;
     int* d_err = nullptr;
     int64_t *d_dUPq = nullptr, *d_dDNq = nullptr;
@@ -179,6 +184,10 @@ int tma_grid(const ed_op* op);
 // model 1 + w * len_up(u) / mean len_up (w from ED_ROW_COST_UP, default kRowCostUp).
 // queue: all rows in decreasing order of that cost.
 // w < 0: ED_ROW_COST_UP or kRowCostUp.
+// The persistent kernel's unit queue from a row queue for G CTAs: the rows
+// past the last full wave (rq.size() mod G of them, the cheapest) each split
+// into up to four column ranges of a multiple of 32 columns.
+std::vector<uint32_t> unit_queue(const std::vector<uint32_t>& rq, int64_t dimDN, int G);
 void row_plan(const SpinTable& up, int G, std::vector<uint32_t>* start, std::vector<uint32_t>* list,
               std::vector<uint32_t>* queue, double w = -1.0);
 cudaError_t launch_matvec_tma(const ed_op* op, const MvArgs& a, int out, cudaStream_t s);

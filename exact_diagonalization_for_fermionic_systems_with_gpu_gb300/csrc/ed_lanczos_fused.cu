@@ -185,7 +185,9 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
     const int tid = threadIdx.x;
     __shared__ uint32_t s_next;  // row-queue index taken by thread 0
     uint32_t u0 = 0;
-    const bool has_row = tma_first_row_dyn(a, &u0);
+    // real runs take the unit queue (its last rows split into column ranges,
+    // which narrows the CTAs' finishing spread); complex runs the row queue
+    const bool has_row = tma_first_row_dyn<!CPLX>(a, &u0);
     const uint32_t G = gridDim.x;
 
     if (tid == 0) {
@@ -252,7 +254,7 @@ __global__ void __launch_bounds__(kTmaThreads, 2) k_lz_fused(const MvArgs a, con
         {
             i128 dot = 0;
             uint64_t mx = 0;
-            tma_rows<CPLX, 1, FAST, true, SCHED, true, SEG>(a, S, xq, f.u, nullptr, rc, 0, s_u, dot, mx,
+            tma_rows<CPLX, 1, FAST, true, SCHED, true, SEG, false, !CPLX>(a, S, xq, f.u, nullptr, rc, 0, s_u, dot, mx,
                                                        f.taken + (j & 1), &s_next);
             if (give_up) return;
             if (stamp) st[1] = global_ns();

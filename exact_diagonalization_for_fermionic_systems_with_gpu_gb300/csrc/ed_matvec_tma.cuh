@@ -242,16 +242,20 @@ __device__ __forceinline__ bool tma_first_row(const MvArgs& a, uint32_t* u) {
 // rowQueue[gridDim.x + atomicAdd(taken, 1)] while it computes the current
 // one, so CTAs that finish early take more rows (the queue is in decreasing
 // order of cost).  *snext is a shared word for the index taken.
+// SPLIT: the unit queue (a.unitQueue), whose last entries are column ranges
+// of rows (low 24 bits: the row).
+template <bool SPLIT = false>
 __device__ __forceinline__ bool tma_first_row_dyn(const MvArgs& a, uint32_t* u) {
-    if (blockIdx.x >= (uint32_t)a.dimUP) return false;
-    *u = __ldg(a.rowQueue + blockIdx.x);
+    if (blockIdx.x >= (SPLIT ? a.nunits : (uint32_t)a.dimUP)) return false;
+    *u = SPLIT ? (__ldg(a.unitQueue + blockIdx.x) & 0xFFFFFFu) : __ldg(a.rowQueue + blockIdx.x);
     return true;
 }
 
 // GDIAG: the folded down diagonal is read from a.dDNq in global memory
 // instead of the staged copy (instances that share staged tables but not
 // their on-site terms, k_lz_multi).
-template <bool CPLX, int OUT, bool FAST, bool COH, bool SCHED, bool DYN, bool SEG = false, bool GDIAG = false>
+template <bool CPLX, int OUT, bool FAST, bool COH, bool SCHED, bool DYN, bool SEG = false, bool GDIAG = false,
+          bool SPLIT = false>
 __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, const int64_t* __restrict__ xq,
                                          int64_t* __restrict__ uq, double* __restrict__ y, uint32_t& rc, int E_out,
                                          int s_u, i128& dot, uint64_t& mx, unsigned int* taken = nullptr,
@@ -262,7 +266,8 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
     const bool merge = a.mergeUD != 0;
     const bool unitU = a.unitUP != 0 && a.nclsUP == 1;
     const bool unitD = a.unitDN != 0 && a.nclsDN == 1;
-    const uint32_t nq = (uint32_t)a.dimUP;
+    const uint32_t nq = SPLIT ? a.nunits : (uint32_t)a.dimUP;
+    const uint32_t* const queue = SPLIT ? a.unitQueue : a.rowQueue;
 
     // The next row is taken and its copy issued by the last thread (with
     // rows shorter than 2T it has the fewest columns) after the barrier below:
@@ -271,7 +276,16 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
     const int qt = T - 1;
     const uint32_t r1 = DYN ? nq : __ldg(a.rowStart + blockIdx.x + 1);
     for (uint32_t r = DYN ? blockIdx.x : __ldg(a.rowStart + blockIdx.x); r < r1; ++rc) {
-        const uint32_t u = DYN ? __ldg(a.rowQueue + r) : __ldg(a.rowList + r);
+        const uint32_t qe = DYN ? __ldg(queue + r) : __ldg(a.rowList + r);
+        const uint32_t u = SPLIT ? (qe & 0xFFFFFFu) : qe;
+        // the unit's columns: the whole row, or a range of a multiple of 32
+        // columns (the lanes keep their columns mod 32)
+        uint32_t lo = 0, hi = dimDN;
+        if (SPLIT && (qe >> 24)) {
+            const uint32_t P = 1u << (qe >> 28), ch = ((dimDN + P - 1) / P + 31u) & ~31u;
+            lo = ((qe >> 24) & 0xFu) * ch;
+            hi = min(dimDN, lo + ch);
+        }
         const int buf = rc & 1;
         const uint32_t parity = (rc >> 1) & 1;
         uint32_t taken_at = 0;
@@ -306,7 +320,7 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
             const uint32_t rn = DYN ? gridDim.x + taken_at : r + 1;
             if (DYN) *snext = rn;
             if (rn < r1) {
-                const uint32_t un = DYN ? __ldg(a.rowQueue + rn) : __ldg(a.rowList + rn);
+                const uint32_t un = DYN ? (__ldg(queue + rn) & (SPLIT ? 0xFFFFFFu : 0xFFFFFFFFu)) : __ldg(a.rowList + rn);
                 tma::fence_proxy_async_smem();
                 tma_issue_row<CPLX>(a, S, xq, un, buf ^ 1);
             }
@@ -317,9 +331,9 @@ __device__ __forceinline__ void tma_rows(const MvArgs& a, const TmaSmem& S, cons
         // two columns (d0, d0 + T) per iteration; one in the class-segmented
         // path, which takes its columns one after the other anyway (fewer
         // live 128-bit accumulators)
-        for (uint32_t d0 = tid; d0 < dimDN; d0 += (SEG ? 1u : 2u) * T) {
+        for (uint32_t d0 = lo + tid; d0 < hi; d0 += (SEG ? 1u : 2u) * T) {
             const uint32_t d1 = d0 + T;
-            const bool v1 = !SEG && d1 < dimDN;
+            const bool v1 = !SEG && d1 < hi;
             const uint32_t d1c = v1 ? d1 : d0;  // clamp: the second column repeats d0 and is not stored
             i128 ar0 = 0, ai0 = 0, ar1 = 0, ai1 = 0;
             if (FAST) {
