@@ -184,10 +184,6 @@ int tma_grid(const ed_op* op);
 // model 1 + w * len_up(u) / mean len_up (w from ED_ROW_COST_UP, default kRowCostUp).
 // queue: all rows in decreasing order of that cost.
 // w < 0: ED_ROW_COST_UP or kRowCostUp.
-// The persistent kernel's unit queue from a row queue for G CTAs: the rows
-// past the last full wave (rq.size() mod G of them, the cheapest) each split
-// into up to four column ranges of a multiple of 32 columns.
-std::vector<uint32_t> unit_queue(const std::vector<uint32_t>& rq, int64_t dimDN, int G);
 void row_plan(const SpinTable& up, int G, std::vector<uint32_t>* start, std::vector<uint32_t>* list,
               std::vector<uint32_t>* queue, double w = -1.0);
 cudaError_t launch_matvec_tma(const ed_op* op, const MvArgs& a, int out, cudaStream_t s);

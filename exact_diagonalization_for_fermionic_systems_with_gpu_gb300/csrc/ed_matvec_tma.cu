@@ -152,22 +152,6 @@ int tma_grid(const ed_op* op) {
     return sms * per_sm;
 }
 
-std::vector<uint32_t> unit_queue(const std::vector<uint32_t>& rq, int64_t dimDN, int G) {
-    const size_t k = G > 0 ? rq.size() % (size_t)G : 0;
-    // parts of a multiple of 32 columns, every one of them non-empty
-    int lg = 2;
-    while (lg > 0) {
-        const int64_t P = (int64_t)1 << lg, ch = ((dimDN + P - 1) / P + 31) / 32 * 32;
-        if ((P - 1) * ch < dimDN) break;
-        --lg;
-    }
-    if (k == 0 || lg == 0) return rq;
-    std::vector<uint32_t> q(rq.begin(), rq.end() - (std::ptrdiff_t)k);
-    for (size_t i = rq.size() - k; i < rq.size(); ++i)
-        for (uint32_t part = 0; part < (1u << lg); ++part) q.push_back(rq[i] | part << 24 | (uint32_t)lg << 28);
-    return q;
-}
-
 void row_plan(const SpinTable& up, int G, std::vector<uint32_t>* start, std::vector<uint32_t>* list,
               std::vector<uint32_t>* queue, double w) {
     const int64_t n = up.count;

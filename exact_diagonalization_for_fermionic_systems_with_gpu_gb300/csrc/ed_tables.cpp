@@ -3,6 +3,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdlib>
 #include <map>
 
@@ -618,6 +619,22 @@ bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& pe
         st = (uint8_t)std::max<int>(st, D);
     }
     return true;
+}
+
+std::vector<uint32_t> unit_queue(const std::vector<uint32_t>& rq, int64_t dimDN, int G) {
+    const size_t k = G > 0 ? rq.size() % (size_t)G : 0;
+    // parts of a multiple of 32 columns, every one of them non-empty
+    int lg = 2;
+    while (lg > 0) {
+        const int64_t P = (int64_t)1 << lg, ch = ((dimDN + P - 1) / P + 31) / 32 * 32;
+        if ((P - 1) * ch < dimDN) break;
+        --lg;
+    }
+    if (k == 0 || lg == 0) return rq;
+    std::vector<uint32_t> q(rq.begin(), rq.end() - (std::ptrdiff_t)k);
+    for (size_t i = rq.size() - k; i < rq.size(); ++i)
+        for (uint32_t part = 0; part < (1u << lg); ++part) q.push_back(rq[i] | part << 24 | (uint32_t)lg << 28);
+    return q;
 }
 
 std::vector<uint8_t> schedule_negcount(const GatherSchedule32& g) {

@@ -137,6 +137,15 @@ struct GatherSchedule32 {
 bool build_gather_schedule32(const SpinTable& t, const std::vector<uint32_t>& perm, const std::vector<uint32_t>& inv,
                              GatherSchedule32* g, std::string* err, int sign_filter = -1, int bank_cap = 1);
 
+// The persistent Lanczos kernel's unit queue from a row queue rq for G CTAs:
+// the rows past the last full wave (rq.size() mod G of them, the cheapest)
+// each split into up to four column ranges.  An entry is a row, or
+// row | part << 24 | log2(P) << 28 for part `part` of P: columns
+// [part ch, min(dimDN, (part + 1) ch)) with ch = ceil(ceil(dimDN / P) / 32) 32,
+// every part non-empty (P = 1, no split, when dimDN is too narrow).  At most
+// rq.size() + 3 (G - 1) entries; rows below 2^24.
+std::vector<uint32_t> unit_queue(const std::vector<uint32_t>& rq, int64_t dimDN, int G);
+
 // Negative entries of each column of a schedule (count_pad values, idle
 // lanes not counted).  Pass D adds v ^ m per step (m = -1 for a negative
 // entry: v ^ -1 = -v - 1) and this count once per column.

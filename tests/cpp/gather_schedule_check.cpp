@@ -370,6 +370,53 @@ static int check(const char* name, int n, int q, const std::vector<ed_term>& ter
     return 0;
 }
 
+// The persistent kernel's unit queue: every (row, column) exactly once,
+// ranges of a multiple of 32 columns and non-empty, at most 3 (G - 1) more
+// entries than rows, whole rows first in the row queue's order.
+static int check_units() {
+    for (int64_t dimUP : {1, 5, 300, 924, 1000})
+        for (int64_t dimDN : {1, 20, 31, 32, 33, 64, 70, 100, 495, 924, 1000})
+            for (int G : {1, 7, 152, 304}) {
+                std::vector<uint32_t> rq((size_t)dimUP);
+                for (int64_t u = 0; u < dimUP; ++u) rq[(size_t)u] = (uint32_t)((u * 7919) % dimUP);
+                const std::vector<uint32_t> uq = unit_queue(rq, dimDN, G);
+                if (uq.size() > rq.size() + 3 * (size_t)(G - 1)) {
+                    std::printf("units %lld x %lld G %d: %zu entries\n", (long long)dimUP, (long long)dimDN, G, uq.size());
+                    return 1;
+                }
+                std::vector<int> hit((size_t)(dimUP * dimDN), 0);
+                size_t whole = 0;
+                for (size_t q = 0; q < uq.size(); ++q) {
+                    const uint32_t e = uq[q], u = e & 0xFFFFFFu;
+                    int64_t lo = 0, hi = dimDN;
+                    if (e >> 24) {
+                        const int64_t P = (int64_t)1 << (e >> 28), ch = ((dimDN + P - 1) / P + 31) / 32 * 32;
+                        lo = (int64_t)((e >> 24) & 0xFu) * ch;
+                        hi = std::min<int64_t>(dimDN, lo + ch);
+                        if (lo % 32 != 0 || lo >= hi || ((e >> 24) & 0xFu) >= (uint32_t)P) {
+                            std::printf("units %lld x %lld G %d: bad range\n", (long long)dimUP, (long long)dimDN, G);
+                            return 1;
+                        }
+                    } else {
+                        if (q != whole || rq[q] != u) {
+                            std::printf("units %lld x %lld G %d: whole rows out of order\n", (long long)dimUP,
+                                        (long long)dimDN, G);
+                            return 1;
+                        }
+                        ++whole;
+                    }
+                    for (int64_t d = lo; d < hi; ++d) ++hit[(size_t)(u * dimDN + d)];
+                }
+                for (int h : hit)
+                    if (h != 1) {
+                        std::printf("units %lld x %lld G %d: coverage\n", (long long)dimUP, (long long)dimDN, G);
+                        return 1;
+                    }
+            }
+    std::printf("unit queue ok\n");
+    return 0;
+}
+
 static std::vector<ed_term> bonds(const std::vector<std::pair<int, int>>& bs, double t) {
     std::vector<ed_term> v;
     for (auto& p : bs) v.push_back({ED_TERM_HOP, p.first, p.second, 0, t, 0.0});
@@ -410,5 +457,6 @@ int main() {
         std::vector<std::pair<int, int>> bs = {{0, 1}};
         fails += check("dimer_q1", 2, 1, bonds(bs, -1.0));
     }
+    fails += check_units();
     return fails ? 1 : 0;
 }

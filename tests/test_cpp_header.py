@@ -48,7 +48,8 @@ def test_cpp_header_lanczos_on_gpu(tmp_path, edlib, golden_energies):
 def test_gather_schedule_host_check(tmp_path):
     """The down-term gather schedule (host code, no GPU): every table entry
     scheduled exactly once, no bank pair used twice by one half warp in one
-    step, step counts covering the entries."""
+    step, step counts covering the entries; and the persistent kernel's unit
+    queue covering every (row, column) exactly once."""
     cxx = shutil.which("g++") or shutil.which("c++")
     if cxx is None:
         pytest.skip("no C++ compiler")
@@ -59,4 +60,5 @@ def test_gather_schedule_host_check(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stdout + out.stderr
     lines = out.stdout.strip().splitlines()
-    assert len(lines) == 5 and all(l.endswith(" ok") for l in lines)
+    assert len(lines) == 6 and all(l.endswith(" ok") for l in lines)
+    assert lines[-1] == "unit queue ok"
