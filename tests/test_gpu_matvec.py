@@ -104,6 +104,39 @@ def test_lanczos_degenerate_sectors_vs_dense(ed, orc, case):
     op.close()
 
 
+def complex_degenerate_cases():
+    """Kagome12 with a Peierls twist (complex, four coefficient classes) on
+    sectors with an empty or a full spin species, no particle, and one
+    particle against eleven."""
+    return [("k12_0_6", 0, 6), ("k12_6_0", 6, 0), ("k12_12_5", 12, 5), ("k12_5_12", 5, 12),
+            ("k12_0_0", 0, 0), ("k12_1_11", 1, 11)]
+
+
+@pytest.mark.parametrize("case", complex_degenerate_cases(), ids=lambda c: c[0])
+def test_complex_degenerate_sectors_vs_dense(ed, orc, case):
+    """Complex matvec against the oracle's dense Hamiltonian, and Lanczos E0
+    (fixed steps, up to the dimension) against its lowest eigenvalue."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
+    name, qu, qd = case
+    terms = L.kagome12(flux=0.37)
+    op = make_op(ed, 12, qu, qd, terms, terms, 4.0)
+    assert op.is_complex or not (0 < qu < 12 or 0 < qd < 12)
+    H = orc.hamiltonian(12, qu, qd, terms, terms, 4.0)
+    H = H.toarray() if hasattr(H, "toarray") else np.asarray(H)
+    assert H.shape == (op.rows(), op.rows())
+    rng = np.random.default_rng(7)
+    x = rng.standard_normal(op.rows()) + (1j * rng.standard_normal(op.rows()) if op.is_complex else 0)
+    y, yo = op.matvec(x), H @ x
+    if not np.any(yo):
+        assert not np.any(y), name
+    else:
+        assert rel_err(y, yo) < TOL, (name, rel_err(y, yo))
+    e0, _ = ed.Lanczos().eigen(op, max_steps=min(200, op.rows()), mode="fixed", ritz="none", seed=0)
+    e_ref = float(np.linalg.eigvalsh(H)[0])
+    assert abs(e0 - e_ref) < 1e-10 * max(1.0, abs(e_ref)), (name, e0, e_ref)
+    op.close()
+
+
 def test_matvec_device_path_matches_host_path(ed):
     import torch
     from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L
