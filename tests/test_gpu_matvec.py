@@ -257,6 +257,9 @@ def kernel_cases():
         ("chain8_04_no_up_hops", 8, 0, 4, L.chain(8), L.chain(8), 2.0),
         ("chain2_11", 2, 1, 1, L.chain(2, periodic=False), L.chain(2, periodic=False), 3.0),
         ("chain14_75", 14, 7, 5, L.chain(14), L.chain(14), 4.0),
+        # one-row sectors (an empty or a full up species) through every kernel
+        ("chain14_07", 14, 0, 7, L.chain(14), L.chain(14), 4.0),
+        ("chain14_147", 14, 14, 7, L.chain(14), L.chain(14), 4.0),
     ]
 
 

@@ -57,6 +57,40 @@ def test_mixed_sector_mixed_kind_batch_equals_single_runs(ed, edlib, steps):
         op.close()
 
 
+def test_degenerate_sector_batch_equals_single_runs(ed, edlib):
+    """A batch holding one-row sectors (an empty or a full up species), a
+    one-column sector (no down particle), a regular sector and a complex
+    one-row sector: each run equals its own single run bit for bit."""
+    import torch
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, sweeps
+    eu, edn = sweeps.mbl_disorder(2, 12, 6.0)
+    tu, td = sweeps.mbl_chain_terms(eu), sweeps.mbl_chain_terms(edn)
+    ops = [ed.Hubbard(ed.H_TBq(12, qu).extend(tu), ed.H_TBq(12, qd).extend(td), 1.0)
+           for qu, qd in ((0, 6), (12, 6), (6, 0), (6, 6))]
+    k = L.kagome12(flux=0.3)
+    ops.append(ed.Hubbard(ed.H_TBq(12, 0).extend(k), ed.H_TBq(12, 6).extend(k), 4.0))
+    steps = 40
+    sizes = [op.rows() * (2 if op.is_complex else 1) for op in ops]
+    offs = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    starts = torch.empty(int(offs[-1]), dtype=torch.float64, device="cuda")
+    for b, n in enumerate(sizes):
+        assert edlib.ed_random_vector_device(int(n), 200 + b, C.c_void_p(starts[int(offs[b])].data_ptr()), None) == 0
+    evecs = torch.empty_like(starts)
+    e0s, views, alpha, beta = ed.hubbard.lanczos_multi(ops, steps, starts=starts, evec_out=evecs, results=[])
+    sh = starts.cpu().numpy()
+    for b, op in enumerate(ops):
+        f = sh[int(offs[b]):int(offs[b + 1])].copy()
+        if op.is_complex:
+            f = f.view(np.complex128)
+        lz = ed.Lanczos()
+        e0, v = lz.eigen(op, f=f, max_steps=steps, mode="fixed", ritz="stored")
+        assert e0 == e0s[b], (b, e0, e0s[b])
+        assert np.array_equal(np.array(lz.a), alpha[b]) and np.array_equal(np.array(lz.b), beta[b])
+        assert np.array_equal(views[b].cpu().numpy(), v), b
+    for op in ops:
+        op.close()
+
+
 def test_homogeneous_batch_in_general_kernel_equals_specialised(ed, monkeypatch):
     """The same-sector real batch that the specialised kernel takes gives the
     same coefficients when ED_LZ_BATCH=multi routes it to the general one."""
