@@ -81,6 +81,28 @@ def test_entanglement_entropy_device(ed, orc, golden_energies):
         assert abs(a - ra) < 1e-10 and abs(b - rb) < 1e-9 * max(1.0, rb)
 
 
+@pytest.mark.parametrize("qu,qd", [(0, 6), (12, 6), (6, 0), (0, 0), (1, 11), (12, 12)])
+def test_observables_on_degenerate_sectors(ed, orc, golden_energies, qu, qd):
+    """Ground states of sectors with an empty or a full spin species (one
+    block of the entanglement reshape per species) and of the one-state
+    sectors: entanglement entropies of sites 0..5 against the oracle's dense
+    reshape + SVD, site densities against numpy."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    gg = golden_energies["chain12_open_W6_seed100_q66_U1"]
+    terms = L.chain(12, periodic=False, eps=gg["eps"])
+    op = ed.Hubbard(ed.H_TBq(12, qu).extend(terms), ed.H_TBq(12, qd).extend(terms), 1.0)
+    e0, v = ed.Lanczos().eigen(op, max_steps=min(300, op.rows()), mode="fixed", seed=1)
+    assert abs(np.linalg.norm(v) - 1.0) < 1e-12
+    a, b = ob.entanglement_entropy(op, v, list(range(6)))
+    ra, rb = orc.entanglement_entropy(v, 12, qu, qd, list(range(6)))
+    assert abs(a - ra) < 1e-10 and abs(b - rb) < 1e-9 * max(1.0, abs(rb)), (a, ra, b, rb)
+    nu, nd, dd = ob.site_densities(op, v)
+    ru, rd, rdd = numpy_densities(orc, 12, qu, qd, v)
+    assert np.max(np.abs(nu - ru)) < 1e-12 and np.max(np.abs(nd - rd)) < 1e-12 and np.max(np.abs(dd - rdd)) < 1e-12
+    assert abs(nu.sum() - qu) < 1e-12 and abs(nd.sum() - qd) < 1e-12
+    op.close()
+
+
 def test_drude_kubo_matches_oracle(ed, orc):
     """The reference's drude_weight_Jx on Kagome12 3+3 (U=4): the device
     result equals the oracle's restatement (oracle Lanczos, continued
