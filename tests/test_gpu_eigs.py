@@ -65,3 +65,25 @@ def test_eigs_reports_not_converged(ed):
     info = {}
     spectra.eigs_lowest(op, 5, ncv=8, tol=1e-14, max_restarts=1, result=info)
     assert not info["converged"] and info["restarts"] == 1 and info["nconv"] < 5
+
+
+def test_eigs_on_degenerate_sectors(ed, orc):
+    """One up particle against eleven down (dim 144): the 4 lowest pairs
+    against dense diagonalisation; a one-state sector cannot hold a pair
+    beyond its only state and is refused."""
+    from conftest import philox_uniform
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, spectra
+    t = L.chain(12, periodic=False, eps=list(philox_uniform(8, 12, 2.0)))
+    op = ed.Hubbard(ed.H_TBq(12, 1).extend(t), ed.H_TBq(12, 11).extend(t), 1.5)
+    nev = 4
+    info = {}
+    w, v, r = spectra.eigs_lowest(op, nev, result=info)
+    assert info["converged"]
+    wd = np.linalg.eigvalsh(orc.hamiltonian(12, 1, 11, t, t, 1.5).toarray())
+    assert np.min(np.diff(wd[: nev + 1])) > 1e-6
+    assert np.max(np.abs(w - wd[:nev])) < 1e-10 * np.max(np.abs(wd[:nev]))
+    op.close()
+    one = ed.Hubbard(ed.H_TBq(12, 0).extend(t), ed.H_TBq(12, 0).extend(t), 1.5)
+    with pytest.raises(Exception):
+        spectra.eigs_lowest(one, 1)
+    one.close()

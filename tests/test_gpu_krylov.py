@@ -50,6 +50,28 @@ def test_krylov_matches_dense(ed, orc, case):
     assert info["err_est"] < 1e-9 * nrm
 
 
+@pytest.mark.parametrize("qu,qd", [(0, 0), (12, 12), (0, 6), (1, 11)])
+def test_krylov_degenerate_sectors(ed, orc, qu, qd):
+    """Sectors of one state (the recurrence stops after its first step) and
+    with an empty spin species, against dense exp(-iHt)."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import evolution as ev, lattices as L
+    from conftest import philox_uniform
+    t = L.chain(12, periodic=False, eps=list(philox_uniform(7, 12, 2.0)))
+    op = ed.Hubbard(ed.H_TBq(12, qu).extend(t), ed.H_TBq(12, qd).extend(t), 1.5)
+    Hd = orc.hamiltonian(12, qu, qd, t, t, 1.5)
+    Hd = Hd.toarray() if hasattr(Hd, "toarray") else np.asarray(Hd)
+    x = philox_uniform(13, 2 * op.rows())
+    psi0 = (x[0::2] + 1j * x[1::2]) * 0.5
+    times = [0.0, 0.4, 1.3, 2.0]
+    info = {}
+    got = ev.krylov_evolve(op, psi0, times, max_steps=250, tol=1e-12, result=info)
+    ref = dense_evolve(Hd, psi0, times)
+    nrm = np.linalg.norm(psi0)
+    for i in range(len(times)):
+        assert np.linalg.norm(got[i] - ref[i]) < 1e-10 * nrm, (qu, qd, times[i])
+    op.close()
+
+
 def test_krylov_stops_at_invariant_subspace(ed, orc):
     """A start in a tiny invariant subspace (2 sites, 1+1 particles: 4 states)
     stops the recurrence at beta < tol, like the reference's b < 1e-10."""
