@@ -210,6 +210,33 @@ def test_flux_response_vs_dense_sum_over_states(ed, orc, flux):
     assert abs((ep - 2 * e0 + em) / h ** 2 - second) < 1e-4 * max(1.0, abs(second))
 
 
+@pytest.mark.parametrize("qu,qd", [(0, 3), (12, 3)])
+def test_flux_response_on_degenerate_sectors(ed, orc, qu, qd):
+    """The flux response of Kagome12 sectors whose up species is empty or
+    full (only the down electrons carry current) against the dense sum over
+    states."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    N, U, flux = 12, 4.0, 0.3
+    terms = L.kagome12(flux=flux)
+    d1t, d2t = L.kagome12_flux_derivatives(flux)
+    H, e0, v = ground(ed, N, qu, qd, terms, U, steps=220)
+    dH = ed.Hubbard(ed.H_TBq(N, qu).extend(d1t), ed.H_TBq(N, qd).extend(d1t), 0.0)
+    d2H = ed.Hubbard(ed.H_TBq(N, qu).extend(d2t), ed.H_TBq(N, qd).extend(d2t), 0.0)
+    first, second = ob.response(H, dH, d2H, v, e0, steps=200)
+    Hd = orc.hamiltonian(N, qu, qd, terms, terms, U).toarray()
+    w, V = np.linalg.eigh(Hd)
+    assert w[1] - w[0] > 1e-6
+    g = V[:, 0]
+    A1 = orc.hamiltonian(N, qu, qd, d1t, d1t, 0.0).toarray()
+    A2 = orc.hamiltonian(N, qu, qd, d2t, d2t, 0.0).toarray()
+    m = V.conj().T @ (A1 @ g)
+    exact1 = float(np.real(np.vdot(g, A1 @ g)))
+    exact2 = float(np.real(np.vdot(g, A2 @ g)) - 2 * np.sum(np.abs(m[1:]) ** 2 / (w[1:] - w[0])))
+    assert abs(e0 - w[0]) < 1e-10 * max(1.0, abs(w[0]))
+    assert abs(first - exact1) < 1e-9 * max(1.0, abs(exact1))
+    assert abs(second - exact2) < 1e-8 * max(1.0, abs(exact2))
+
+
 @pytest.mark.parametrize("case", ["chain8_35", "kagome12_54", "kagome12_22_flux"])
 def test_s2_apply_matches_oracle(ed, orc, case):
     """ed_s2_apply (TotalSpin::Hubbard::Hubbard_mv) against the restated
