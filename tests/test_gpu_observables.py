@@ -237,6 +237,23 @@ def test_flux_response_on_degenerate_sectors(ed, orc, qu, qd):
     assert abs(second - exact2) < 1e-8 * max(1.0, abs(exact2))
 
 
+@pytest.mark.parametrize("qu,qd", [(0, 6), (6, 0), (12, 6), (6, 12)])
+def test_s2_on_polarised_sectors(ed, qu, qd):
+    """With one species empty or full every state of the sector has the
+    largest spin, S = |N_up - N_dn| / 2 = 3: S^2 = 12 and S_xy = S^2 - S_z^2
+    = 3 on any vector (S_xy x = 3 x)."""
+    from exact_diagonalization_for_fermionic_systems_with_gpu_gb300 import lattices as L, observables as ob
+    t = L.chain(12, periodic=False)
+    op = ed.Hubbard(ed.H_TBq(12, qu).extend(t), ed.H_TBq(12, qd).extend(t), 2.0)
+    x = philox_uniform(21, op.rows())
+    x /= np.linalg.norm(x)
+    y = ob.s2_apply(op, x)
+    assert np.max(np.abs(y - 3.0 * x)) < 1e-13
+    sxy, s2 = ob.s2_expect(op, x)
+    assert abs(sxy - 3.0) < 1e-12 and abs(s2 - 12.0) < 1e-12
+    op.close()
+
+
 @pytest.mark.parametrize("case", ["chain8_35", "kagome12_54", "kagome12_22_flux"])
 def test_s2_apply_matches_oracle(ed, orc, case):
     """ed_s2_apply (TotalSpin::Hubbard::Hubbard_mv) against the restated
